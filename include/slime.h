@@ -1,0 +1,267 @@
+/*
+ * slime.h - C ABI of the GB300 Physarum core.
+ *
+ * The reference (Velfi/slime-mold) runs one simulation step as three wgpu
+ * compute dispatches from its event loop (src/main.rs:1163-1235):
+ *   "main"          agents: sense, turn, move, deposit   (src/compute.wgsl:57-145)
+ *   "decay_trail"   trail decay                          (src/compute.wgsl:148-161)
+ *   "diffuse_trail" 3x3 toroidal blur                    (src/compute.wgsl:164-195)
+ * built by PipelineManager (src/pipeline_manager.rs:37-54) over one bind group
+ * {0: agents vec4<f32>, 1: trail f32, 2: SimSizeUniform}
+ * (src/bind_group_manager.rs:101-125).  This library replaces those three
+ * pipelines, their bind group and the dispatch code with one context object
+ * that owns the agent and trail buffers on one GPU and advances them with two
+ * CUDA kernels per step (agents; fused deposit+decay+diffuse), captured in a
+ * CUDA graph.
+ *
+ * Conventions:
+ *   - every function returns an int status (SLIME_OK = 0, negative = error)
+ *     unless stated; slime_last_error() gives a message for the last failure;
+ *   - host pointers belong to the caller and are only read/written during the
+ *     call (the call synchronises with the context's stream before returning);
+ *   - agents cross the ABI as the reference's AoS layout, 4 floats per agent
+ *     (x, y, angle, speed) in agent-id order (src/main.rs:263-282); trails as
+ *     width*height floats, row-major (src/main.rs:285-293);
+ *   - one context is used from one host thread at a time (like the winit event
+ *     loop thread); distinct contexts are independent.
+ *
+ * Semantics where the reference has data races (documented deviations):
+ *   - sensing reads the trail as it was at the start of the step (the shader
+ *     reads a buffer that other invocations are depositing into);
+ *   - the k deposits that land in a cell in one step are applied as the
+ *     sequential fold t <- clamp(t + deposition, 0, 1), k times (the shader's
+ *     non-atomic read-modify-write at compute.wgsl:140 loses updates);
+ *   - decay and diffuse read one buffer and write another (the shader blurs in
+ *     place);
+ *   - every agent is updated exactly once per step (the shader's index
+ *     gid.x + gid.y*65535 at compute.wgsl:60 leaves agents above 4,194,240
+ *     frozen and updates some low indices several times).
+ */
+#ifndef SLIME_H
+#define SLIME_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+#define SLIME_OK 0
+#define SLIME_ERR_INVALID_ARGUMENT (-1)
+#define SLIME_ERR_OUT_OF_MEMORY (-2)
+#define SLIME_ERR_CUDA (-3)
+#define SLIME_ERR_STATE (-4)          /* call not valid in the current state */
+#define SLIME_ERR_DEVICE_TIMEOUT (-5) /* a bounded device-side wait gave up */
+#define SLIME_ERR_NO_DEVICE (-6)
+
+/* ------------------------------------------------------------ modes */
+/* Trail decay (compute.wgsl:159-160 is the subtractive form). */
+#define SLIME_DECAY_REF_SUBTRACT 0u /* t = max(t - decay_factor * 0.001, 0) */
+#define SLIME_DECAY_MULTIPLY 1u     /* t = t * decay_factor */
+/* Trail blur (compute.wgsl:175-194 is the 3x3 box). */
+#define SLIME_BLUR_REF_BOX3 0u /* 3x3 toroidal box, summed in shader order, /9 */
+#define SLIME_BLUR_GAUSS 1u    /* separable Gaussian, radius blur_radius, sigma blur_sigma */
+#define SLIME_MAX_BLUR_RADIUS 8
+
+/* ------------------------------------------------------------ parameters */
+/* The first 14 fields are SimSizeUniform (src/main.rs:29-46) in the same
+ * order and layout (56 bytes); the rest extend it with what the shader hard
+ * codes.  width/height must be 0 or equal to the context's trail size. */
+typedef struct SlimeParams {
+    uint32_t width;
+    uint32_t height;
+    float decay_factor;
+    float agent_jitter;
+    float agent_speed_min;
+    float agent_speed_max;
+    float agent_turn_speed;
+    float agent_sensor_angle;
+    float agent_sensor_distance;
+    float diffusion_rate;
+    float pheromone_deposition_amount;
+    float blur_radius;
+    float blur_sigma;
+    uint32_t _pad;
+    /* extensions */
+    float time_step;     /* TIME_STEP, compute.wgsl:55 (0.016) */
+    uint32_t decay_mode; /* SLIME_DECAY_* */
+    uint32_t blur_mode;  /* SLIME_BLUR_* */
+    uint32_t reserved;   /* must be 0 */
+} SlimeParams;
+
+/* Settings (src/settings.rs:30-47), field for field. */
+typedef struct SlimeSettings {
+    uint64_t agent_count;
+    float agent_jitter;
+    float agent_possible_starting_headings_start;
+    float agent_possible_starting_headings_end;
+    float agent_speed_max;
+    float agent_speed_min;
+    float agent_turn_speed;
+    float pheromone_decay_factor;
+    float pheromone_diffusion_rate;
+    float pheromone_deposition_amount;
+    uint32_t window_fullscreen;
+    uint32_t window_height;
+    uint32_t window_width;
+    float agent_sensor_angle;
+    float agent_sensor_distance;
+    float blur_radius;
+    float blur_sigma;
+} SlimeSettings;
+
+/* Engine options (no counterpart in the reference). */
+typedef struct SlimeOptions {
+    uint32_t use_graphs;        /* 1: capture step chunks in CUDA graphs (default 1) */
+    uint32_t graph_chunk;       /* steps per captured graph (default 50) */
+    uint32_t reorder_every;     /* Morton-reorder agents every k steps, 0 = never (default 0) */
+    uint32_t reorder_cell_log2; /* Morton key granularity, log2 of a square of cells (default 2) */
+    uint32_t l2_persist;        /* 1: persisting-L2 access window over the sensed trail (default 1) */
+    uint32_t trail_tile;        /* 0: autotuned/default, otherwise an index into the tile table */
+    uint32_t reserved[2];
+} SlimeOptions;
+
+typedef struct SlimeInfo {
+    uint32_t width;
+    uint32_t height;
+    uint64_t n_agents;
+    uint64_t steps_done;
+    uint64_t kernel_launches; /* kernels enqueued by this context (graph nodes count) */
+    uint32_t trail_tile;      /* tile-table index in use */
+    uint32_t reordered;       /* 1 if device agent order differs from id order */
+} SlimeInfo;
+
+const char* slime_version(void);
+const char* slime_status_string(int status);
+
+/* ------------------------------------------------ settings and presets */
+/* Settings::default() (src/settings.rs:49-70). */
+void slime_settings_default(SlimeSettings* out);
+/* The preset table of init_preset_manager() (src/presets.rs:45-155). */
+int slime_preset_count(void);
+/* PresetManager::get_preset_names / get_preset by position; *name is static. */
+int slime_preset_get(int index, const char** name, SlimeSettings* out);
+/* PresetManager::get_preset(name) (src/presets.rs:30-32). */
+int slime_preset_find(const char* name, SlimeSettings* out);
+/* SimSizeUniform::new(width, height, settings.pheromone_decay_factor, settings)
+ * (src/main.rs:48-66) plus the reference's defaults for the extensions. */
+void slime_params_from_settings(const SlimeSettings* settings, uint32_t width, uint32_t height,
+                                SlimeParams* out);
+
+/* ------------------------------------------------ simulation context */
+typedef struct slime_ctx slime_ctx;
+
+/* Allocates agents (zeroed) and a zeroed trail on the current CUDA device and
+ * installs the default settings' parameters.  Replaces buffer creation at
+ * src/main.rs:263-293, PipelineManager::new and BindGroupManager::new. */
+slime_ctx* slime_create(uint32_t width, uint32_t height, uint64_t n_agents, int* status);
+void slime_destroy(slime_ctx* ctx);
+const char* slime_last_error(const slime_ctx* ctx);
+
+/* queue.write_buffer of the uniform (update_settings, src/main.rs:83-99). */
+int slime_set_params(slime_ctx* ctx, const SlimeParams* params);
+int slime_get_params(const slime_ctx* ctx, SlimeParams* out);
+int slime_set_options(slime_ctx* ctx, const SlimeOptions* options);
+int slime_get_options(const slime_ctx* ctx, SlimeOptions* out);
+int slime_get_info(const slime_ctx* ctx, SlimeInfo* out);
+
+/* Agent buffer writes/reads (src/main.rs:263-282 layout; readback as at
+ * src/main.rs:126-131). n must equal the context's agent count. */
+int slime_upload_agents(slime_ctx* ctx, const float* aos_xyzw, uint64_t n);
+int slime_download_agents(slime_ctx* ctx, float* aos_xyzw, uint64_t n);
+/* Seeded replacement of the unseeded host init (src/main.rs:273-280):
+ * x ~ U[0,w), y ~ U[0,h), angle ~ U[heading_min, heading_max),
+ * speed ~ U[speed_min, speed_max] of the current parameters. */
+int slime_seed_agents(slime_ctx* ctx, uint64_t seed, float heading_min, float heading_max);
+/* reassign_agent_speeds (src/main.rs:101-145), on the device, seeded. */
+int slime_reassign_speeds(slime_ctx* ctx, uint64_t seed);
+
+int slime_upload_trail(slime_ctx* ctx, const float* trail, uint64_t n_cells);
+int slime_download_trail(slime_ctx* ctx, float* trail, uint64_t n_cells);
+/* Trail clear on key C (src/main.rs:909-913). */
+int slime_clear_trail(slime_ctx* ctx);
+/* Window resize (src/main.rs:954-1015): agent x,y are scaled by new/old size,
+ * the trail is reallocated zeroed. */
+int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height);
+/* Agent-count change (src/main.rs:682-791): reallocates the agent buffer and
+ * seeds every agent anew (seeded; the reference uses rand::random). */
+int slime_set_agent_count(slime_ctx* ctx, uint64_t n_agents, uint64_t seed);
+
+/* Advance n_steps steps: the agent dispatch, the decay dispatch and the
+ * diffuse dispatch of src/main.rs:1163-1235, n_steps times.  Asynchronous with
+ * respect to the host; use slime_sync or any download to wait. */
+int slime_step(slime_ctx* ctx, uint32_t n_steps);
+int slime_sync(slime_ctx* ctx);
+/* The cudaStream_t the context enqueues on. */
+int slime_get_stream(slime_ctx* ctx, void** stream);
+/* Deposit counts of the most recent step (cells receiving k agents hold k). */
+int slime_download_deposit_counts(slime_ctx* ctx, uint32_t* counts, uint64_t n_cells);
+/* Reorder agents in Morton order of their cell now (results are unchanged:
+ * every agent keeps its id, which seeds its jitter hash). */
+int slime_reorder_agents(slime_ctx* ctx);
+
+/* Run n_steps steps without graphs, timing each kernel with CUDA events on
+ * the context's stream; totals in milliseconds (NULL outputs are skipped). */
+int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, double* trail_ms,
+                        double* other_ms);
+/* Pick the fastest trail tile for this context's size by timing each
+ * candidate (the trail state is restored afterwards). */
+int slime_autotune(slime_ctx* ctx, uint32_t reps);
+
+/* ------------------------------------------------ adjoint (frozen trajectories) */
+/* Gradients of a scalar trail loss L(T_final) with respect to the trail-chain
+ * parameters, holding the recorded agent trajectories (hence the per-step
+ * deposit counts) fixed. */
+typedef struct SlimeGrads {
+    double d_decay_factor;
+    double d_diffusion_rate;
+    double d_deposition_amount;
+    double reserved;
+} SlimeGrads;
+
+/* Run n_steps forward steps from the current state, keeping a checkpoint of
+ * agents and trail every ckpt_every steps in device memory. */
+int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every);
+/* Back-propagate dL/dT_final (host, width*height floats) through the recorded
+ * steps, recomputing each checkpoint segment; writes the parameter gradients
+ * and, if d_trail0 is not NULL, dL/dT_0 (host, width*height floats). */
+int slime_backward(slime_ctx* ctx, const float* dl_dtrail_final, SlimeGrads* grads, float* d_trail0);
+
+/* ------------------------------------------------ batched ensemble */
+/* Independent colonies of uneven sizes advanced together: one launch per
+ * step covers every colony. */
+typedef struct slime_ensemble slime_ensemble;
+
+slime_ensemble* slime_ensemble_create(uint32_t n_colonies, const uint32_t* widths,
+                                      const uint32_t* heights, const uint64_t* n_agents,
+                                      const SlimeParams* params, int* status);
+void slime_ensemble_destroy(slime_ensemble* ens);
+const char* slime_ensemble_last_error(const slime_ensemble* ens);
+int slime_ensemble_set_params(slime_ensemble* ens, uint32_t colony, const SlimeParams* params);
+int slime_ensemble_upload_agents(slime_ensemble* ens, uint32_t colony, const float* aos_xyzw, uint64_t n);
+int slime_ensemble_download_agents(slime_ensemble* ens, uint32_t colony, float* aos_xyzw, uint64_t n);
+int slime_ensemble_seed_agents(slime_ensemble* ens, uint32_t colony, uint64_t seed, float heading_min,
+                               float heading_max);
+int slime_ensemble_upload_trail(slime_ensemble* ens, uint32_t colony, const float* trail, uint64_t n_cells);
+int slime_ensemble_download_trail(slime_ensemble* ens, uint32_t colony, float* trail, uint64_t n_cells);
+int slime_ensemble_step(slime_ensemble* ens, uint32_t n_steps);
+int slime_ensemble_sync(slime_ensemble* ens);
+int slime_ensemble_get_stream(slime_ensemble* ens, void** stream);
+int slime_ensemble_autotune(slime_ensemble* ens, uint32_t reps);
+/* Total kernels enqueued so far. */
+int slime_ensemble_launch_count(const slime_ensemble* ens, uint64_t* out);
+
+/* ------------------------------------------------ display feed */
+/* Headless equivalent of src/display.wgsl:44-86: colourise the current trail
+ * through a 256-entry LUT (768 bytes: R[256] G[256] B[256], the .lut format)
+ * into an RGBA8 image of tex_width x tex_height with the same aspect fit. */
+int slime_colorize(slime_ctx* ctx, const uint8_t* lut768, uint32_t tex_width, uint32_t tex_height,
+                   uint8_t* rgba_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLIME_H */

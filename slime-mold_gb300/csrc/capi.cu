@@ -1,0 +1,720 @@
+// capi.cu - the C ABI of include/slime.h for one simulation context.
+//
+// Replaces the reference's PipelineManager (src/pipeline_manager.rs:19-113),
+// BindGroupManager (src/bind_group_manager.rs:13-125) and the per-frame
+// dispatch code (src/main.rs:1163-1235).  A context owns, on one GPU:
+//   agents   SoA x/y/angle/speed (+ slot->id map once reordered)
+//   trail[2] ping-pong binary32 trails (trail[cur] is the state)
+//   counts[2] per-cell deposit counters: counts[cur] collects the next step's
+//            deposits (kept zero between steps), counts[1-cur] holds the
+//            previous step's
+// and enqueues everything on its own stream.  Steps are captured in CUDA
+// graphs of `graph_chunk` steps, one per starting parity, and replayed.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <string>
+#include <utility>
+
+#include "ctx.h"
+
+using namespace slime;
+
+namespace slime {
+
+bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* out, const char** why) {
+    const float fs[] = {p.decay_factor, p.agent_jitter, p.agent_speed_min, p.agent_speed_max,
+                        p.agent_turn_speed, p.agent_sensor_angle, p.agent_sensor_distance, p.diffusion_rate,
+                        p.pheromone_deposition_amount, p.time_step};
+    for (float f : fs)
+        if (!isfinite(f)) {
+            *why = "parameters must be finite (NaN/inf rejected)";
+            return false;
+        }
+    if (p.width != 0 && p.width != W) {
+        *why = "params.width must be 0 or the context's width";
+        return false;
+    }
+    if (p.height != 0 && p.height != H) {
+        *why = "params.height must be 0 or the context's height";
+        return false;
+    }
+    if (p.decay_mode > SLIME_DECAY_MULTIPLY) {
+        *why = "unknown decay_mode";
+        return false;
+    }
+    if (p.blur_mode > SLIME_BLUR_GAUSS) {
+        *why = "unknown blur_mode";
+        return false;
+    }
+    if (p.reserved != 0) {
+        *why = "params.reserved must be 0";
+        return false;
+    }
+    DevParams d;
+    memset(&d, 0, sizeof(d));
+    d.W = (int32_t)W;
+    d.H = (int32_t)H;
+    d.Wf = (float)W;
+    d.Hf = (float)H;
+    d.speed_min = p.agent_speed_min;
+    d.speed_max = p.agent_speed_max;
+    d.turn = p.agent_turn_speed;
+    d.sensor_angle = p.agent_sensor_angle;
+    d.sensor_dist = p.agent_sensor_distance;
+    d.jitter = p.agent_jitter;
+    d.time_step = p.time_step;
+    d.dep = p.pheromone_deposition_amount;
+    d.decay = p.decay_factor;
+    d.decay_k = slm_mul(p.decay_factor, 0.001f);          // compute.wgsl:159
+    d.rate = slm_clamp(p.diffusion_rate, 0.0f, 1.0f);     // compute.wgsl:173
+    d.decay_mode = p.decay_mode;
+    d.blur_mode = p.blur_mode;
+    d.R = 1;
+    if (p.blur_mode == SLIME_BLUR_GAUSS) {
+        if (!isfinite(p.blur_radius) || !isfinite(p.blur_sigma)) {
+            *why = "blur_radius and blur_sigma must be finite";
+            return false;
+        }
+        d.R = slm_gauss_radius(p.blur_radius, kMaxR);
+        if (slm_gauss_weights(d.R, p.blur_sigma, d.w) != 0) {
+            *why = "blur_sigma must be > 0 in Gaussian mode";
+            return false;
+        }
+    }
+    *out = d;
+    return true;
+}
+
+int set_error(std::string& err, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+}
+
+int cuda_error(std::string& err, cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return set_error(err, SLIME_ERR_OUT_OF_MEMORY, "%s: out of device memory", what);
+    }
+    return set_error(err, SLIME_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+} // namespace slime
+
+#define CK(expr, what)                                                                                      \
+    do {                                                                                                    \
+        cudaError_t _e = (expr);                                                                            \
+        if (_e != cudaSuccess) return cuda_error(ctx->err, _e, what);                                       \
+    } while (0)
+
+namespace {
+
+void free_agents(slime_ctx* ctx) {
+    if (ctx->agent_block) cudaFree(ctx->agent_block);
+    if (ctx->ids_storage) cudaFree(ctx->ids_storage);
+    ctx->agent_block = nullptr;
+    ctx->ids_storage = nullptr;
+    ctx->agents = AgentsSoA();
+}
+
+void free_trail(slime_ctx* ctx) {
+    for (int i = 0; i < 2; i++) {
+        if (ctx->trail[i]) cudaFree(ctx->trail[i]);
+        if (ctx->counts[i]) cudaFree(ctx->counts[i]);
+        ctx->trail[i] = nullptr;
+        ctx->counts[i] = nullptr;
+    }
+}
+
+int alloc_agents(slime_ctx* ctx, uint64_t n) {
+    free_agents(ctx);
+    uint64_t n_pad = (n + kAgentPad - 1) / kAgentPad * kAgentPad;
+    if (n_pad == 0) n_pad = kAgentPad;
+    size_t bytes = 4 * n_pad * sizeof(float);
+    CK(cudaMalloc(&ctx->agent_block, bytes), "allocating agents");
+    CK(cudaMemsetAsync(ctx->agent_block, 0, bytes, ctx->stream), "clearing agents");
+    float* b = (float*)ctx->agent_block;
+    ctx->agents.x = b;
+    ctx->agents.y = b + n_pad;
+    ctx->agents.th = b + 2 * n_pad;
+    ctx->agents.v = b + 3 * n_pad;
+    ctx->agents.ids = nullptr;
+    ctx->agents.n = n;
+    ctx->agents.n_pad = n_pad;
+    return SLIME_OK;
+}
+
+int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
+    free_trail(ctx);
+    size_t cells = (size_t)W * H;
+    for (int i = 0; i < 2; i++) {
+        CK(cudaMalloc(&ctx->trail[i], cells * sizeof(float)), "allocating trail");
+        CK(cudaMalloc(&ctx->counts[i], cells * sizeof(uint32_t)), "allocating deposit counts");
+        CK(cudaMemsetAsync(ctx->trail[i], 0, cells * sizeof(float), ctx->stream), "clearing trail");
+        CK(cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream), "clearing counts");
+    }
+    ctx->cur = 0;
+    ctx->last_counts_valid = false;
+    return SLIME_OK;
+}
+
+int ensure_staging(slime_ctx* ctx, size_t bytes) {
+    if (ctx->staging_bytes >= bytes) return SLIME_OK;
+    if (ctx->staging) cudaFree(ctx->staging);
+    ctx->staging = nullptr;
+    ctx->staging_bytes = 0;
+    CK(cudaMalloc(&ctx->staging, bytes), "allocating staging buffer");
+    ctx->staging_bytes = bytes;
+    return SLIME_OK;
+}
+
+// Put every agent back in id order relative to the slot->id map: after an
+// upload or a seed, slot i holds agent i.
+int reset_ids(slime_ctx* ctx) {
+    if (ctx->agents.ids) CK(launch_iota(ctx->agents.ids, ctx->agents.n, ctx->stream), "resetting agent ids");
+    ctx->reordered = false;
+    return SLIME_OK;
+}
+
+int valid_size(std::string& err, uint32_t W, uint32_t H, uint64_t n) {
+    if (W < 1 || H < 1) return set_error(err, SLIME_ERR_INVALID_ARGUMENT, "trail size must be at least 1x1");
+    if (W > (1u << 24) || H > (1u << 24))
+        return set_error(err, SLIME_ERR_INVALID_ARGUMENT, "trail sides must be <= 2^24 (exact in binary32)");
+    if ((uint64_t)W * H >= (1ull << 31))
+        return set_error(err, SLIME_ERR_INVALID_ARGUMENT, "width*height must be < 2^31 (the shader's i32 index)");
+    if (n >= (1ull << 31))
+        return set_error(err, SLIME_ERR_INVALID_ARGUMENT, "agent count must be < 2^31 (the shader's i32 index)");
+    return SLIME_OK;
+}
+
+} // namespace
+
+namespace slime {
+
+void invalidate_graphs(slime_ctx* ctx) {
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+}
+
+// Enqueue one step on the context's stream (also used under capture).
+cudaError_t enqueue_step(slime_ctx* ctx) {
+    const int cur = ctx->cur;
+    cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream);
+    if (e != cudaSuccess) return e;
+    e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
+                     ctx->counts[1 - cur], ctx->stream);
+    if (e != cudaSuccess) return e;
+    ctx->cur = 1 - cur;
+    return cudaSuccess;
+}
+
+uint64_t kernels_per_step(const slime_ctx* ctx) { return ctx->agents.n ? 2 : 1; }
+
+int run_steps_direct(slime_ctx* ctx, uint32_t m) {
+    for (uint32_t i = 0; i < m; i++) {
+        CK(enqueue_step(ctx), "launching a step");
+        ctx->launches += kernels_per_step(ctx);
+        ctx->steps_done++;
+    }
+    ctx->last_counts_valid = true;
+    return SLIME_OK;
+}
+
+int run_steps_graph(slime_ctx* ctx, uint32_t m) {
+    auto key = std::make_pair(m, ctx->cur);
+    auto it = ctx->graphs.find(key);
+    cudaGraphExec_t exec = nullptr;
+    if (it == ctx->graphs.end()) {
+        const int saved = ctx->cur;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "beginning graph capture");
+        cudaError_t ce = cudaSuccess;
+        for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_step(ctx);
+        cudaGraph_t graph = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(ctx->stream, &graph);
+        ctx->cur = saved;
+        if (ce != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return cuda_error(ctx->err, ce, "capturing steps");
+        }
+        CK(ee, "ending graph capture");
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(ie, "instantiating step graph");
+        ctx->graphs[key] = exec;
+    } else {
+        exec = it->second;
+    }
+    CK(cudaGraphLaunch(exec, ctx->stream), "launching step graph");
+    ctx->cur = (m & 1) ? 1 - ctx->cur : ctx->cur;
+    ctx->launches += kernels_per_step(ctx) * m;
+    ctx->steps_done += m;
+    ctx->last_counts_valid = true;
+    return SLIME_OK;
+}
+
+int do_reorder(slime_ctx* ctx) {
+    if (ctx->agents.n == 0) return SLIME_OK;
+    if (!ctx->agents.ids) {
+        CK(cudaMalloc(&ctx->ids_storage, ctx->agents.n_pad * sizeof(uint32_t)), "allocating agent ids");
+        CK(cudaMemsetAsync(ctx->ids_storage, 0, ctx->agents.n_pad * sizeof(uint32_t), ctx->stream),
+           "clearing agent ids");
+        ctx->agents.ids = ctx->ids_storage;
+        CK(launch_iota(ctx->agents.ids, ctx->agents.n, ctx->stream), "initialising agent ids");
+        invalidate_graphs(ctx); // the agent kernel now reads ids
+    }
+    CK(launch_reorder(ctx->agents, ctx->W, ctx->H, (int)ctx->opt.reorder_cell_log2, ctx->reorder, ctx->stream),
+       "reordering agents");
+    ctx->launches += 5;
+    ctx->reordered = true;
+    ctx->last_reorder_step = ctx->steps_done;
+    return SLIME_OK;
+}
+
+int run_steps(slime_ctx* ctx, uint32_t n) {
+    int rc;
+    while (n > 0) {
+        uint32_t m = n;
+        if (ctx->opt.reorder_every) {
+            if (ctx->steps_done % ctx->opt.reorder_every == 0 && ctx->last_reorder_step != ctx->steps_done)
+                if ((rc = do_reorder(ctx)) != SLIME_OK) return rc;
+            uint64_t to_next = ctx->opt.reorder_every - ctx->steps_done % ctx->opt.reorder_every;
+            if (to_next < m) m = (uint32_t)to_next;
+        }
+        if (ctx->opt.use_graphs) {
+            uint32_t chunk = ctx->opt.graph_chunk ? ctx->opt.graph_chunk : 50;
+            uint32_t take = m < chunk ? m : chunk;
+            if ((rc = run_steps_graph(ctx, take)) != SLIME_OK) return rc;
+            n -= take;
+        } else {
+            if ((rc = run_steps_direct(ctx, m)) != SLIME_OK) return rc;
+            n -= m;
+        }
+    }
+    return SLIME_OK;
+}
+
+} // namespace slime
+
+extern "C" {
+
+const char* slime_version(void) { return "slime-gb300 0.1 (sm_103a)"; }
+
+const char* slime_status_string(int status) {
+    switch (status) {
+    case SLIME_OK: return "ok";
+    case SLIME_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case SLIME_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case SLIME_ERR_CUDA: return "CUDA error";
+    case SLIME_ERR_STATE: return "invalid state";
+    case SLIME_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case SLIME_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+slime_ctx* slime_create(uint32_t width, uint32_t height, uint64_t n_agents, int* status) {
+    std::string err;
+    int dummy;
+    if (!status) status = &dummy;
+    if ((*status = valid_size(err, width, height, n_agents)) != SLIME_OK) return nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        *status = SLIME_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    slime_ctx* ctx = new slime_ctx();
+    cudaGetDevice(&ctx->device);
+    ctx->W = width;
+    ctx->H = height;
+    ctx->opt.use_graphs = 1;
+    ctx->opt.graph_chunk = 50;
+    ctx->opt.reorder_every = 0;
+    ctx->opt.reorder_cell_log2 = 2;
+    ctx->opt.l2_persist = 1;
+    ctx->opt.trail_tile = 0;
+    ctx->tile = trail_tile_default();
+    int rc = SLIME_OK;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        rc = SLIME_ERR_CUDA;
+    } else if ((rc = alloc_agents(ctx, n_agents)) == SLIME_OK && (rc = alloc_trail(ctx, width, height)) == SLIME_OK) {
+        SlimeSettings s;
+        slime_settings_default(&s);
+        slime_params_from_settings(&s, width, height, &ctx->params);
+        const char* why = nullptr;
+        if (!make_dev_params(ctx->params, width, height, &ctx->dev, &why)) rc = SLIME_ERR_INVALID_ARGUMENT;
+        else if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = SLIME_ERR_CUDA;
+    }
+    if (rc != SLIME_OK) {
+        slime_destroy(ctx);
+        *status = rc;
+        return nullptr;
+    }
+    *status = SLIME_OK;
+    return ctx;
+}
+
+void slime_destroy(slime_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    invalidate_graphs(ctx);
+    free_adjoint(ctx);
+    free_agents(ctx);
+    free_trail(ctx);
+    if (ctx->staging) cudaFree(ctx->staging);
+    if (ctx->reorder.buf) cudaFree(ctx->reorder.buf);
+    if (ctx->aux) cudaFree(ctx->aux);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* slime_last_error(const slime_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int slime_set_params(slime_ctx* ctx, const SlimeParams* params) {
+    if (!ctx || !params) return SLIME_ERR_INVALID_ARGUMENT;
+    DevParams d;
+    const char* why = nullptr;
+    if (!make_dev_params(*params, ctx->W, ctx->H, &d, &why))
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "%s", why);
+    ctx->params = *params;
+    ctx->params.width = ctx->W;
+    ctx->params.height = ctx->H;
+    if (memcmp(&d, &ctx->dev, sizeof d) != 0) {
+        ctx->dev = d;
+        invalidate_graphs(ctx); // the parameter block is baked into the captured launches
+    }
+    return SLIME_OK;
+}
+
+int slime_get_params(const slime_ctx* ctx, SlimeParams* out) {
+    if (!ctx || !out) return SLIME_ERR_INVALID_ARGUMENT;
+    *out = ctx->params;
+    return SLIME_OK;
+}
+
+int slime_set_options(slime_ctx* ctx, const SlimeOptions* o) {
+    if (!ctx || !o) return SLIME_ERR_INVALID_ARGUMENT;
+    if (o->trail_tile > (uint32_t)trail_tile_count())
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "trail_tile out of range (0..%d)",
+                         trail_tile_count());
+    if (o->reorder_cell_log2 > 15)
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "reorder_cell_log2 must be <= 15");
+    ctx->opt = *o;
+    if (ctx->opt.graph_chunk == 0) ctx->opt.graph_chunk = 50;
+    int tile = o->trail_tile ? (int)o->trail_tile - 1 : (ctx->tuned_tile >= 0 ? ctx->tuned_tile : trail_tile_default());
+    if (tile != ctx->tile) {
+        ctx->tile = tile;
+        invalidate_graphs(ctx);
+    }
+    return SLIME_OK;
+}
+
+int slime_get_options(const slime_ctx* ctx, SlimeOptions* out) {
+    if (!ctx || !out) return SLIME_ERR_INVALID_ARGUMENT;
+    *out = ctx->opt;
+    return SLIME_OK;
+}
+
+int slime_get_info(const slime_ctx* ctx, SlimeInfo* out) {
+    if (!ctx || !out) return SLIME_ERR_INVALID_ARGUMENT;
+    out->width = ctx->W;
+    out->height = ctx->H;
+    out->n_agents = ctx->agents.n;
+    out->steps_done = ctx->steps_done;
+    out->kernel_launches = ctx->launches;
+    out->trail_tile = (uint32_t)ctx->tile;
+    out->reordered = ctx->reordered ? 1u : 0u;
+    return SLIME_OK;
+}
+
+int slime_upload_agents(slime_ctx* ctx, const float* aos, uint64_t n) {
+    if (!ctx || (!aos && n)) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (n != ctx->agents.n)
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "agent count %llu != context's %llu",
+                         (unsigned long long)n, (unsigned long long)ctx->agents.n);
+    if (n == 0) return SLIME_OK;
+    int rc;
+    if ((rc = ensure_staging(ctx, n * sizeof(float4))) != SLIME_OK) return rc;
+    CK(cudaMemcpyAsync(ctx->staging, aos, n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream), "uploading agents");
+    CK(launch_aos_to_soa((const float4*)ctx->staging, ctx->agents, ctx->stream), "converting agents");
+    if ((rc = reset_ids(ctx)) != SLIME_OK) return rc;
+    CK(cudaStreamSynchronize(ctx->stream), "uploading agents");
+    return SLIME_OK;
+}
+
+int slime_download_agents(slime_ctx* ctx, float* aos, uint64_t n) {
+    if (!ctx || (!aos && n)) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (n != ctx->agents.n)
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "agent count %llu != context's %llu",
+                         (unsigned long long)n, (unsigned long long)ctx->agents.n);
+    if (n == 0) return SLIME_OK;
+    int rc;
+    if ((rc = ensure_staging(ctx, n * sizeof(float4))) != SLIME_OK) return rc;
+    CK(launch_soa_to_aos(ctx->agents, (float4*)ctx->staging, ctx->stream), "converting agents");
+    CK(cudaMemcpyAsync(aos, ctx->staging, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream), "downloading agents");
+    CK(cudaStreamSynchronize(ctx->stream), "downloading agents");
+    return SLIME_OK;
+}
+
+int slime_seed_agents(slime_ctx* ctx, uint64_t seed, float hmin, float hmax) {
+    if (!ctx || !isfinite(hmin) || !isfinite(hmax)) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    CK(launch_seed_agents(ctx->agents, seed, (float)ctx->W, (float)ctx->H, hmin, hmax, ctx->params.agent_speed_min,
+                          ctx->params.agent_speed_max, ctx->stream),
+       "seeding agents");
+    int rc;
+    if ((rc = reset_ids(ctx)) != SLIME_OK) return rc;
+    CK(cudaStreamSynchronize(ctx->stream), "seeding agents");
+    return SLIME_OK;
+}
+
+int slime_reassign_speeds(slime_ctx* ctx, uint64_t seed) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    CK(launch_reassign_speeds(ctx->agents, seed, ctx->params.agent_speed_min, ctx->params.agent_speed_max, ctx->stream),
+       "reassigning speeds");
+    CK(cudaStreamSynchronize(ctx->stream), "reassigning speeds");
+    return SLIME_OK;
+}
+
+int slime_upload_trail(slime_ctx* ctx, const float* trail, uint64_t n_cells) {
+    if (!ctx || !trail) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (n_cells != (uint64_t)ctx->W * ctx->H)
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "trail has %llu cells, context has %llu",
+                         (unsigned long long)n_cells, (unsigned long long)ctx->W * ctx->H);
+    CK(cudaMemcpyAsync(ctx->trail[ctx->cur], trail, n_cells * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+       "uploading trail");
+    CK(cudaStreamSynchronize(ctx->stream), "uploading trail");
+    return SLIME_OK;
+}
+
+int slime_download_trail(slime_ctx* ctx, float* trail, uint64_t n_cells) {
+    if (!ctx || !trail) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (n_cells != (uint64_t)ctx->W * ctx->H)
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "trail has %llu cells, context has %llu",
+                         (unsigned long long)n_cells, (unsigned long long)ctx->W * ctx->H);
+    CK(cudaMemcpyAsync(trail, ctx->trail[ctx->cur], n_cells * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+       "downloading trail");
+    CK(cudaStreamSynchronize(ctx->stream), "downloading trail");
+    return SLIME_OK;
+}
+
+int slime_clear_trail(slime_ctx* ctx) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    CK(cudaMemsetAsync(ctx->trail[ctx->cur], 0, (size_t)ctx->W * ctx->H * sizeof(float), ctx->stream), "clearing trail");
+    CK(cudaStreamSynchronize(ctx->stream), "clearing trail");
+    return SLIME_OK;
+}
+
+int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    int rc;
+    if ((rc = valid_size(ctx->err, width, height, ctx->agents.n)) != SLIME_OK) return rc;
+    SlimeParams np = ctx->params;
+    np.width = width;
+    np.height = height;
+    DevParams d;
+    const char* why = nullptr;
+    if (!make_dev_params(np, width, height, &d, &why)) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "%s", why);
+    // src/main.rs:987-993: scale = new / old as f32 division.
+    float sx = slm_div((float)width, (float)ctx->W);
+    float sy = slm_div((float)height, (float)ctx->H);
+    CK(launch_scale_positions(ctx->agents, sx, sy, ctx->stream), "scaling agent positions");
+    CK(cudaStreamSynchronize(ctx->stream), "resizing");
+    invalidate_graphs(ctx);
+    free_adjoint(ctx);
+    if ((rc = alloc_trail(ctx, width, height)) != SLIME_OK) return rc;
+    ctx->W = width;
+    ctx->H = height;
+    ctx->params = np;
+    ctx->dev = d;
+    ctx->tuned_tile = -1;
+    CK(cudaStreamSynchronize(ctx->stream), "resizing");
+    return SLIME_OK;
+}
+
+int slime_set_agent_count(slime_ctx* ctx, uint64_t n, uint64_t seed) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    int rc;
+    if ((rc = valid_size(ctx->err, ctx->W, ctx->H, n)) != SLIME_OK) return rc;
+    cudaStreamSynchronize(ctx->stream);
+    invalidate_graphs(ctx);
+    free_adjoint(ctx);
+    if ((rc = alloc_agents(ctx, n)) != SLIME_OK) return rc;
+    ctx->reordered = false;
+    // src/main.rs:700-712 draws x, y, angle in [0, 2*pi) and speed anew.
+    return slime_seed_agents(ctx, seed, 0.0f, 6.28318530718f);
+}
+
+int slime_step(slime_ctx* ctx, uint32_t n_steps) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    return run_steps(ctx, n_steps);
+}
+
+int slime_sync(slime_ctx* ctx) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream), "synchronising");
+    return SLIME_OK;
+}
+
+int slime_get_stream(slime_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return SLIME_ERR_INVALID_ARGUMENT;
+    *stream = (void*)ctx->stream;
+    return SLIME_OK;
+}
+
+int slime_download_deposit_counts(slime_ctx* ctx, uint32_t* counts, uint64_t n_cells) {
+    if (!ctx || !counts) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (n_cells != (uint64_t)ctx->W * ctx->H)
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "counts have %llu cells, context has %llu",
+                         (unsigned long long)n_cells, (unsigned long long)ctx->W * ctx->H);
+    if (!ctx->last_counts_valid) {
+        memset(counts, 0, n_cells * sizeof(uint32_t));
+        return SLIME_OK;
+    }
+    CK(cudaMemcpyAsync(counts, ctx->counts[1 - ctx->cur], n_cells * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                       ctx->stream),
+       "downloading deposit counts");
+    CK(cudaStreamSynchronize(ctx->stream), "downloading deposit counts");
+    return SLIME_OK;
+}
+
+int slime_reorder_agents(slime_ctx* ctx) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    int rc = do_reorder(ctx);
+    if (rc != SLIME_OK) return rc;
+    CK(cudaStreamSynchronize(ctx->stream), "reordering agents");
+    return SLIME_OK;
+}
+
+int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, double* trail_ms, double* other_ms) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    cudaEvent_t ev[4];
+    for (auto& e : ev) CK(cudaEventCreate(&e), "creating events");
+    double ta = 0, tt = 0, to = 0;
+    int rc = SLIME_OK;
+    for (uint32_t i = 0; i < n_steps && rc == SLIME_OK; i++) {
+        cudaEventRecord(ev[0], ctx->stream);
+        if (ctx->opt.reorder_every && ctx->steps_done % ctx->opt.reorder_every == 0 &&
+            ctx->last_reorder_step != ctx->steps_done)
+            rc = do_reorder(ctx);
+        cudaEventRecord(ev[1], ctx->stream);
+        const int cur = ctx->cur;
+        cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream);
+        cudaEventRecord(ev[2], ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
+                             ctx->counts[1 - cur], ctx->stream);
+        cudaEventRecord(ev[3], ctx->stream);
+        if (e != cudaSuccess) {
+            rc = cuda_error(ctx->err, e, "profiling a step");
+            break;
+        }
+        ctx->cur = 1 - cur;
+        ctx->steps_done++;
+        ctx->launches += kernels_per_step(ctx);
+        ctx->last_counts_valid = true;
+        if ((e = cudaEventSynchronize(ev[3])) != cudaSuccess) {
+            rc = cuda_error(ctx->err, e, "profiling a step");
+            break;
+        }
+        float a, b, c;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        cudaEventElapsedTime(&c, ev[2], ev[3]);
+        to += a;
+        ta += b;
+        tt += c;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (agents_ms) *agents_ms = ta;
+    if (trail_ms) *trail_ms = tt;
+    if (other_ms) *other_ms = to;
+    return rc;
+}
+
+int slime_autotune(slime_ctx* ctx, uint32_t reps) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (reps == 0) reps = 5;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "creating events");
+    CK(cudaEventCreate(&e1), "creating events");
+    // The trial launches read trail[cur] and the (zero) counts[cur] and write
+    // the other buffers, so the state is untouched; the previous step's
+    // counts are overwritten with zeros.
+    const int cur = ctx->cur;
+    float best = 1e30f;
+    int best_tile = ctx->tile;
+    for (int t = 0; t < trail_tile_count(); t++) {
+        cudaError_t e = launch_trail(ctx->dev, t, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
+                                     ctx->counts[1 - cur], ctx->stream); // warm-up
+        if (e != cudaSuccess) continue;
+        cudaEventRecord(e0, ctx->stream);
+        for (uint32_t r = 0; r < reps; r++)
+            launch_trail(ctx->dev, t, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur], ctx->counts[1 - cur],
+                         ctx->stream);
+        cudaEventRecord(e1, ctx->stream);
+        CK(cudaEventSynchronize(e1), "autotuning");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ctx->launches += reps + 1;
+        if (ms < best) {
+            best = ms;
+            best_tile = t;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->last_counts_valid = false;
+    ctx->tuned_tile = best_tile;
+    if (ctx->opt.trail_tile == 0 && best_tile != ctx->tile) {
+        ctx->tile = best_tile;
+        invalidate_graphs(ctx);
+    }
+    return SLIME_OK;
+}
+
+int slime_colorize(slime_ctx* ctx, const uint8_t* lut768, uint32_t tw, uint32_t th, uint8_t* rgba_out) {
+    if (!ctx || !lut768 || !rgba_out || tw == 0 || th == 0) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    size_t need = 768 + (size_t)tw * th * 4;
+    if (ctx->aux_bytes < need) {
+        if (ctx->aux) cudaFree(ctx->aux);
+        ctx->aux = nullptr;
+        ctx->aux_bytes = 0;
+        CK(cudaMalloc(&ctx->aux, need), "allocating display buffer");
+        ctx->aux_bytes = need;
+    }
+    uint8_t* dlut = (uint8_t*)ctx->aux;
+    uint8_t* drgba = dlut + 768;
+    CK(cudaMemcpyAsync(dlut, lut768, 768, cudaMemcpyHostToDevice, ctx->stream), "uploading LUT");
+    CK(launch_colorize(ctx->trail[ctx->cur], ctx->W, ctx->H, dlut, tw, th, drgba, ctx->stream), "colourising");
+    ctx->launches += 1;
+    CK(cudaMemcpyAsync(rgba_out, drgba, (size_t)tw * th * 4, cudaMemcpyDeviceToHost, ctx->stream), "downloading image");
+    CK(cudaStreamSynchronize(ctx->stream), "colourising");
+    return SLIME_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,65 @@
+// common.cuh - device parameter block and helpers shared by the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/slime.h"
+#include "../../include/slime_math.h"
+
+namespace slime {
+
+constexpr int kMaxR = SLIME_MAX_BLUR_RADIUS;
+
+// Everything a step needs, derived once on the host from SlimeParams with the
+// same binary32 operations the shader performs per invocation
+// (compute.wgsl:159 decay_factor*0.001, :173 clamp(rate, 0, 1)).  Passed by
+// value as a __grid_constant__ kernel argument, i.e. it lives in the constant
+// bank like the reference's uniform buffer.
+struct DevParams {
+    int32_t W, H;
+    float Wf, Hf;
+    float speed_min, speed_max;
+    float turn;
+    float sensor_angle, sensor_dist;
+    float jitter;
+    float time_step;
+    float dep;
+    float decay;    // decay_factor (multiplicative mode)
+    float decay_k;  // decay_factor * 0.001 (subtractive mode)
+    float rate;     // clamp(diffusion_rate, 0, 1)
+    uint32_t decay_mode;
+    uint32_t blur_mode;
+    int32_t R;      // Gaussian taps per side
+    float w[2 * kMaxR + 1];
+};
+
+// Translate SlimeParams into DevParams; returns false (with a message) on
+// values the kernels cannot honour.
+bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* out, const char** why);
+
+// --------------------------------------------------------------- device code
+// Deposit fold: t <- clamp(t + dep, 0, 1), k times; stops once an iteration
+// leaves the bits of t unchanged (every later iteration would too).
+__device__ __forceinline__ float fold_deposits(float t, uint32_t k, float dep) {
+    for (uint32_t i = 0; i < k; i++) {
+        float nt = slm_clamp(slm_add(t, dep), 0.0f, 1.0f);
+        if (__float_as_uint(nt) == __float_as_uint(t)) break;
+        t = nt;
+    }
+    return t;
+}
+
+__device__ __forceinline__ float apply_decay(const DevParams& p, float v) {
+    return p.decay_mode == SLIME_DECAY_MULTIPLY ? slm_mul(v, p.decay) : slm_max(slm_sub(v, p.decay_k), 0.0f);
+}
+
+// Wrap g into [0, n) for g in [-n*k, n*(k+1)); the loops run at most once for
+// the halos the kernels use unless the grid is smaller than the blur radius.
+__device__ __forceinline__ int wrap_coord(int g, int n) {
+    while (g < 0) g += n;
+    while (g >= n) g -= n;
+    return g;
+}
+
+} // namespace slime

@@ -1,0 +1,73 @@
+// ctx.h - the simulation context behind the opaque slime_ctx handle
+// (internal to the library).
+#pragma once
+
+#include <map>
+#include <string>
+#include <utility>
+
+#include "kernels.h"
+
+struct slime_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t W = 0, H = 0;
+
+    slime::AgentsSoA agents;
+    void* agent_block = nullptr;     // x | y | angle | speed, n_pad floats each
+    uint32_t* ids_storage = nullptr; // slot -> agent id, allocated at the first reorder
+    bool reordered = false;
+    uint64_t last_reorder_step = ~0ull;
+    slime::ReorderScratch reorder;
+
+    float* trail[2] = {nullptr, nullptr};
+    uint32_t* counts[2] = {nullptr, nullptr};
+    int cur = 0;
+    bool last_counts_valid = false;
+
+    SlimeParams params{};
+    slime::DevParams dev{};
+    SlimeOptions opt{};
+    int tile = 0;
+    int tuned_tile = -1;
+
+    std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs; // (steps, start parity) -> graph
+
+    uint64_t steps_done = 0;
+    uint64_t launches = 0;
+
+    void* staging = nullptr; // AoS agent staging for uploads/downloads
+    size_t staging_bytes = 0;
+    void* aux = nullptr; // display buffer
+    size_t aux_bytes = 0;
+
+    // Adjoint recording (adjoint.cu).
+    struct Adjoint {
+        bool recorded = false;
+        uint32_t n_steps = 0, ckpt_every = 0, n_ckpt = 0;
+        int start_parity = 0;
+        void* ckpt_agents = nullptr; // n_ckpt * 4 * n_pad floats
+        float* ckpt_trail = nullptr; // n_ckpt * cells
+        float* seg_trail = nullptr;  // ckpt_every * cells: T_s of the segment being back-propagated
+        uint32_t* seg_counts = nullptr; // ckpt_every * cells: k_s
+        float* g[2] = {nullptr, nullptr};
+        double* acc = nullptr; // 3 doubles: d_decay, d_rate, d_dep
+        void* agents_tmp = nullptr; // replay copy of the agents
+        float* trail_tmp[2] = {nullptr, nullptr};
+        uint32_t* counts_tmp = nullptr;
+    } adj;
+
+    std::string err;
+};
+
+namespace slime {
+
+int set_error(std::string& err, int code, const char* fmt, ...);
+int cuda_error(std::string& err, cudaError_t e, const char* what);
+void invalidate_graphs(slime_ctx* ctx);
+cudaError_t enqueue_step(slime_ctx* ctx);
+uint64_t kernels_per_step(const slime_ctx* ctx);
+int run_steps(slime_ctx* ctx, uint32_t n);
+void free_adjoint(slime_ctx* ctx);
+
+} // namespace slime

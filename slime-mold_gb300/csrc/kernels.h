@@ -1,0 +1,66 @@
+// kernels.h - launch wrappers of the CUDA kernels (host side, internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace slime {
+
+// Agent state in HBM: structure of arrays, each array padded to a multiple of
+// kAgentPad agents and 16-byte aligned so that one thread moves four agents
+// with one float4 load/store per field.
+constexpr uint64_t kAgentPad = 128;
+
+struct AgentsSoA {
+    float* x = nullptr;
+    float* y = nullptr;
+    float* th = nullptr;
+    float* v = nullptr;
+    uint32_t* ids = nullptr; // original agent id per slot; nullptr = identity order
+    uint64_t n = 0;          // live agents
+    uint64_t n_pad = 0;      // allocated slots
+};
+
+// ---- agents.cu
+// One agent pass (compute.wgsl:57-145): reads trail, adds deposit counts.
+cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
+                          cudaStream_t s);
+// AoS staging (x, y, angle, speed per agent, id order) <-> SoA slots.
+cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s);
+cudaError_t launch_soa_to_aos(const AgentsSoA& a, float4* aos, cudaStream_t s);
+cudaError_t launch_seed_agents(const AgentsSoA& a, uint64_t seed, float Wf, float Hf, float hmin, float hmax,
+                               float smin, float smax, cudaStream_t s);
+cudaError_t launch_reassign_speeds(const AgentsSoA& a, uint64_t seed, float smin, float smax, cudaStream_t s);
+cudaError_t launch_scale_positions(const AgentsSoA& a, float sx, float sy, cudaStream_t s);
+
+// ---- trail.cu
+// Tile shapes of the fused deposit-fold + decay + diffuse kernel.
+struct TrailTile {
+    int tw, th;
+};
+int trail_tile_count();
+TrailTile trail_tile(int index);
+int trail_tile_default();
+// Fused trail pass: out = Diffuse(Decay(Fold(in, counts_in))); zeroes
+// counts_zero (the other step's count buffer) over the same cells.
+cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
+                         uint32_t* counts_zero, cudaStream_t s);
+
+// ---- reorder.cu
+// Morton reordering of agent slots by cell; permutes SoA in place through
+// scratch buffers and keeps ids.
+struct ReorderScratch {
+    void* buf = nullptr;
+    size_t bytes = 0;
+};
+cudaError_t launch_iota(uint32_t* ids, uint64_t n, cudaStream_t s);
+cudaError_t launch_reorder(AgentsSoA& a, uint32_t W, uint32_t H, int cell_log2, ReorderScratch& scratch,
+                           cudaStream_t s);
+
+// ---- colorize.cu
+cudaError_t launch_colorize(const float* trail, uint32_t W, uint32_t H, const uint8_t* lut, uint32_t tw,
+                            uint32_t th, uint8_t* rgba, cudaStream_t s);
+
+} // namespace slime

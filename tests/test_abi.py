@@ -1,0 +1,103 @@
+"""The C ABI library: builds, loads, exports every declared symbol, and its
+host-only entry points (settings, presets, parameter translation, error
+paths) behave like the reference's Settings/presets (no GPU needed)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared_functions():
+    names = set()
+    for h in ("slime.h",):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(slime_[a-z0-9_]+)\s*\(", src):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    from slime_gb300 import _abi
+    declared = declared_functions()
+    assert len(declared) > 40
+    out = subprocess.run(["nm", "-D", "--defined-only", _abi.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\b(slime_[a-z0-9_]+)\b", out))
+    missing = declared - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    assert declared <= set(_abi.SIGNATURES), sorted(declared - set(_abi.SIGNATURES))
+
+
+def test_struct_layouts():
+    from slime_gb300 import SlimeParams, SlimeSettings, SlimeOptions, SlimeGrads
+    # SimSizeUniform is 14 x 4 bytes (src/main.rs:29-46); the extensions add 16.
+    assert C.sizeof(SlimeParams) == 72
+    assert SlimeParams.blur_sigma.offset == 48 and SlimeParams._pad.offset == 52
+    assert SlimeParams.time_step.offset == 56
+    assert C.sizeof(SlimeGrads) == 32
+    assert C.sizeof(SlimeOptions) == 32
+
+
+def test_settings_default_matches_reference(built_lib):
+    import slime_gb300 as sg
+    s = sg.default_settings()
+    # src/settings.rs:4-27
+    assert s.agent_count == 10_000_000
+    assert (s.window_width, s.window_height, s.window_fullscreen) == (1600, 900, 0)
+    assert s.agent_speed_min == 30.0 and s.agent_speed_max == 50.0
+    assert s.agent_turn_speed == pytest.approx(0.43)
+    assert s.agent_sensor_angle == pytest.approx(0.3) and s.agent_sensor_distance == 20.0
+    assert s.pheromone_decay_factor == 10.0 and s.pheromone_diffusion_rate == 1.0
+    assert s.pheromone_deposition_amount == 1.0 and s.agent_jitter == 0.0
+    assert s.blur_radius == 2.0 and s.blur_sigma == 1.0
+    assert (s.agent_possible_starting_headings_start, s.agent_possible_starting_headings_end) == (0.0, 360.0)
+
+
+def test_presets_match_reference(built_lib):
+    import slime_gb300 as sg
+    names = sg.preset_names()
+    assert names == ["Default", "Sponge", "Firecracker Trees", "Threads", "Curls", "Waves", "Snake", "Mesh"]
+    curls = sg.preset("Curls")  # src/presets.rs:93-107
+    assert curls.agent_count == 3_000_000 and curls.agent_jitter == 5.0
+    assert curls.pheromone_decay_factor == 75.0 and curls.pheromone_diffusion_rate == pytest.approx(0.1)
+    mesh = sg.preset("Mesh")  # src/presets.rs:139-152
+    assert mesh.agent_sensor_distance == 225.0 and mesh.agent_sensor_angle == pytest.approx(1.57)
+    assert mesh.agent_turn_speed == 6.0 and mesh.agent_count == 10_000_000
+    with pytest.raises(KeyError):
+        sg.preset("Nope")
+
+
+def test_params_from_settings_is_sim_size_uniform_new(built_lib):
+    import slime_gb300 as sg
+    s = sg.preset("Snake")
+    p = sg.params_from_settings(s, 1600, 900)
+    assert (p.width, p.height) == (1600, 900)
+    assert p.decay_factor == s.pheromone_decay_factor
+    assert p.diffusion_rate == s.pheromone_diffusion_rate
+    assert p.pheromone_deposition_amount == s.pheromone_deposition_amount
+    assert p.agent_sensor_distance == 225.0 and p.blur_radius == 2.0 and p.blur_sigma == 1.0
+    assert p.time_step == pytest.approx(0.016) and p.decay_mode == 0 and p.blur_mode == 0
+
+
+def test_create_without_gpu_reports_no_device(built_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import slime_gb300 as sg
+    with pytest.raises(sg.SlimeError) as e:
+        sg.Simulation(16, 16, 4)
+    assert e.value.status == -6
+
+
+def test_invalid_sizes_rejected_before_touching_the_device(built_lib):
+    import slime_gb300 as sg
+    L = sg.lib()
+    st = C.c_int(0)
+    assert not L.slime_create(0, 16, 4, C.byref(st)) and st.value == -1
+    assert not L.slime_create(65536, 65536, 4, C.byref(st)) and st.value == -1
+    assert not L.slime_create(16, 16, 1 << 31, C.byref(st)) and st.value == -1
+    assert L.slime_status_string(-5) == b"device-side wait timed out"

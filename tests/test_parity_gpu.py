@@ -1,0 +1,278 @@
+"""Parity of the CUDA step (through the C ABI) with the CPU oracle.
+
+Integer and index work (deposit cells, counts, floor/wrap) and, because the
+shared builtins are evaluated identically on both sides, every binary32 value
+of the agent state and the trail are compared bit for bit.  Sizes are the
+512x512 reference-size configuration and small edge cases the oracle finishes
+in seconds; the full-size configurations are covered by property tests in
+test_properties_gpu.py.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import agents_uniform, config0_params
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def assert_bitexact(gpu_arr, cpu_arr, what):
+    g, c = bits(gpu_arr), bits(cpu_arr)
+    bad = np.flatnonzero(g.reshape(-1) != c.reshape(-1))
+    assert bad.size == 0, (f"{what}: {bad.size} mismatches, first at {bad[:5]}: "
+                           f"gpu={np.asarray(gpu_arr).reshape(-1)[bad[:5]]} cpu={np.asarray(cpu_arr).reshape(-1)[bad[:5]]}")
+
+
+def make_sim(W, H, n, params, agents, trail=None):
+    import slime_gb300 as sg
+    sim = sg.Simulation(W, H, n, params)
+    sim.upload_agents(agents)
+    if trail is not None:
+        sim.upload_trail(trail)
+    return sim
+
+
+@pytest.mark.parametrize("decay_mode,blur_mode", [(0, 0), (1, 1), (0, 1), (1, 0)])
+def test_one_step_bitexact_random_trail(gpu, decay_mode, blur_mode):
+    W = H = 512
+    n = 65536
+    p = config0_params(W, H, decay_mode=decay_mode, blur_mode=blur_mode, agent_speed_min=30.0,
+                       agent_speed_max=50.0)
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=1)
+    trail = np.random.default_rng(2).random((H, W), dtype=np.float32)
+    sim = make_sim(W, H, n, p, agents, trail)
+    sim.step(1)
+    ga, gt, gc = sim.download_agents(), sim.download_trail(), sim.download_deposit_counts()
+    ca = agents.copy()
+    cc = oracle.agents_pass(p, W, H, ca, trail)
+    ct = oracle.trail_pass(p, W, H, trail, cc)
+    assert np.array_equal(gc, cc), "deposit counts differ"
+    assert_bitexact(ga, ca, "agents")
+    assert_bitexact(gt, ct, "trail")
+    # the random trail makes every turn branch occur
+    turned = np.abs(ga[:, 2] - np.mod(agents[:, 2], np.float32(2 * np.pi)))
+    assert (turned > 0.1).mean() > 0.3
+
+
+def test_config0_100_steps_every_step_bitexact(gpu):
+    """The 512x512 / 65,536-agent configuration from a zero trail, 100 steps,
+    agent state and trail compared after every step."""
+    W = H = 512
+    n = 65536
+    p = config0_params(W, H)
+    agents = agents_uniform(n, W, H, 1.0, 2.0, seed=0)
+    trail = np.zeros((H, W), np.float32)
+    sim = make_sim(W, H, n, p, agents)
+    ca, ct = agents.copy(), trail.copy()
+    for s in range(100):
+        sim.step(1)
+        oracle.run(p, W, H, ca, ct, 1)
+        if s % 10 == 9 or s < 3:
+            assert_bitexact(sim.download_agents(), ca, f"agents after step {s + 1}")
+            assert_bitexact(sim.download_trail(), ct, f"trail after step {s + 1}")
+    assert_bitexact(sim.download_agents(), ca, "agents after 100 steps")
+    assert_bitexact(sim.download_trail(), ct, "trail after 100 steps")
+    assert ct.sum() > 0
+
+
+def test_graph_chunks_match_single_steps(gpu):
+    W, H, n = 300, 200, 20000
+    p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, agent_speed_min=30.0,
+                       agent_speed_max=50.0, agent_jitter=0.3)
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=3)
+    a = make_sim(W, H, n, p, agents)
+    b = make_sim(W, H, n, p, agents)
+    a.set_options(use_graphs=1, graph_chunk=7)
+    b.set_options(use_graphs=0)
+    a.step(23)
+    for _ in range(23):
+        b.step(1)
+    assert_bitexact(a.download_agents(), b.download_agents(), "agents")
+    assert_bitexact(a.download_trail(), b.download_trail(), "trail")
+    ca, ct = agents.copy(), np.zeros((H, W), np.float32)
+    oracle.run(p, W, H, ca, ct, 23)
+    assert_bitexact(a.download_agents(), ca, "agents vs oracle")
+    assert_bitexact(a.download_trail(), ct, "trail vs oracle")
+    assert a.info().steps_done == 23
+
+
+@pytest.mark.parametrize("tile", range(1, 8))
+def test_every_trail_tile_is_bitexact(gpu, tile):
+    W, H, n = 333, 77, 5000  # ragged against every tile shape
+    for blur_mode, radius in ((0, 1.0), (1, 1.0), (1, 3.0)):
+        p = config0_params(W, H, decay_mode=1, blur_mode=blur_mode, blur_radius=radius, blur_sigma=1.5)
+        agents = agents_uniform(n, W, H, 1.0, 2.0, seed=4)
+        trail = np.random.default_rng(5).random((H, W), dtype=np.float32)
+        sim = make_sim(W, H, n, p, agents, trail)
+        sim.set_options(trail_tile=tile)
+        sim.step(2)
+        ca, ct = agents.copy(), trail.copy()
+        oracle.run(p, W, H, ca, ct, 2)
+        assert_bitexact(sim.download_trail(), ct, f"trail tile {tile} blur {blur_mode} r {radius}")
+        assert_bitexact(sim.download_agents(), ca, "agents")
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (2, 3), (3, 2), (5, 3), (4, 4), (17, 1), (1, 19)])
+def test_tiny_toroidal_grids(gpu, W, H):
+    n = 64
+    for blur_mode, radius in ((0, 1.0), (1, 2.0)):
+        p = config0_params(W, H, decay_mode=0, blur_mode=blur_mode, blur_radius=radius,
+                           decay_factor=5.0, agent_sensor_distance=1.5, agent_speed_min=30.0, agent_speed_max=90.0,
+                           pheromone_deposition_amount=0.3)
+        agents = agents_uniform(n, W, H, 30.0, 90.0, seed=6)
+        trail = np.random.default_rng(7).random((H, W), dtype=np.float32)
+        sim = make_sim(W, H, n, p, agents, trail)
+        sim.step(3)
+        ca, ct = agents.copy(), trail.copy()
+        oracle.run(p, W, H, ca, ct, 3)
+        assert_bitexact(sim.download_agents(), ca, f"agents {W}x{H}")
+        assert_bitexact(sim.download_trail(), ct, f"trail {W}x{H}")
+
+
+def test_edge_positions_and_sensor_bounds(gpu):
+    """Agents on the last row/column, at x rounding up to W after the wrap,
+    sensors off the grid (the sampler returns 0 there, it does not wrap),
+    negative and huge angles."""
+    W, H = 64, 48
+    Wf, Hf = np.float32(W), np.float32(H)
+    eps = np.float32(1e-6)
+    rows = [
+        (Wf - eps, 10.0, 0.0, 1.0), (0.0, 0.0, np.pi, 1.0), (Wf - 1, Hf - 1, 0.3, 1.0),
+        (-1e-8, 5.0, np.pi, 1.0), (5.0, -1e-8, 1.5 * np.pi, 1.0), (W - 0.5, H - 0.5, 0.785, 60.0),
+        (31.5, 23.5, -7.0, 40.0), (10.0, 10.0, 1e6, 40.0), (10.0, 10.0, -1e7, 40.0), (0.0, 0.0, 0.0, 0.0),
+        (Wf - np.float32(2e-6), Hf - np.float32(2e-6), 0.01, 1.0),
+    ]
+    agents = np.array(rows, np.float32)
+    n = agents.shape[0]
+    trail = np.random.default_rng(8).random((H, W), dtype=np.float32)
+    p = config0_params(W, H, decay_mode=0, blur_mode=0, agent_sensor_distance=20.0, agent_speed_min=0.5,
+                       agent_speed_max=100.0, agent_jitter=1.0, agent_turn_speed=0.43)
+    sim = make_sim(W, H, n, p, agents, trail)
+    for s in range(5):
+        sim.step(1)
+    ca, ct = agents.copy(), trail.copy()
+    oracle.run(p, W, H, ca, ct, 5)
+    assert_bitexact(sim.download_agents(), ca, "edge agents")
+    assert_bitexact(sim.download_trail(), ct, "edge trail")
+
+
+def test_deposit_fold_many_agents_one_cell(gpu):
+    """Thousands of agents landing in one cell in one step: the sequential
+    clamp fold is reproduced exactly (small deposition so it does not
+    saturate at once)."""
+    W, H, n = 32, 32, 4096
+    agents = np.zeros((n, 4), np.float32)
+    agents[:, 0] = 16.25
+    agents[:, 1] = 16.25
+    agents[:, 2] = 0.0
+    agents[:, 3] = 0.0
+    trail = np.zeros((H, W), np.float32)
+    for dep in (1.0e-4, 0.37, 3.0, 0.0):
+        p = config0_params(W, H, decay_mode=1, blur_mode=0, agent_jitter=0.0, agent_speed_min=0.0,
+                           agent_speed_max=0.0, pheromone_deposition_amount=dep, decay_factor=1.0)
+        sim = make_sim(W, H, n, p, agents, trail)
+        sim.step(1)
+        gc = sim.download_deposit_counts()
+        assert gc[16, 16] == n and gc.sum() == n
+        ca, ct = agents.copy(), trail.copy()
+        oracle.run(p, W, H, ca, ct, 1)
+        assert_bitexact(sim.download_trail(), ct, f"fold dep={dep}")
+
+
+def test_zero_agents_and_odd_counts(gpu):
+    W, H = 40, 30
+    p = config0_params(W, H)
+    trail = np.random.default_rng(9).random((H, W), dtype=np.float32)
+    for n in (0, 1, 3, 5, 129):
+        agents = agents_uniform(n, W, H, 1.0, 2.0, seed=n)
+        sim = make_sim(W, H, n, p, agents, trail)
+        sim.step(4)
+        ca, ct = agents.copy(), trail.copy()
+        oracle.run(p, W, H, ca, ct, 4)
+        assert_bitexact(sim.download_trail(), ct, f"trail n={n}")
+        if n:
+            assert_bitexact(sim.download_agents(), ca, f"agents n={n}")
+
+
+def test_morton_reorder_changes_nothing(gpu):
+    W, H, n = 256, 256, 30000
+    p = config0_params(W, H, decay_mode=0, blur_mode=0, agent_speed_min=30.0, agent_speed_max=50.0,
+                       agent_jitter=0.2)
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=10)
+    a = make_sim(W, H, n, p, agents)
+    b = make_sim(W, H, n, p, agents)
+    a.set_options(reorder_every=5, reorder_cell_log2=1)
+    a.step(17)
+    b.step(17)
+    assert a.info().reordered == 1
+    assert_bitexact(a.download_agents(), b.download_agents(), "agents (reordered vs not)")
+    assert_bitexact(a.download_trail(), b.download_trail(), "trail (reordered vs not)")
+    ca, ct = agents.copy(), np.zeros((H, W), np.float32)
+    oracle.run(p, W, H, ca, ct, 17)
+    assert_bitexact(a.download_agents(), ca, "agents vs oracle")
+
+
+def test_seed_agents_matches_generator(gpu):
+    import slime_gb300 as sg
+    W, H, n = 1600, 900, 1000
+    sim = sg.Simulation(W, H, n, config0_params(W, H, agent_speed_min=30.0, agent_speed_max=50.0))
+    sim.seed_agents(1234, 0.0, 6.28318530718)
+    a = sim.download_agents()
+    u = [oracle.uniform01(1234, n, f) for f in range(4)]
+    x = (u[0] * np.float32(W)).astype(np.float32)
+    assert np.array_equal(a[:, 0], np.minimum(x, np.nextafter(np.float32(W), np.float32(0))))
+    assert np.array_equal(a[:, 2], np.float32(0.0) + u[2] * np.float32(6.28318530718))
+    assert np.array_equal(a[:, 3], np.float32(30.0) + u[3] * np.float32(20.0))
+    assert (a[:, 1] < H).all() and (a[:, 1] >= 0).all()
+
+
+def test_resize_and_clear_follow_reference(gpu):
+    """Resize scales x, y by new/old and drops the trail (src/main.rs:954-1015);
+    clear zeroes the trail (src/main.rs:909-913)."""
+    import slime_gb300 as sg
+    W, H, n = 200, 100, 500
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=11)
+    sim = make_sim(W, H, n, config0_params(W, H), agents, np.ones((H, W), np.float32))
+    sim.resize(300, 50)
+    a = sim.download_agents()
+    assert np.array_equal(a[:, 0], agents[:, 0] * (np.float32(300) / np.float32(200)))
+    assert np.array_equal(a[:, 1], agents[:, 1] * (np.float32(50) / np.float32(100)))
+    assert sim.download_trail().shape == (50, 300) and not sim.download_trail().any()
+    sim.upload_trail(np.ones((50, 300), np.float32))
+    sim.clear_trail()
+    assert not sim.download_trail().any()
+    p = sim.params()
+    assert (p.width, p.height) == (300, 50)
+    sim.set_agent_count(77, seed=5)
+    assert sim.download_agents().shape == (77, 4)
+    with pytest.raises(sg.SlimeError):
+        sim.upload_agents(np.zeros((5, 4), np.float32))
+
+
+def test_nan_parameters_rejected(gpu):
+    import slime_gb300 as sg
+    sim = sg.Simulation(16, 16, 4)
+    p = config0_params(16, 16)
+    p.diffusion_rate = float("nan")
+    with pytest.raises(sg.SlimeError) as e:
+        sim.set_params(p)
+    assert e.value.status == -1
+    p = config0_params(16, 16, blur_mode=1, blur_sigma=0.0)
+    with pytest.raises(sg.SlimeError):
+        sim.set_params(p)
+    p = config0_params(32, 16)
+    with pytest.raises(sg.SlimeError):
+        sim.set_params(p)
+
+
+def test_colorize_matches_display_pass(gpu):
+    W, H = 160, 90
+    trail = np.random.default_rng(12).random((H, W), dtype=np.float32) * 1.2 - 0.1
+    lut = np.random.default_rng(13).integers(0, 256, 768).astype(np.uint8)
+    sim = make_sim(W, H, 4, config0_params(W, H), agents_uniform(4, W, H, 1, 2), trail)
+    for tw, th in ((160, 90), (200, 90), (160, 200), (37, 11)):
+        assert np.array_equal(sim.colorize(lut, tw, th), oracle.colorize(W, H, trail, lut, tw, th)), (tw, th)
