@@ -344,9 +344,11 @@ static void chain_setup(ChainParams* c, const SlimeParams* p, uint32_t W, uint32
     c->blur_mode = p->blur_mode;
     c->R = p->blur_mode == SLIME_BLUR_GAUSS ? slm_gauss_radius(p->blur_radius, SLIME_MAX_BLUR_RADIUS) : 1;
     if (p->blur_mode == SLIME_BLUR_GAUSS) {
-        double tot = 0.0, s2 = 2.0 * (double)p->blur_sigma * (double)p->blur_sigma;
-        for (int i = -c->R; i <= c->R; i++) tot += (c->w[i + c->R] = slm_exp_neg_host((double)(i * i) / s2));
-        for (int i = 0; i <= 2 * c->R; i++) c->w[i] /= tot;
+        /* The binary32 weights the forward applies, evaluated in binary64:
+         * the chain is the same linear operator the kernels implement. */
+        float w32[2 * SLIME_MAX_BLUR_RADIUS + 1];
+        slm_gauss_weights(c->R, p->blur_sigma, w32);
+        for (int i = 0; i <= 2 * c->R; i++) c->w[i] = (double)w32[i];
     } else {
         for (int i = 0; i < 3; i++) c->w[i] = 1.0 / 3.0;
     }

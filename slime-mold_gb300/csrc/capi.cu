@@ -84,6 +84,9 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
             *why = "blur_sigma must be > 0 in Gaussian mode";
             return false;
         }
+        double ws = 0.0;
+        for (int i = 0; i <= 2 * d.R; i++) ws += (double)d.w[i];
+        d.w2sum_m1 = (float)(ws * ws - 1.0);
     }
     *out = d;
     return true;
@@ -668,6 +671,7 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
     float best = 1e30f;
     int best_tile = ctx->tile;
     for (int t = 0; t < trail_tile_count(); t++) {
+        if (!trail_tile_supported(ctx->dev, t)) continue;
         cudaError_t e = launch_trail(ctx->dev, t, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
                                      ctx->counts[1 - cur], ctx->stream); // warm-up
         if (e != cudaSuccess) continue;

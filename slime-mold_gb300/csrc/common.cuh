@@ -32,6 +32,7 @@ struct DevParams {
     uint32_t blur_mode;
     int32_t R;      // Gaussian taps per side
     float w[2 * kMaxR + 1];
+    float w2sum_m1; // (sum of w)^2 - 1 in binary64, rounded: B(u) - u = sum w w (u_n - u_c) + this * u_c
 };
 
 // Translate SlimeParams into DevParams; returns false (with a message) on

@@ -45,16 +45,20 @@ struct slime_ctx {
     struct Adjoint {
         bool recorded = false;
         uint32_t n_steps = 0, ckpt_every = 0, n_ckpt = 0;
-        int start_parity = 0;
-        void* ckpt_agents = nullptr; // n_ckpt * 4 * n_pad floats
-        float* ckpt_trail = nullptr; // n_ckpt * cells
-        float* seg_trail = nullptr;  // ckpt_every * cells: T_s of the segment being back-propagated
-        uint32_t* seg_counts = nullptr; // ckpt_every * cells: k_s
-        float* g[2] = {nullptr, nullptr};
-        double* acc = nullptr; // 3 doubles: d_decay, d_rate, d_dep
-        void* agents_tmp = nullptr; // replay copy of the agents
-        float* trail_tmp[2] = {nullptr, nullptr};
-        uint32_t* counts_tmp = nullptr;
+        slime::DevParams dev{};          // parameters the recorded steps ran with
+        int tile = 0;
+        uint32_t rate_active = 0;         // 0 < diffusion_rate < 1
+        uint64_t n = 0, n_pad = 0;
+        bool with_ids = false;
+        float* ckpt_agents = nullptr;     // n_ckpt * 4 * n_pad floats
+        uint32_t* ckpt_ids = nullptr;     // n_ckpt * n_pad (when reordered)
+        float* ckpt_trail = nullptr;      // n_ckpt * cells
+        float* seg_trail = nullptr;       // ckpt_every * cells: T_s of the segment being replayed
+        uint32_t* seg_counts = nullptr;   // ckpt_every * cells: k_s
+        float* g[2] = {nullptr, nullptr}; // dL/dT ping-pong
+        double* acc = nullptr;            // d_decay, d_rate, d_dep
+        float* agents_tmp = nullptr;      // replay copy of the agents (4 * n_pad)
+        uint32_t* ids_tmp = nullptr;
     } adj;
 
     std::string err;

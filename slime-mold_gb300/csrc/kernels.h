@@ -43,10 +43,22 @@ struct TrailTile {
 int trail_tile_count();
 TrailTile trail_tile(int index);
 int trail_tile_default();
+// Whether tile `index` can run this parameter set / grid (the streaming
+// tiles need W % 4 == 0 and a blur radius of 1 or 2).
+bool trail_tile_supported(const DevParams& p, int tile);
 // Fused trail pass: out = Diffuse(Decay(Fold(in, counts_in))); zeroes
-// counts_zero (the other step's count buffer) over the same cells.
+// counts_zero (the other step's count buffer, may be null) over the same cells.
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
                          uint32_t* counts_zero, cudaStream_t s);
+
+// ---- adjoint.cu
+// One backward step of the frozen-trajectory chain: from g_in = dL/dT_{s+1}
+// and the step's input trail T_s and counts k_s, writes g_out = dL/dT_s and
+// adds the step's parameter-gradient contributions to acc[0..2]
+// (decay_factor, diffusion_rate, deposition), in binary64.
+cudaError_t launch_adjoint_step(const DevParams& p, const float* trail_s, const uint32_t* counts_s,
+                                const float* g_in, float* g_out, double* acc, uint32_t rate_active,
+                                cudaStream_t s);
 
 // ---- reorder.cu
 // Morton reordering of agent slots by cell; permutes SoA in place through

@@ -1,0 +1,86 @@
+"""The checkpointed GPU adjoint of the deposit -> decay -> diffuse chain
+against the binary64 oracle adjoint and binary64 central finite differences
+on the frozen-trajectory forward (the deposit counts of every step are taken
+from the oracle's bit-identical replay of the same agents)."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import agents_uniform, config0_params
+from test_oracle import fd4
+
+pytestmark = pytest.mark.gpu
+
+
+def run_case(W, H, n, steps, K, dm, bm, dep, seed=0, radius=1.0, t_lo=0.0):
+    import slime_gb300 as sg
+    p = config0_params(W, H, decay_mode=dm, blur_mode=bm, pheromone_deposition_amount=dep,
+                       decay_factor=0.97 if dm else 10.0, agent_speed_min=30.0, agent_speed_max=50.0,
+                       blur_radius=radius)
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    t0 = (t_lo + rng.random((H, W)) * (0.5 - t_lo)).astype(np.float32)
+    target = rng.random((H, W)).astype(np.float32)
+    with sg.Simulation(W, H, n, p) as sim:
+        sim.upload_agents(agents)
+        sim.upload_trail(t0)
+        sim.forward_record(steps, K)
+        tn = sim.download_trail()
+        g = tn - target
+        grads, d0 = sim.backward(g)
+        # the live state is untouched by the backward
+        assert np.array_equal(sim.download_trail(), tn)
+    a, t = agents.copy(), t0.copy()
+    counts = oracle.run(p, W, H, a, t, steps, record_counts=True)
+    assert np.array_equal(t, tn), "forward differs from the oracle"
+    theta = [float(np.float32(p.decay_factor)), float(np.float32(p.diffusion_rate)),
+             float(np.float32(p.pheromone_deposition_amount))]
+    loss, ref, d0_ref = oracle.chain_adjoint_f64(p, W, H, *theta, t0, counts, g_final=g.astype(np.float64))
+    return p, t0, counts, theta, grads, d0, ref, d0_ref, g
+
+
+@pytest.mark.parametrize("dm,bm,dep", [(1, 1, 0.3), (0, 0, 0.3), (1, 0, 0.05), (0, 1, 1.0)])
+def test_adjoint_matches_binary64_adjoint(gpu, dm, bm, dep):
+    W, H = 96, 80
+    p, t0, counts, theta, grads, d0, ref, d0_ref, g = run_case(W, H, 2000, 37, 10, dm, bm, dep)
+    got = [grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount]
+    for i in range(3):
+        assert abs(got[i] - ref[i]) <= 1e-5 * max(1.0, abs(ref[i])), (i, got[i], ref[i])
+    assert np.abs(d0 - d0_ref).max() <= 1e-5 * max(1.0, np.abs(d0_ref).max())
+
+
+def test_adjoint_matches_finite_differences(gpu):
+    W, H = 64, 64
+    # off the kinks: small deposition, trail away from 0 and 1
+    p, t0, counts, theta, grads, d0, ref, d0_ref, g = run_case(W, H, 1500, 25, 7, 1, 1, 0.02, seed=3, t_lo=0.1)
+    assert counts.max() * 0.02 + 0.5 < 1.0
+    target = None
+    # loss L = <g_fixed, T_n>: linear in T_n, so its FD needs no target
+    got = [grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount]
+    h = 1e-4
+    gf = g.astype(np.float64)
+
+    def lin_loss(th):
+        _, fin = oracle.chain_loss_f64(p, W, H, *th, t0, counts, np.zeros((H, W)))
+        return (fin * gf).sum()
+
+    for i in range(3):
+        fd = fd4(lin_loss, theta, i, h)
+        assert abs(got[i] - fd) <= 1e-5 * max(1.0, abs(fd)), (i, got[i], fd)
+    assert target is None
+
+
+def test_adjoint_radius2_and_ragged_segments(gpu):
+    W, H = 70, 45
+    p, t0, counts, theta, grads, d0, ref, d0_ref, g = run_case(W, H, 900, 23, 5, 1, 1, 0.2, seed=5, radius=2.0)
+    got = [grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount]
+    for i in range(3):
+        assert abs(got[i] - ref[i]) <= 1e-5 * max(1.0, abs(ref[i])), (i, got[i], ref[i])
+
+
+def test_backward_without_record_is_an_error(gpu):
+    import slime_gb300 as sg
+    with sg.Simulation(16, 16, 8) as sim:
+        with pytest.raises(sg.SlimeError) as e:
+            sim.backward(np.zeros((16, 16), np.float32))
+        assert e.value.status == -4

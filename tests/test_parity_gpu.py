@@ -100,10 +100,11 @@ def test_graph_chunks_match_single_steps(gpu):
     assert a.info().steps_done == 23
 
 
-@pytest.mark.parametrize("tile", range(1, 8))
-def test_every_trail_tile_is_bitexact(gpu, tile):
-    W, H, n = 333, 77, 5000  # ragged against every tile shape
-    for blur_mode, radius in ((0, 1.0), (1, 1.0), (1, 3.0)):
+@pytest.mark.parametrize("tile", range(1, 11))
+@pytest.mark.parametrize("W,H", [(333, 77), (336, 77), (256, 40), (8, 9)])
+def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
+    n = 5000  # sizes ragged against every tile shape; the streaming tiles need W % 4 == 0
+    for blur_mode, radius in ((0, 1.0), (1, 1.0), (1, 2.0), (1, 3.0)):
         p = config0_params(W, H, decay_mode=1, blur_mode=blur_mode, blur_radius=radius, blur_sigma=1.5)
         agents = agents_uniform(n, W, H, 1.0, 2.0, seed=4)
         trail = np.random.default_rng(5).random((H, W), dtype=np.float32)
