@@ -8,8 +8,6 @@ nearest binary32 value, so the header carries no number of unknown origin:
     Payne-Hanek reduction for large arguments.
   * SLM_PIO2_{1,2,3}: pi/2 split into three binary32 parts for the
     Cody-Waite reduction of small arguments.
-  * SLM_PH_C{H,L}: pi/2 * 2^-63 split into two binary32 parts, which scales the
-    63-bit fixed-point remainder of the Payne-Hanek reduction back to radians.
   * SLM_S*, SLM_C*: Taylor coefficients (-1)^k / (2k+1)! and (-1)^k / (2k)!.
 
 Run `python include/gen_slime_math_constants.py` to print the C block; the
@@ -61,16 +59,11 @@ def constants():
     p1 = f32(pio2)
     p2 = f32(pio2 - p1)
     p3 = f32(pio2 - p1 - p2)
-    c = pio2 * mpmath.mpf(2) ** -63
-    ch = f32(c)
-    cl = f32(c - ch)
     out = {
         "SLM_TWO_OVER_PI_F": f32(2 / mpmath.pi),
         "SLM_PIO2_1": p1,
         "SLM_PIO2_2": p2,
         "SLM_PIO2_3": p3,
-        "SLM_PH_CH": ch,
-        "SLM_PH_CL": cl,
     }
     for k in range(1, 5):
         out[f"SLM_S{k}"] = f32(mpmath.mpf((-1) ** k) / mpmath.factorial(2 * k + 1))

@@ -119,8 +119,9 @@ typedef struct SlimeOptions {
     uint32_t reorder_every;     /* Morton-reorder agents every k steps, 0 = never (default 0) */
     uint32_t reorder_cell_log2; /* Morton key granularity, log2 of a square of cells (default 2) */
     uint32_t l2_persist;        /* 1: persisting-L2 access window over the sensed trail (default 1) */
-    uint32_t trail_tile;        /* 0: autotuned/default, otherwise an index into the tile table */
-    uint32_t reserved[2];
+    uint32_t trail_tile;        /* 0: autotuned/default, otherwise 1 + an index into the tile table */
+    uint32_t agent_shape;       /* 0: autotuned/default, otherwise 1 + an index into the agent-shape table */
+    uint32_t reserved;
 } SlimeOptions;
 
 typedef struct SlimeInfo {
@@ -131,6 +132,8 @@ typedef struct SlimeInfo {
     uint64_t kernel_launches; /* kernels enqueued by this context (graph nodes count) */
     uint32_t trail_tile;      /* tile-table index in use */
     uint32_t reordered;       /* 1 if device agent order differs from id order */
+    uint32_t agent_shape;     /* agent-kernel shape index in use */
+    uint32_t reserved;
 } SlimeInfo;
 
 const char* slime_version(void);
@@ -206,8 +209,9 @@ int slime_reorder_agents(slime_ctx* ctx);
  * the context's stream; totals in milliseconds (NULL outputs are skipped). */
 int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, double* trail_ms,
                         double* other_ms);
-/* Pick the fastest trail tile for this context's size by timing each
- * candidate (the trail state is restored afterwards). */
+/* Pick the fastest trail tile and agent-kernel shape for this context by
+ * timing each candidate (agents and trail are restored afterwards; the
+ * previous step's deposit counts are cleared). */
 int slime_autotune(slime_ctx* ctx, uint32_t reps);
 
 /* ------------------------------------------------ adjoint (frozen trajectories) */

@@ -17,7 +17,8 @@
  *   - sin and cos are computed here from published methods:
  *       * |x| < 4096: Cody-Waite reduction by pi/2 split into three binary32
  *         parts (W. J. Cody and W. Waite, "Software Manual for the Elementary
- *         Functions", 1980), evaluated with fused multiply-adds;
+ *         Functions", 1980), evaluated with fused multiply-adds, the nearest
+ *         multiple found by the 1.5 * 2^23 rounding addition;
  *       * otherwise: Payne-Hanek reduction (M. Payne and R. Hanek, "Radian
  *         reduction for trigonometric functions", SIGNUM Newsletter 18(1),
  *         1983) with a 96-bit window of 2/pi and 32x32->64 integer products;
@@ -46,8 +47,6 @@
 #define SLM_PIO2_1 (0x1.921fb60000000p+0f)
 #define SLM_PIO2_2 (-0x1.777a5c0000000p-25f)
 #define SLM_PIO2_3 (-0x1.ee59da0000000p-50f)
-#define SLM_PH_CH (0x1.921fb60000000p-63f)
-#define SLM_PH_CL (-0x1.777a5c0000000p-88f)
 #define SLM_S1 (-0x1.5555560000000p-3f)
 #define SLM_S2 (0x1.1111120000000p-7f)
 #define SLM_S3 (-0x1.a01a020000000p-13f)
@@ -142,15 +141,32 @@ SLM_FN float slm_mix(float a, float b, float t) {
 }
 /* The f32 `%` operator: remainder with the sign of the dividend.  fmodf is
  * exact on every conforming implementation, so host and device agree. */
-SLM_FN float slm_fmod(float x, float y) { return fmodf(x, y); }
+SLM_FN float slm_fmod(float x, float y) {
+    /* For y > 0 and |x| < 2y the remainder is one of x, x - y, x + y, each
+     * exact (Sterbenz), which is what every exact fmodf returns; the
+     * remainder of -y is -0.  Everything else goes to fmodf. */
+    if (y > 0.0f) {
+        if (slm_abs(x) < y) return x;
+        if (x >= y && x < slm_add(y, y)) return slm_sub(x, y);
+        if (x <= -y && x > -slm_add(y, y)) {
+            float r = slm_add(x, y);
+            return r == 0.0f ? -0.0f : r;
+        }
+    }
+    return fmodf(x, y);
+}
 
 /* WGSL i32(f32): truncate toward zero, saturate to the i32 range, NaN -> 0.
  * (Matches the device's cvt.rzi.sat; spelled out so the host has no UB.) */
 SLM_FN int32_t slm_f2i(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float2int_rz(x); /* cvt.rzi.s32.f32: truncates, saturates, NaN -> 0 */
+#else
     if (slm_isnan(x)) return 0;
     if (x >= 2147483648.0f) return 2147483647;
     if (x <= -2147483648.0f) return (int32_t)(-2147483647 - 1);
     return (int32_t)x;
+#endif
 }
 /* WGSL f32(i32): round to nearest even. */
 SLM_FN float slm_i2f(int32_t i) { return (float)i; }
@@ -158,16 +174,30 @@ SLM_FN float slm_i2f(int32_t i) { return (float)i; }
 /* ---------------------------------------------------------- sin and cos */
 /* Reduce x to r in about [-pi/4, pi/4] and quadrant q in 0..3 with
  * x = (4k + q) * pi/2 + r. */
+SLM_FN int slm_clz64(uint64_t a) {
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)a);
+#else
+    return __builtin_clzll(a);
+#endif
+}
+
+/* Reduce x to r in about [-pi/4, pi/4] and quadrant q in 0..3 with
+ * x = (4k + q) * pi/2 + r. */
 SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
     if (slm_abs(x) < 4096.0f) {
-        /* Cody-Waite: P1 has its last bit at 2^-23, so the first fma is exact
-         * for every |x| < 4096; the two later parts restore the lost bits. */
-        float j = rintf(slm_mul(x, SLM_TWO_OVER_PI_F));
+        /* Cody-Waite.  j = rint(x * 2/pi) by adding and removing 1.5 * 2^23
+         * (exact round-to-nearest-even for |j| < 2^22); the low bits of the
+         * biased sum are j mod 4.  SLM_PIO2_1 has its last bit at 2^-23, so
+         * the first fma is exact for every |x| < 4096; the two later parts
+         * restore the lost bits. */
+        float biased = slm_add(slm_mul(x, SLM_TWO_OVER_PI_F), 12582912.0f);
+        float j = slm_sub(biased, 12582912.0f);
         float r = slm_fma(-j, SLM_PIO2_1, x);
         r = slm_fma(-j, SLM_PIO2_2, r);
         r = slm_fma(-j, SLM_PIO2_3, r);
         *r_out = r;
-        *q_out = ((int32_t)j) & 3;
+        *q_out = (int)(slm_f2u_bits(biased) & 3u);
         return;
     }
     uint32_t ix = slm_f2u_bits(x);
@@ -204,13 +234,24 @@ SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
     uint32_t ipart = (uint32_t)(c >> 30) & 3u;
     uint64_t frac64 = ((c & 0x3fffffffull) << 34) | ((uint64_t)limb1 << 2) | (limb0 >> 30);
     /* Round to the nearest quadrant: a fraction >= 1/2 becomes negative. */
-    int64_t fs = (int64_t)frac64;
     uint32_t q = (ipart + (uint32_t)(frac64 >> 63)) & 3u;
-    int64_t fs2 = fs >> 1; /* units of 2^-63 quadrants, |fs2| <= 2^62 */
-    float hi = (float)fs2;
-    int64_t lo_i = fs2 - (int64_t)hi;
-    float lo = (float)lo_i;
-    float r = slm_fma(hi, SLM_PH_CH, slm_fma(hi, SLM_PH_CL, slm_mul(lo, SLM_PH_CH)));
+    int neg = (int)(frac64 >> 63);
+    uint64_t a = neg ? (0ull - frac64) : frac64; /* |fraction| * 2^64 */
+    float r = 0.0f;
+    if (a != 0) {
+        /* 30 leading bits as a 24-bit head plus an exact correction, both
+         * scaled by a power of two built in the exponent field: only 32-bit
+         * conversions. */
+        int lz = slm_clz64(a);
+        uint32_t t = (uint32_t)((a << lz) >> 34); /* in [2^29, 2^30) */
+        float hi = (float)(int32_t)t;
+        float lo = (float)((int32_t)t - (int32_t)hi);
+        float scale = slm_u2f_bits((uint32_t)(127 - 30 - lz) << 23); /* 2^(-30-lz) */
+        float rh = slm_mul(hi, scale);
+        float rl = slm_mul(lo, scale);
+        r = slm_fma(rh, SLM_PIO2_1, slm_fma(rh, SLM_PIO2_2, slm_mul(rl, SLM_PIO2_1)));
+        if (neg) r = -r;
+    }
     if (ix >> 31) {
         r = -r;
         q = (4u - q) & 3u;
@@ -233,15 +274,11 @@ SLM_FN void slm_sincos(float x, float* s_out, float* c_out) {
     pc = slm_fma(z, pc, SLM_C2);
     pc = slm_fma(z, pc, SLM_C1);
     float c = slm_fma(z, pc, 1.0f);
-    float so, co;
-    switch (q) {
-    case 0: so = s; co = c; break;
-    case 1: so = c; co = -s; break;
-    case 2: so = -s; co = -c; break;
-    default: so = -c; co = s; break;
-    }
-    *s_out = so;
-    *c_out = co;
+    /* quadrant q: (sin, cos) = (s, c), (c, -s), (-s, -c), (-c, s) */
+    float a = (q & 1) ? c : s;
+    float bb = (q & 1) ? s : c;
+    *s_out = (q & 2) ? -a : a;
+    *c_out = ((q + 1) & 2) ? -bb : bb;
 }
 
 SLM_FN float slm_sin(float x) { float s, c; slm_sincos(x, &s, &c); return s; }

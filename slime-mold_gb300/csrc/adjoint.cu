@@ -205,6 +205,7 @@ int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every) 
     a.n_ckpt = (n_steps + K - 1) / K;
     a.dev = ctx->dev;
     a.tile = ctx->tile;
+    a.agent_shape = ctx->agent_shape;
     a.rate_active = (ctx->params.diffusion_rate > 0.0f && ctx->params.diffusion_rate < 1.0f) ? 1u : 0u;
     a.n = ctx->agents.n;
     a.n_pad = n_pad;
@@ -284,7 +285,7 @@ int slime_backward(slime_ctx* ctx, const float* dl_dtrail_final, SlimeGrads* gra
         for (uint32_t i = 0; i < m; i++) {
             float* Ti = a.seg_trail + (size_t)i * cells;
             uint32_t* Ki = a.seg_counts + (size_t)i * cells;
-            CK(launch_agents(a.dev, tmp, Ti, Ki, ctx->stream), "replaying agents");
+            CK(launch_agents(a.dev, tmp, Ti, Ki, ctx->stream, a.agent_shape), "replaying agents");
             ctx->launches++;
             if (i + 1 < m) {
                 CK(launch_trail(a.dev, a.tile, Ti, Ki, Ti + cells, nullptr, ctx->stream), "replaying trail");

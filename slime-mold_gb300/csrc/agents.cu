@@ -11,108 +11,91 @@
 //     read-only path (12 loads/agent, L2-resident at 4096^2);
 //   * the deposit is one 32-bit atomic increment of the cell's count; the trail
 //     pass folds the counts into the trail deterministically.
+#include "agent_step.cuh"
 #include "kernels.h"
 
 namespace slime {
 namespace {
 
-// sample_trail_map, compute.wgsl:7-29 (x1 >= W written as x0 >= W - 1).
-__device__ __forceinline__ float sample_trail(const float* __restrict__ trail, int W, int H, float px, float py) {
-    int x0 = slm_f2i(floorf(px));
-    int y0 = slm_f2i(floorf(py));
-    if (x0 < 0 || x0 >= W - 1 || y0 < 0 || y0 >= H - 1) return 0.0f;
-    float dx = slm_sub(px, slm_i2f(x0));
-    float dy = slm_sub(py, slm_i2f(y0));
-    const float* r0 = trail + (y0 * W + x0);
-    float v00 = __ldg(r0);
-    float v10 = __ldg(r0 + 1);
-    float v01 = __ldg(r0 + W);
-    float v11 = __ldg(r0 + W + 1);
-    float v0 = slm_mix(v00, v10, dx);
-    float v1 = slm_mix(v01, v11, dx);
-    return slm_mix(v0, v1, dy);
-}
+inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
-// One agent, compute.wgsl:65-144.  Returns the deposit cell or -1.
-__device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,
-                                          int32_t index, const float* __restrict__ trail) {
-    speed = slm_clamp(speed, p.speed_min, p.speed_max);
-
-    float sl, cl, sr, cr, sc, cc;
-    slm_sincos(slm_sub(angle, p.sensor_angle), &sl, &cl);
-    slm_sincos(slm_add(angle, p.sensor_angle), &sr, &cr);
-    slm_sincos(angle, &sc, &cc);
-    float left = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)),
-                              slm_add(y, slm_mul(p.sensor_dist, sl)));
-    float right = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)),
-                               slm_add(y, slm_mul(p.sensor_dist, sr)));
-    float center = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)),
-                                slm_add(y, slm_mul(p.sensor_dist, sc)));
-
-    if (center > left && center > right) {
-        // straight
-    } else if (left > right) {
-        float diff = slm_sub(slm_sub(angle, SLM_WGSL_TAU), angle);
-        angle = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
-    } else if (right > left) {
-        float diff = slm_sub(slm_add(angle, SLM_WGSL_TAU), angle);
-        angle = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
+// Vector access to APT consecutive slots (float, float2, float4).
+template <int APT>
+struct Lanes;
+template <>
+struct Lanes<1> {
+    __device__ static void load(const float* p, float* v) { v[0] = __ldcs(p); }
+    __device__ static void store(float* p, const float* v) { __stcs(p, v[0]); }
+    __device__ static void load_ids(const uint32_t* p, uint32_t* v) { v[0] = __ldcs(p); }
+};
+template <>
+struct Lanes<2> {
+    __device__ static void load(const float* p, float* v) {
+        float2 t = __ldcs(reinterpret_cast<const float2*>(p));
+        v[0] = t.x;
+        v[1] = t.y;
     }
+    __device__ static void store(float* p, const float* v) { __stcs(reinterpret_cast<float2*>(p), make_float2(v[0], v[1])); }
+    __device__ static void load_ids(const uint32_t* p, uint32_t* v) {
+        uint2 t = __ldcs(reinterpret_cast<const uint2*>(p));
+        v[0] = t.x;
+        v[1] = t.y;
+    }
+};
+template <>
+struct Lanes<4> {
+    __device__ static void load(const float* p, float* v) {
+        float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+        v[0] = t.x;
+        v[1] = t.y;
+        v[2] = t.z;
+        v[3] = t.w;
+    }
+    __device__ static void store(float* p, const float* v) {
+        __stcs(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+    }
+    __device__ static void load_ids(const uint32_t* p, uint32_t* v) {
+        uint4 t = __ldcs(reinterpret_cast<const uint4*>(p));
+        v[0] = t.x;
+        v[1] = t.y;
+        v[2] = t.z;
+        v[3] = t.w;
+    }
+};
 
-    float rv = slm_jitter_hash(index, x, y);
-    angle = slm_add(angle, slm_mul(slm_sub(slm_mul(rv, 2.0f), 1.0f), p.jitter));
-    angle = slm_fmod(angle, SLM_WGSL_TWO_PI);
-    if (angle < 0.0f) angle = slm_add(angle, SLM_WGSL_TWO_PI);
-
-    float move = slm_mul(speed, p.time_step);
-    float sm, cm;
-    slm_sincos(angle, &sm, &cm);
-    x = slm_add(x, slm_mul(move, cm));
-    y = slm_add(y, slm_mul(move, sm));
-    x = slm_fmod(x, p.Wf);
-    if (x < 0.0f) x = slm_add(x, p.Wf);
-    y = slm_fmod(y, p.Hf);
-    if (y < 0.0f) y = slm_add(y, p.Hf);
-
-    int dx = slm_f2i(x);
-    int dy = slm_f2i(y);
-    if (dx >= 0 && dx < p.W && dy >= 0 && dy < p.H) return dy * p.W + dx;
-    return -1;
-}
-
-template <bool kIds>
-__global__ void __launch_bounds__(256) agents_kernel(const __grid_constant__ DevParams p, float4* __restrict__ X,
-                                                     float4* __restrict__ Y, float4* __restrict__ TH,
-                                                     float4* __restrict__ V, const uint4* __restrict__ ids,
-                                                     const float* __restrict__ trail, uint32_t* __restrict__ counts,
-                                                     uint32_t n_groups, uint64_t n) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+// A thread moves APT consecutive slots with one vector load/store per field.
+template <int APT, int BS, bool kIds>
+__global__ void __launch_bounds__(BS) agents_kernel(const __grid_constant__ DevParams p, float* __restrict__ X,
+                                                    float* __restrict__ Y, float* __restrict__ TH,
+                                                    float* __restrict__ V, const uint32_t* __restrict__ ids,
+                                                    const float* __restrict__ trail, uint32_t* __restrict__ counts,
+                                                    uint32_t n_groups, uint64_t n) {
+    const uint32_t g = blockIdx.x * BS + threadIdx.x;
     if (g >= n_groups) return;
-    float4 x = __ldcs(X + g);
-    float4 y = __ldcs(Y + g);
-    float4 th = __ldcs(TH + g);
-    float4 v = __ldcs(V + g);
-    uint4 id;
+    const uint64_t base = (uint64_t)g * APT;
+    float x[APT], y[APT], th[APT], v[APT];
+    uint32_t id[APT];
+    Lanes<APT>::load(X + base, x);
+    Lanes<APT>::load(Y + base, y);
+    Lanes<APT>::load(TH + base, th);
+    Lanes<APT>::load(V + base, v);
     if (kIds) {
-        id = __ldcs(ids + g);
+        Lanes<APT>::load_ids(ids + base, id);
     } else {
-        uint32_t b = 4u * g;
-        id = make_uint4(b, b + 1, b + 2, b + 3);
+#pragma unroll
+        for (int j = 0; j < APT; j++) id[j] = (uint32_t)(base + j);
     }
-    uint64_t base = 4ull * g;
-    int c0 = -1, c1 = -1, c2 = -1, c3 = -1;
-    if (base + 0 < n) c0 = agent_step(p, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
-    if (base + 1 < n) c1 = agent_step(p, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
-    if (base + 2 < n) c2 = agent_step(p, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
-    if (base + 3 < n) c3 = agent_step(p, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
-    if (c0 >= 0) atomicAdd(counts + c0, 1u);
-    if (c1 >= 0) atomicAdd(counts + c1, 1u);
-    if (c2 >= 0) atomicAdd(counts + c2, 1u);
-    if (c3 >= 0) atomicAdd(counts + c3, 1u);
-    __stcs(X + g, x);
-    __stcs(Y + g, y);
-    __stcs(TH + g, th);
-    __stcs(V + g, v);
+    int cell[APT];
+#pragma unroll
+    for (int j = 0; j < APT; j++)
+        cell[j] = (base + j < n) ? agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail) : -1;
+#pragma unroll
+    for (int j = 0; j < APT; j++)
+        if (cell[j] >= 0) atomicAdd(counts + cell[j], 1u);
+    Lanes<APT>::store(X + base, x);
+    Lanes<APT>::store(Y + base, y);
+    Lanes<APT>::store(TH + base, th);
+    Lanes<APT>::store(V + base, v);
 }
 
 __global__ void aos_to_soa_kernel(const float4* __restrict__ aos, float* __restrict__ x, float* __restrict__ y,
@@ -171,22 +154,38 @@ __global__ void scale_positions_kernel(float* __restrict__ x, float* __restrict_
     y[i] = slm_mul(y[i], sy);
 }
 
-inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+template <int APT, int BS>
+cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
+                                  cudaStream_t s) {
+    uint32_t n_groups = (uint32_t)((a.n + APT - 1) / APT);
+    unsigned blocks = blocks_for(n_groups, BS);
+    if (a.ids)
+        agents_kernel<APT, BS, true><<<blocks, BS, 0, s>>>(p, a.x, a.y, a.th, a.v, a.ids, trail, counts, n_groups,
+                                                           a.n);
+    else
+        agents_kernel<APT, BS, false><<<blocks, BS, 0, s>>>(p, a.x, a.y, a.th, a.v, nullptr, trail, counts,
+                                                            n_groups, a.n);
+    return cudaGetLastError();
+}
 
 } // namespace
 
+// Agent-kernel shapes: (agents per thread, threads per block).
+const AgentShape kAgentShapes[] = {{4, 256}, {2, 256}, {1, 256}, {4, 128}, {1, 128}};
+
+int agent_shape_count() { return (int)(sizeof(kAgentShapes) / sizeof(kAgentShapes[0])); }
+AgentShape agent_shape(int i) { return kAgentShapes[(i >= 0 && i < agent_shape_count()) ? i : 0]; }
+
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
-                          cudaStream_t s) {
+                          cudaStream_t s, int shape) {
     if (a.n == 0) return cudaSuccess;
-    uint32_t n_groups = (uint32_t)((a.n + 3) / 4);
-    unsigned blocks = blocks_for(n_groups, 256);
-    if (a.ids)
-        agents_kernel<true><<<blocks, 256, 0, s>>>(p, (float4*)a.x, (float4*)a.y, (float4*)a.th, (float4*)a.v,
-                                                   (const uint4*)a.ids, trail, counts, n_groups, a.n);
-    else
-        agents_kernel<false><<<blocks, 256, 0, s>>>(p, (float4*)a.x, (float4*)a.y, (float4*)a.th, (float4*)a.v,
-                                                    nullptr, trail, counts, n_groups, a.n);
-    return cudaGetLastError();
+    switch (shape) {
+    case 1: return launch_agents_variant<2, 256>(p, a, trail, counts, s);
+    case 2: return launch_agents_variant<1, 256>(p, a, trail, counts, s);
+    case 3: return launch_agents_variant<4, 128>(p, a, trail, counts, s);
+    case 4: return launch_agents_variant<1, 128>(p, a, trail, counts, s);
+    default: return launch_agents_variant<4, 256>(p, a, trail, counts, s);
+    }
 }
 
 cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s) {

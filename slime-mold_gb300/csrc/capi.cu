@@ -210,7 +210,8 @@ void invalidate_graphs(slime_ctx* ctx) {
 // Enqueue one step on the context's stream (also used under capture).
 cudaError_t enqueue_step(slime_ctx* ctx) {
     const int cur = ctx->cur;
-    cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream);
+    cudaError_t e =
+        launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, ctx->agent_shape);
     if (e != cudaSuccess) return e;
     e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
                      ctx->counts[1 - cur], ctx->stream);
@@ -411,11 +412,17 @@ int slime_set_options(slime_ctx* ctx, const SlimeOptions* o) {
                          trail_tile_count());
     if (o->reorder_cell_log2 > 15)
         return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "reorder_cell_log2 must be <= 15");
+    if (o->agent_shape > (uint32_t)agent_shape_count())
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "agent_shape out of range (0..%d)",
+                         agent_shape_count());
+    if (o->reserved != 0) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "options.reserved must be 0");
     ctx->opt = *o;
     if (ctx->opt.graph_chunk == 0) ctx->opt.graph_chunk = 50;
     int tile = o->trail_tile ? (int)o->trail_tile - 1 : (ctx->tuned_tile >= 0 ? ctx->tuned_tile : trail_tile_default());
-    if (tile != ctx->tile) {
+    int shape = o->agent_shape ? (int)o->agent_shape - 1 : (ctx->tuned_shape >= 0 ? ctx->tuned_shape : 0);
+    if (tile != ctx->tile || shape != ctx->agent_shape) {
         ctx->tile = tile;
+        ctx->agent_shape = shape;
         invalidate_graphs(ctx);
     }
     return SLIME_OK;
@@ -435,6 +442,7 @@ int slime_get_info(const slime_ctx* ctx, SlimeInfo* out) {
     out->steps_done = ctx->steps_done;
     out->kernel_launches = ctx->launches;
     out->trail_tile = (uint32_t)ctx->tile;
+    out->agent_shape = (uint32_t)ctx->agent_shape;
     out->reordered = ctx->reordered ? 1u : 0u;
     return SLIME_OK;
 }
@@ -624,7 +632,8 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
             rc = do_reorder(ctx);
         cudaEventRecord(ev[1], ctx->stream);
         const int cur = ctx->cur;
-        cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream);
+        cudaError_t e =
+            launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, ctx->agent_shape);
         cudaEventRecord(ev[2], ctx->stream);
         if (e == cudaSuccess)
             e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
@@ -664,10 +673,11 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "creating events");
     CK(cudaEventCreate(&e1), "creating events");
-    // The trial launches read trail[cur] and the (zero) counts[cur] and write
-    // the other buffers, so the state is untouched; the previous step's
-    // counts are overwritten with zeros.
     const int cur = ctx->cur;
+    const size_t cells = (size_t)ctx->W * ctx->H;
+    // 1. trail tiles.  The trial launches read trail[cur] and the (zero)
+    // counts[cur] and write the other buffers, so the state is untouched; the
+    // previous step's counts are overwritten with zeros.
     float best = 1e30f;
     int best_tile = ctx->tile;
     for (int t = 0; t < trail_tile_count(); t++) {
@@ -689,12 +699,50 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
             best_tile = t;
         }
     }
+    // 2. agent-kernel shapes, on a snapshot of the agents that is put back
+    // afterwards (the trial passes write agents and counts[cur]).
+    int best_shape = ctx->agent_shape;
+    if (ctx->agents.n > 0) {
+        const size_t abytes = 4 * ctx->agents.n_pad * sizeof(float);
+        void* snap = nullptr;
+        if (cudaMalloc(&snap, abytes) == cudaSuccess) {
+            CK(cudaMemcpyAsync(snap, ctx->agent_block, abytes, cudaMemcpyDeviceToDevice, ctx->stream), "snapshot");
+            float best_a = 1e30f;
+            for (int sh = 0; sh < agent_shape_count(); sh++) {
+                launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, sh);
+                cudaEventRecord(e0, ctx->stream);
+                for (uint32_t r = 0; r < reps; r++) {
+                    cudaMemcpyAsync(ctx->agent_block, snap, abytes, cudaMemcpyDeviceToDevice, ctx->stream);
+                    launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, sh);
+                }
+                cudaEventRecord(e1, ctx->stream);
+                CK(cudaEventSynchronize(e1), "autotuning");
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ctx->launches += reps + 1;
+                if (ms < best_a) {
+                    best_a = ms;
+                    best_shape = sh;
+                }
+            }
+            CK(cudaMemcpyAsync(ctx->agent_block, snap, abytes, cudaMemcpyDeviceToDevice, ctx->stream), "restore");
+            CK(cudaMemsetAsync(ctx->counts[cur], 0, cells * sizeof(uint32_t), ctx->stream), "restore");
+            CK(cudaStreamSynchronize(ctx->stream), "autotuning");
+            cudaFree(snap);
+        } else {
+            cudaGetLastError();
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ctx->last_counts_valid = false;
     ctx->tuned_tile = best_tile;
-    if (ctx->opt.trail_tile == 0 && best_tile != ctx->tile) {
-        ctx->tile = best_tile;
+    ctx->tuned_shape = best_shape;
+    int tile = ctx->opt.trail_tile ? (int)ctx->opt.trail_tile - 1 : best_tile;
+    int shape = ctx->opt.agent_shape ? (int)ctx->opt.agent_shape - 1 : best_shape;
+    if (tile != ctx->tile || shape != ctx->agent_shape) {
+        ctx->tile = tile;
+        ctx->agent_shape = shape;
         invalidate_graphs(ctx);
     }
     return SLIME_OK;

@@ -30,6 +30,8 @@ struct slime_ctx {
     SlimeOptions opt{};
     int tile = 0;
     int tuned_tile = -1;
+    int agent_shape = 0; // index into the agent-kernel shape table
+    int tuned_shape = -1;
 
     std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs; // (steps, start parity) -> graph
 
@@ -47,6 +49,7 @@ struct slime_ctx {
         uint32_t n_steps = 0, ckpt_every = 0, n_ckpt = 0;
         slime::DevParams dev{};          // parameters the recorded steps ran with
         int tile = 0;
+        int agent_shape = 0;
         uint32_t rate_active = 0;         // 0 < diffusion_rate < 1
         uint64_t n = 0, n_pad = 0;
         bool with_ids = false;

@@ -1,22 +1,677 @@
-// ensemble.cu - batched ensemble of independent colonies.
+// ensemble.cu - independent colonies of uneven sizes in one persistent launch
+// per step.
+//
+// All colonies' agents live in one SoA block (each colony padded to a
+// multiple of 128 slots) and all trails/counts in one ping-pong pair of
+// buffers.  One cooperative launch per step runs
+//   phase 1: agent work items (1,024 agents of one colony per block item),
+//   a grid-wide barrier (bounded spin: gives up after about a second and
+//            reports SLIME_ERR_DEVICE_TIMEOUT instead of hanging),
+//   phase 2: trail strips (128 columns x ROWS rows of one colony per warp
+//            item) through the same streaming code as the single-colony
+//            kernel.
+// Each colony keeps its own parameter block, so the colonies are exactly the
+// runs a single Simulation would produce for them (the tests compare bit for
+// bit).  The blur mode and radius must be common to all colonies (they select
+// the compiled strip variant); sigma, decay, diffusion and the agent
+// parameters may differ.
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "agent_step.cuh"
 #include "ctx.h"
+#include "kernels.h"
+#include "trail_stream.cuh"
+
+using namespace slime;
+
+namespace {
+
+constexpr int kEnsThreads = 256;
+constexpr int kAgentsPerItem = 4 * kEnsThreads; // one float4 group per thread
+
+struct DevColony {
+    DevParams p;
+    uint64_t agent_off; // first slot of the colony in each SoA array
+    uint64_t n;         // live agents
+    uint64_t trail_off; // first cell of the colony in the trail/count buffers
+    int32_t warps_x;    // 128-column strips per row band
+    int32_t pad;
+};
+
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+    int error;
+    int pad;
+};
+
+struct Colony {
+    uint32_t W, H;
+    uint64_t n, n_pad, agent_off, trail_off;
+    SlimeParams params;
+    DevParams dev;
+};
+
+// Bounded grid barrier: every block arrives once; the last one to arrive
+// releases the others.  A waiter gives up after ~1 s of clock64() cycles,
+// flags the error and returns false (the kernel then skips its second phase).
+__device__ bool grid_barrier(GridBarrier* b, unsigned nblocks) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int* vgen = &b->gen;
+        unsigned int gen = *vgen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(&b->count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            long long t0 = clock64();
+            while (*vgen == gen) {
+                if (clock64() - t0 > 2000000000ll) {
+                    atomicExch(&b->error, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int R, bool kGauss, int ROWS>
+__global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
+    const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
+    const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
+    float* __restrict__ TH, float* __restrict__ V, const float* __restrict__ trail_in, uint32_t* counts_in,
+    float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar) {
+    __shared__ DevParams sp;
+    // ---- phase 1: agents
+    for (uint32_t item = blockIdx.x; item < n_agent_items; item += gridDim.x) {
+        const uint2 it = agent_items[item];
+        __syncthreads();
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(&cols[it.x].p);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&sp);
+            for (int w = threadIdx.x; w < (int)(sizeof(DevParams) / 4); w += kEnsThreads) dst[w] = src[w];
+        }
+        __syncthreads();
+        const DevColony& c = cols[it.x];
+        const uint64_t g = (uint64_t)it.y + threadIdx.x; // float4 group within the colony
+        const uint64_t base = 4 * g;
+        if (base >= c.n) continue;
+        const uint64_t slot = c.agent_off + base;
+        float4* px = reinterpret_cast<float4*>(X + slot);
+        float4* py = reinterpret_cast<float4*>(Y + slot);
+        float4* pt = reinterpret_cast<float4*>(TH + slot);
+        float4* pv = reinterpret_cast<float4*>(V + slot);
+        float4 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
+        const float* trail = trail_in + c.trail_off;
+        uint32_t* counts = counts_in + c.trail_off;
+        int c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)base, trail);
+        int c1 = -1, c2 = -1, c3 = -1;
+        if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)(base + 1), trail);
+        if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)(base + 2), trail);
+        if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)(base + 3), trail);
+        if (c0 >= 0) atomicAdd(counts + c0, 1u);
+        if (c1 >= 0) atomicAdd(counts + c1, 1u);
+        if (c2 >= 0) atomicAdd(counts + c2, 1u);
+        if (c3 >= 0) atomicAdd(counts + c3, 1u);
+        __stcs(px, x);
+        __stcs(py, y);
+        __stcs(pt, th);
+        __stcs(pv, v);
+    }
+    // ---- grid-wide barrier: all deposits of this step are counted
+    __threadfence();
+    if (!grid_barrier(bar, gridDim.x)) return;
+    // ---- phase 2: trail strips, one warp per item
+    const uint32_t warps = gridDim.x * (kEnsThreads / 32);
+    const uint32_t gw = blockIdx.x * (kEnsThreads / 32) + (threadIdx.x >> 5);
+    for (uint32_t item = gw; item < n_strip_items; item += warps) {
+        const uint4 it = strip_items[item];
+        const DevColony& c = cols[it.x];
+        process_strip<R, kGauss, ROWS, true>(c.p, trail_in + c.trail_off, counts_in + c.trail_off,
+                                             trail_out + c.trail_off, counts_zero + c.trail_off, (int)it.y,
+                                             (int)it.z);
+    }
+}
+
+typedef void (*EnsKernel)(const DevColony*, const uint2*, uint32_t, const uint4*, uint32_t, float*, float*, float*,
+                          float*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*);
+
+template <int ROWS>
+EnsKernel pick_rows(int R, bool gauss) {
+    if (!gauss) return ensemble_step_kernel<1, false, ROWS>;
+    if (R == 1) return ensemble_step_kernel<1, true, ROWS>;
+    return ensemble_step_kernel<2, true, ROWS>;
+}
+
+EnsKernel pick_kernel(int rows, int R, bool gauss) {
+    switch (rows) {
+    case 8: return pick_rows<8>(R, gauss);
+    case 32: return pick_rows<32>(R, gauss);
+    default: return pick_rows<16>(R, gauss);
+    }
+}
+
+} // namespace
+
+struct slime_ensemble {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<Colony> colonies;
+    uint64_t total_slots = 0, total_cells = 0;
+    float* agent_block = nullptr; // x | y | angle | speed, total_slots each
+    float* trail[2] = {nullptr, nullptr};
+    uint32_t* counts[2] = {nullptr, nullptr};
+    int cur = 0;
+    DevColony* d_cols = nullptr;
+    uint2* d_agent_items = nullptr;
+    uint32_t n_agent_items = 0;
+    uint4* d_strip_items = nullptr;
+    uint32_t n_strip_items = 0;
+    GridBarrier* d_bar = nullptr;
+    float4* staging = nullptr;
+    size_t staging_bytes = 0;
+    int rows = 16;
+    int R = 1;
+    bool gauss = false;
+    int grid = 0;
+    int blocks_per_sm = 0;
+    bool use_graphs = true;
+    std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs;
+    uint64_t launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int ens_fail(slime_ensemble* e, int code, const char* msg) {
+    e->err = msg;
+    return code;
+}
+
+#define ECK(expr, what)                                                                                     \
+    do {                                                                                                    \
+        cudaError_t _e = (expr);                                                                            \
+        if (_e != cudaSuccess) return cuda_error(e->err, _e, what);                                         \
+    } while (0)
+
+void ens_invalidate(slime_ensemble* e) {
+    for (auto& kv : e->graphs) cudaGraphExecDestroy(kv.second);
+    e->graphs.clear();
+}
+
+int upload_cols(slime_ensemble* e) {
+    std::vector<DevColony> dc(e->colonies.size());
+    for (size_t j = 0; j < e->colonies.size(); j++) {
+        const Colony& c = e->colonies[j];
+        memset(&dc[j], 0, sizeof(DevColony));
+        dc[j].p = c.dev;
+        dc[j].agent_off = c.agent_off;
+        dc[j].n = c.n;
+        dc[j].trail_off = c.trail_off;
+        dc[j].warps_x = (int32_t)((c.W + 127) / 128);
+    }
+    ECK(cudaMemcpyAsync(e->d_cols, dc.data(), dc.size() * sizeof(DevColony), cudaMemcpyHostToDevice, e->stream),
+        "uploading colony table");
+    ECK(cudaStreamSynchronize(e->stream), "uploading colony table");
+    return SLIME_OK;
+}
+
+int build_strip_items(slime_ensemble* e) {
+    std::vector<uint4> items;
+    for (size_t j = 0; j < e->colonies.size(); j++) {
+        const Colony& c = e->colonies[j];
+        uint32_t wx = (c.W + 127) / 128, strips = (c.H + e->rows - 1) / e->rows;
+        for (uint32_t rs = 0; rs < strips; rs++)
+            for (uint32_t cw = 0; cw < wx; cw++) items.push_back(make_uint4((uint32_t)j, cw, rs, 0));
+    }
+    if (e->d_strip_items) cudaFree(e->d_strip_items);
+    e->d_strip_items = nullptr;
+    ECK(cudaMalloc(&e->d_strip_items, items.size() * sizeof(uint4)), "allocating strip table");
+    ECK(cudaMemcpy(e->d_strip_items, items.data(), items.size() * sizeof(uint4), cudaMemcpyHostToDevice),
+        "uploading strip table");
+    e->n_strip_items = (uint32_t)items.size();
+    return SLIME_OK;
+}
+
+int size_grid(slime_ensemble* e) {
+    EnsKernel k = pick_kernel(e->rows, e->R, e->gauss);
+    int per_sm = 0, sms = 0;
+    ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEnsThreads, 0), "occupancy query");
+    ECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device), "SM count");
+    if (per_sm < 1) return ens_fail(e, SLIME_ERR_CUDA, "ensemble kernel cannot be resident");
+    int want = e->blocks_per_sm > 0 ? (e->blocks_per_sm < per_sm ? e->blocks_per_sm : per_sm) : per_sm;
+    e->grid = want * sms;
+    return SLIME_OK;
+}
+
+cudaError_t enqueue_ens_step(slime_ensemble* e) {
+    const int cur = e->cur;
+    EnsKernel k = pick_kernel(e->rows, e->R, e->gauss);
+    float* X = e->agent_block;
+    float* Y = X + e->total_slots;
+    float* TH = Y + e->total_slots;
+    float* V = TH + e->total_slots;
+    const DevColony* cols = e->d_cols;
+    const uint2* ai = e->d_agent_items;
+    uint32_t nai = e->n_agent_items;
+    const uint4* si = e->d_strip_items;
+    uint32_t nsi = e->n_strip_items;
+    const float* tin = e->trail[cur];
+    uint32_t* cin = e->counts[cur];
+    float* tout = e->trail[1 - cur];
+    uint32_t* cz = e->counts[1 - cur];
+    GridBarrier* bar = e->d_bar;
+    void* args[] = {&cols, &ai, &nai, &si, &nsi, &X, &Y, &TH, &V, &tin, &cin, &tout, &cz, &bar};
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(e->grid);
+    cfg.blockDim = dim3(kEnsThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = e->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t err = cudaLaunchKernelExC(&cfg, (const void*)k, args);
+    if (err != cudaSuccess) return err;
+    e->cur = 1 - cur;
+    return cudaSuccess;
+}
+
+int check_barrier(slime_ensemble* e) {
+    GridBarrier b;
+    ECK(cudaMemcpyAsync(&b, e->d_bar, sizeof b, cudaMemcpyDeviceToHost, e->stream), "reading barrier state");
+    ECK(cudaStreamSynchronize(e->stream), "reading barrier state");
+    if (b.error) {
+        cudaMemsetAsync(e->d_bar, 0, sizeof(GridBarrier), e->stream);
+        cudaStreamSynchronize(e->stream);
+        return ens_fail(e, SLIME_ERR_DEVICE_TIMEOUT, "the ensemble's grid barrier timed out");
+    }
+    return SLIME_OK;
+}
+
+int run_ens_steps(slime_ensemble* e, uint32_t n) {
+    const uint32_t chunk = 50;
+    while (n > 0) {
+        uint32_t m = n < chunk ? n : chunk;
+        if (e->use_graphs) {
+            auto key = std::make_pair(m, e->cur);
+            auto it = e->graphs.find(key);
+            cudaGraphExec_t exec = nullptr;
+            if (it == e->graphs.end()) {
+                const int saved = e->cur;
+                cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+                for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_ens_step(e);
+                cudaGraph_t g = nullptr;
+                cudaError_t ee = cudaStreamEndCapture(e->stream, &g);
+                e->cur = saved;
+                if (ce == cudaSuccess && ee == cudaSuccess) ee = cudaGraphInstantiate(&exec, g, 0);
+                if (g) cudaGraphDestroy(g);
+                if (ce != cudaSuccess || ee != cudaSuccess) {
+                    // cooperative launches that cannot be captured run directly
+                    cudaGetLastError();
+                    e->use_graphs = false;
+                    continue;
+                }
+                e->graphs[key] = exec;
+            } else {
+                exec = it->second;
+            }
+            ECK(cudaGraphLaunch(exec, e->stream), "launching ensemble graph");
+            if (m & 1) e->cur = 1 - e->cur;
+        } else {
+            for (uint32_t i = 0; i < m; i++) ECK(enqueue_ens_step(e), "launching ensemble step");
+        }
+        e->launches += m;
+        n -= m;
+    }
+    return SLIME_OK;
+}
+
+int check_colony(slime_ensemble* e, uint32_t j) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    if (j >= e->colonies.size()) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "colony index out of range");
+    cudaSetDevice(e->device);
+    return SLIME_OK;
+}
+
+} // namespace
 
 extern "C" {
-slime_ensemble* slime_ensemble_create(uint32_t, const uint32_t*, const uint32_t*, const uint64_t*, const SlimeParams*, int* status) {
-    if (status) *status = SLIME_ERR_STATE;
-    return nullptr;
+
+slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const uint32_t* heights,
+                                      const uint64_t* n_agents, const SlimeParams* params, int* status) {
+    int dummy;
+    if (!status) status = &dummy;
+    *status = SLIME_ERR_INVALID_ARGUMENT;
+    if (k == 0 || !widths || !heights || !n_agents || !params) return nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        *status = SLIME_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    slime_ensemble* e = new slime_ensemble();
+    cudaGetDevice(&e->device);
+    uint64_t slots = 0, cells = 0;
+    for (uint32_t j = 0; j < k; j++) {
+        Colony c;
+        c.W = widths[j];
+        c.H = heights[j];
+        c.n = n_agents[j];
+        const char* why = nullptr;
+        if (c.W < 8 || c.H < 1 || c.W % 4 != 0 || (uint64_t)c.W * c.H >= (1ull << 31) || c.n >= (1ull << 31) ||
+            c.W > (1u << 24) || c.H > (1u << 24)) {
+            e->err = "each colony needs width % 4 == 0, width >= 8 and width*height < 2^31";
+            break;
+        }
+        if (!make_dev_params(params[j], c.W, c.H, &c.dev, &why)) {
+            e->err = why;
+            break;
+        }
+        int R = params[j].blur_mode == SLIME_BLUR_GAUSS ? c.dev.R : 1;
+        if (R < 1 || R > 2) {
+            e->err = "ensemble blur radius must be 1 or 2";
+            break;
+        }
+        if (j == 0) {
+            e->R = R;
+            e->gauss = params[j].blur_mode == SLIME_BLUR_GAUSS;
+        } else if (R != e->R || e->gauss != (params[j].blur_mode == SLIME_BLUR_GAUSS)) {
+            e->err = "all colonies must share blur mode and radius";
+            break;
+        }
+        c.params = params[j];
+        c.params.width = c.W;
+        c.params.height = c.H;
+        c.n_pad = (c.n + kAgentPad - 1) / kAgentPad * kAgentPad;
+        c.agent_off = slots;
+        c.trail_off = cells;
+        slots += c.n_pad;
+        cells += (uint64_t)c.W * c.H;
+        // keep every colony's first cell 16-byte aligned
+        cells = (cells + 3) & ~3ull;
+        e->colonies.push_back(c);
+    }
+    if (e->colonies.size() != k) {
+        *status = SLIME_ERR_INVALID_ARGUMENT;
+        slime_ensemble_destroy(e);
+        return nullptr;
+    }
+    e->total_slots = slots ? slots : kAgentPad;
+    e->total_cells = cells;
+    // agent work items: 1,024 agents of one colony each
+    std::vector<uint2> ai;
+    for (uint32_t j = 0; j < k; j++) {
+        uint64_t groups = (e->colonies[j].n + 3) / 4;
+        for (uint64_t g0 = 0; g0 < groups; g0 += kEnsThreads) ai.push_back(make_uint2(j, (uint32_t)g0));
+    }
+    e->n_agent_items = (uint32_t)ai.size();
+    int rc = SLIME_OK;
+    cudaError_t ce = cudaSuccess;
+    do {
+        if ((ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) break;
+        if ((ce = cudaMalloc(&e->agent_block, 4 * e->total_slots * sizeof(float))) != cudaSuccess) break;
+        if ((ce = cudaMemset(e->agent_block, 0, 4 * e->total_slots * sizeof(float))) != cudaSuccess) break;
+        for (int i = 0; i < 2 && ce == cudaSuccess; i++) {
+            if ((ce = cudaMalloc(&e->trail[i], e->total_cells * sizeof(float))) != cudaSuccess) break;
+            if ((ce = cudaMalloc(&e->counts[i], e->total_cells * sizeof(uint32_t))) != cudaSuccess) break;
+            if ((ce = cudaMemset(e->trail[i], 0, e->total_cells * sizeof(float))) != cudaSuccess) break;
+            ce = cudaMemset(e->counts[i], 0, e->total_cells * sizeof(uint32_t));
+        }
+        if (ce != cudaSuccess) break;
+        if ((ce = cudaMalloc(&e->d_cols, k * sizeof(DevColony))) != cudaSuccess) break;
+        if ((ce = cudaMalloc(&e->d_agent_items, (ai.size() ? ai.size() : 1) * sizeof(uint2))) != cudaSuccess) break;
+        if (ai.size() &&
+            (ce = cudaMemcpy(e->d_agent_items, ai.data(), ai.size() * sizeof(uint2), cudaMemcpyHostToDevice)) !=
+                cudaSuccess)
+            break;
+        if ((ce = cudaMalloc(&e->d_bar, sizeof(GridBarrier))) != cudaSuccess) break;
+        ce = cudaMemset(e->d_bar, 0, sizeof(GridBarrier));
+    } while (0);
+    if (ce != cudaSuccess) rc = cuda_error(e->err, ce, "creating the ensemble");
+    if (rc == SLIME_OK) rc = upload_cols(e);
+    if (rc == SLIME_OK) rc = build_strip_items(e);
+    if (rc == SLIME_OK) rc = size_grid(e);
+    if (rc != SLIME_OK) {
+        *status = rc;
+        slime_ensemble_destroy(e);
+        return nullptr;
+    }
+    *status = SLIME_OK;
+    return e;
 }
-void slime_ensemble_destroy(slime_ensemble*) {}
-const char* slime_ensemble_last_error(const slime_ensemble*) { return "ensemble not built yet"; }
-int slime_ensemble_set_params(slime_ensemble*, uint32_t, const SlimeParams*) { return SLIME_ERR_STATE; }
-int slime_ensemble_upload_agents(slime_ensemble*, uint32_t, const float*, uint64_t) { return SLIME_ERR_STATE; }
-int slime_ensemble_download_agents(slime_ensemble*, uint32_t, float*, uint64_t) { return SLIME_ERR_STATE; }
-int slime_ensemble_seed_agents(slime_ensemble*, uint32_t, uint64_t, float, float) { return SLIME_ERR_STATE; }
-int slime_ensemble_upload_trail(slime_ensemble*, uint32_t, const float*, uint64_t) { return SLIME_ERR_STATE; }
-int slime_ensemble_download_trail(slime_ensemble*, uint32_t, float*, uint64_t) { return SLIME_ERR_STATE; }
-int slime_ensemble_step(slime_ensemble*, uint32_t) { return SLIME_ERR_STATE; }
-int slime_ensemble_sync(slime_ensemble*) { return SLIME_ERR_STATE; }
-int slime_ensemble_get_stream(slime_ensemble*, void**) { return SLIME_ERR_STATE; }
-int slime_ensemble_autotune(slime_ensemble*, uint32_t) { return SLIME_ERR_STATE; }
-int slime_ensemble_launch_count(const slime_ensemble*, uint64_t*) { return SLIME_ERR_STATE; }
+
+void slime_ensemble_destroy(slime_ensemble* e) {
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    ens_invalidate(e);
+    void* ptrs[] = {e->agent_block, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->d_cols,
+                    e->d_agent_items, e->d_strip_items, e->d_bar, e->staging};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
 }
+
+const char* slime_ensemble_last_error(const slime_ensemble* e) { return e ? e->err.c_str() : "null ensemble"; }
+
+int slime_ensemble_set_params(slime_ensemble* e, uint32_t j, const SlimeParams* params) {
+    int rc = check_colony(e, j);
+    if (rc != SLIME_OK) return rc;
+    if (!params) return SLIME_ERR_INVALID_ARGUMENT;
+    Colony& c = e->colonies[j];
+    DevParams d;
+    const char* why = nullptr;
+    if (!make_dev_params(*params, c.W, c.H, &d, &why)) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, why);
+    int R = params->blur_mode == SLIME_BLUR_GAUSS ? d.R : 1;
+    if (R != e->R || e->gauss != (params->blur_mode == SLIME_BLUR_GAUSS))
+        return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "all colonies must share blur mode and radius");
+    c.params = *params;
+    c.params.width = c.W;
+    c.params.height = c.H;
+    c.dev = d;
+    return upload_cols(e); // the colony table is read by the kernel: graphs stay valid
+}
+
+int slime_ensemble_upload_agents(slime_ensemble* e, uint32_t j, const float* aos, uint64_t n) {
+    int rc = check_colony(e, j);
+    if (rc != SLIME_OK) return rc;
+    Colony& c = e->colonies[j];
+    if (n != c.n || (!aos && n)) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "agent count mismatch");
+    if (n == 0) return SLIME_OK;
+    if (e->staging_bytes < n * sizeof(float4)) {
+        if (e->staging) cudaFree(e->staging);
+        e->staging = nullptr;
+        e->staging_bytes = 0;
+        ECK(cudaMalloc(&e->staging, n * sizeof(float4)), "allocating staging");
+        e->staging_bytes = n * sizeof(float4);
+    }
+    ECK(cudaMemcpyAsync(e->staging, aos, n * sizeof(float4), cudaMemcpyHostToDevice, e->stream), "uploading agents");
+    AgentsSoA a;
+    a.x = e->agent_block + c.agent_off;
+    a.y = e->agent_block + e->total_slots + c.agent_off;
+    a.th = e->agent_block + 2 * e->total_slots + c.agent_off;
+    a.v = e->agent_block + 3 * e->total_slots + c.agent_off;
+    a.n = n;
+    a.n_pad = c.n_pad;
+    ECK(launch_aos_to_soa(e->staging, a, e->stream), "converting agents");
+    ECK(cudaStreamSynchronize(e->stream), "uploading agents");
+    return SLIME_OK;
+}
+
+int slime_ensemble_download_agents(slime_ensemble* e, uint32_t j, float* aos, uint64_t n) {
+    int rc = check_colony(e, j);
+    if (rc != SLIME_OK) return rc;
+    Colony& c = e->colonies[j];
+    if (n != c.n || (!aos && n)) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "agent count mismatch");
+    if (n == 0) return SLIME_OK;
+    if (e->staging_bytes < n * sizeof(float4)) {
+        if (e->staging) cudaFree(e->staging);
+        e->staging = nullptr;
+        e->staging_bytes = 0;
+        ECK(cudaMalloc(&e->staging, n * sizeof(float4)), "allocating staging");
+        e->staging_bytes = n * sizeof(float4);
+    }
+    AgentsSoA a;
+    a.x = e->agent_block + c.agent_off;
+    a.y = e->agent_block + e->total_slots + c.agent_off;
+    a.th = e->agent_block + 2 * e->total_slots + c.agent_off;
+    a.v = e->agent_block + 3 * e->total_slots + c.agent_off;
+    a.n = n;
+    a.n_pad = c.n_pad;
+    ECK(launch_soa_to_aos(a, e->staging, e->stream), "converting agents");
+    ECK(cudaMemcpyAsync(aos, e->staging, n * sizeof(float4), cudaMemcpyDeviceToHost, e->stream), "downloading agents");
+    ECK(cudaStreamSynchronize(e->stream), "downloading agents");
+    return SLIME_OK;
+}
+
+int slime_ensemble_seed_agents(slime_ensemble* e, uint32_t j, uint64_t seed, float hmin, float hmax) {
+    int rc = check_colony(e, j);
+    if (rc != SLIME_OK) return rc;
+    Colony& c = e->colonies[j];
+    AgentsSoA a;
+    a.x = e->agent_block + c.agent_off;
+    a.y = e->agent_block + e->total_slots + c.agent_off;
+    a.th = e->agent_block + 2 * e->total_slots + c.agent_off;
+    a.v = e->agent_block + 3 * e->total_slots + c.agent_off;
+    a.n = c.n;
+    a.n_pad = c.n_pad;
+    ECK(launch_seed_agents(a, seed, (float)c.W, (float)c.H, hmin, hmax, c.params.agent_speed_min,
+                           c.params.agent_speed_max, e->stream),
+        "seeding agents");
+    ECK(cudaStreamSynchronize(e->stream), "seeding agents");
+    return SLIME_OK;
+}
+
+int slime_ensemble_upload_trail(slime_ensemble* e, uint32_t j, const float* trail, uint64_t n_cells) {
+    int rc = check_colony(e, j);
+    if (rc != SLIME_OK) return rc;
+    Colony& c = e->colonies[j];
+    if (!trail || n_cells != (uint64_t)c.W * c.H) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "trail size mismatch");
+    ECK(cudaMemcpyAsync(e->trail[e->cur] + c.trail_off, trail, n_cells * sizeof(float), cudaMemcpyHostToDevice,
+                        e->stream), "uploading trail");
+    ECK(cudaStreamSynchronize(e->stream), "uploading trail");
+    return SLIME_OK;
+}
+
+int slime_ensemble_download_trail(slime_ensemble* e, uint32_t j, float* trail, uint64_t n_cells) {
+    int rc = check_colony(e, j);
+    if (rc != SLIME_OK) return rc;
+    Colony& c = e->colonies[j];
+    if (!trail || n_cells != (uint64_t)c.W * c.H) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "trail size mismatch");
+    ECK(cudaMemcpyAsync(trail, e->trail[e->cur] + c.trail_off, n_cells * sizeof(float), cudaMemcpyDeviceToHost,
+                        e->stream), "downloading trail");
+    ECK(cudaStreamSynchronize(e->stream), "downloading trail");
+    return SLIME_OK;
+}
+
+int slime_ensemble_step(slime_ensemble* e, uint32_t n_steps) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(e->device);
+    return run_ens_steps(e, n_steps);
+}
+
+int slime_ensemble_sync(slime_ensemble* e) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(e->device);
+    ECK(cudaStreamSynchronize(e->stream), "synchronising");
+    return check_barrier(e);
+}
+
+int slime_ensemble_get_stream(slime_ensemble* e, void** stream) {
+    if (!e || !stream) return SLIME_ERR_INVALID_ARGUMENT;
+    *stream = (void*)e->stream;
+    return SLIME_OK;
+}
+
+// Time trial steps for every strip height and residency, keep the fastest,
+// and put the state back (snapshot of agents, trails and counts).
+int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(e->device);
+    if (reps == 0) reps = 3;
+    size_t abytes = 4 * e->total_slots * sizeof(float), tbytes = e->total_cells * sizeof(float);
+    void* snap = nullptr;
+    ECK(cudaMalloc(&snap, abytes + 2 * tbytes + 2 * tbytes), "allocating autotune snapshot");
+    char* s = (char*)snap;
+    cudaMemcpyAsync(s, e->agent_block, abytes, cudaMemcpyDeviceToDevice, e->stream);
+    for (int i = 0; i < 2; i++) {
+        cudaMemcpyAsync(s + abytes + i * tbytes, e->trail[i], tbytes, cudaMemcpyDeviceToDevice, e->stream);
+        cudaMemcpyAsync(s + abytes + 2 * tbytes + i * tbytes, e->counts[i], tbytes, cudaMemcpyDeviceToDevice,
+                        e->stream);
+    }
+    const int saved_cur = e->cur;
+    const bool saved_graphs = e->use_graphs;
+    e->use_graphs = false;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best_rows = e->rows, best_bps = e->blocks_per_sm;
+    float best = 1e30f;
+    const int rows_opts[] = {8, 16, 32};
+    const int bps_opts[] = {0, 2, 4};
+    int rc = SLIME_OK;
+    for (int ro : rows_opts) {
+        for (int bo : bps_opts) {
+            e->rows = ro;
+            e->blocks_per_sm = bo;
+            if ((rc = build_strip_items(e)) != SLIME_OK || (rc = size_grid(e)) != SLIME_OK) break;
+            run_ens_steps(e, 1); // warm-up
+            cudaEventRecord(e0, e->stream);
+            run_ens_steps(e, reps);
+            cudaEventRecord(e1, e->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if ((rc = check_barrier(e)) != SLIME_OK) break;
+            if (ms < best) {
+                best = ms;
+                best_rows = ro;
+                best_bps = bo;
+            }
+        }
+        if (rc != SLIME_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaMemcpyAsync(e->agent_block, s, abytes, cudaMemcpyDeviceToDevice, e->stream);
+    for (int i = 0; i < 2; i++) {
+        cudaMemcpyAsync(e->trail[i], s + abytes + i * tbytes, tbytes, cudaMemcpyDeviceToDevice, e->stream);
+        cudaMemcpyAsync(e->counts[i], s + abytes + 2 * tbytes + i * tbytes, tbytes, cudaMemcpyDeviceToDevice,
+                        e->stream);
+    }
+    cudaStreamSynchronize(e->stream);
+    cudaFree(snap);
+    e->cur = saved_cur;
+    e->use_graphs = saved_graphs;
+    e->rows = best_rows;
+    e->blocks_per_sm = best_bps;
+    ens_invalidate(e);
+    if (rc == SLIME_OK) rc = build_strip_items(e);
+    if (rc == SLIME_OK) rc = size_grid(e);
+    return rc;
+}
+
+int slime_ensemble_launch_count(const slime_ensemble* e, uint64_t* out) {
+    if (!e || !out) return SLIME_ERR_INVALID_ARGUMENT;
+    *out = e->launches;
+    return SLIME_OK;
+}
+
+} // extern "C"

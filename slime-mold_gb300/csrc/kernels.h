@@ -24,9 +24,15 @@ struct AgentsSoA {
 };
 
 // ---- agents.cu
+// Launch shapes of the agent kernel: agents per thread and threads per block.
+struct AgentShape {
+    int apt, threads;
+};
+int agent_shape_count();
+AgentShape agent_shape(int index);
 // One agent pass (compute.wgsl:57-145): reads trail, adds deposit counts.
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
-                          cudaStream_t s);
+                          cudaStream_t s, int shape = 0);
 // AoS staging (x, y, angle, speed per agent, id order) <-> SoA slots.
 cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const AgentsSoA& a, float4* aos, cudaStream_t s);

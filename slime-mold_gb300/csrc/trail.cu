@@ -14,6 +14,7 @@
 // bit for bit; Gaussian mode is separable (horizontal then vertical, fused
 // multiply-adds over taps -R..R).
 #include "kernels.h"
+#include "trail_stream.cuh"
 
 namespace slime {
 namespace {
@@ -102,138 +103,14 @@ __global__ void __launch_bounds__(kThreads) trail_gauss_kernel(const __grid_cons
     }
 }
 
-// ---------------------------------------------------------------------------
-// Streaming variant for W % 4 == 0 and radius <= 2: one thread owns four
-// adjacent columns (16-byte loads of trail and counts, 16-byte stores of the
-// new trail and of the zeroed counts) and walks a strip of ROWS output rows
-// with a rolling window of 2R+1 input rows in registers.  Horizontal halos
-// come from the neighbouring lanes by warp shuffle; the first lane and the
-// last active lane of a warp load theirs (wrapped) directly.  Every output
-// is produced by the same operations in the same order as the tiled kernels.
-template <int R>
-struct ExtRow {
-    float v[4 + 2 * R]; // columns c0-R .. c0+3+R after fold + decay
-};
-
-template <int R>
-__device__ __forceinline__ void load_ext_row(const DevParams& p, const float* __restrict__ in,
-                                             const uint32_t* __restrict__ cin, int row, int c0, bool active,
-                                             bool left_edge, bool right_edge, const float4& t, const uint4& k,
-                                             ExtRow<R>& e) {
-    float d0 = apply_decay(p, fold_deposits(t.x, k.x, p.dep));
-    float d1 = apply_decay(p, fold_deposits(t.y, k.y, p.dep));
-    float d2 = apply_decay(p, fold_deposits(t.z, k.z, p.dep));
-    float d3 = apply_decay(p, fold_deposits(t.w, k.w, p.dep));
-    float d[4] = {d0, d1, d2, d3};
-#pragma unroll
-    for (int j = 0; j < 4; j++) e.v[R + j] = d[j];
-#pragma unroll
-    for (int j = 0; j < R; j++) {
-        e.v[j] = __shfl_up_sync(0xffffffffu, d[4 - R + j], 1);
-        e.v[R + 4 + j] = __shfl_down_sync(0xffffffffu, d[j], 1);
-    }
-    const size_t base = (size_t)row * p.W;
-    if (active && left_edge) {
-#pragma unroll
-        for (int j = 0; j < R; j++) {
-            int col = wrap_coord(c0 - R + j, p.W);
-            e.v[j] = apply_decay(p, fold_deposits(__ldg(in + base + col), __ldg(cin + base + col), p.dep));
-        }
-    }
-    if (right_edge) {
-#pragma unroll
-        for (int j = 0; j < R; j++) {
-            int col = wrap_coord(c0 + 4 + j, p.W);
-            e.v[R + 4 + j] = apply_decay(p, fold_deposits(__ldg(in + base + col), __ldg(cin + base + col), p.dep));
-        }
-    }
-}
-
 template <int R, bool kGauss, int ROWS>
 __global__ void __launch_bounds__(128) trail_stream_kernel(const __grid_constant__ DevParams p,
                                                            const float* __restrict__ in,
                                                            const uint32_t* __restrict__ cin,
                                                            float* __restrict__ out,
                                                            uint32_t* __restrict__ czero, int warps_x) {
-    const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
-    const int cw = gw % warps_x, rs = gw / warps_x;
-    const int W = p.W, H = p.H;
-    const int y0 = rs * ROWS;
-    if (y0 >= H) return; // warp-uniform
-    const int c0 = cw * 128 + lane * 4;
-    const bool active = c0 < W;
-    const bool left_edge = lane == 0;
-    const bool right_edge = active && (lane == 31 || c0 + 4 >= W);
-    const int cl = active ? c0 : 0; // inactive lanes load a valid line and discard it
-
-    constexpr int NWIN = 2 * R + 1;
-    ExtRow<R> win[NWIN];
-    float hwin[NWIN][4];
-
-    float4 tn;
-    uint4 kn;
-    {
-        const size_t off = (size_t)wrap_coord(y0 - R, H) * W + cl;
-        tn = __ldg(reinterpret_cast<const float4*>(in + off));
-        kn = __ldg(reinterpret_cast<const uint4*>(cin + off));
-    }
-#pragma unroll 2
-    for (int r = 0; r < ROWS + 2 * R; r++) {
-        float4 t = tn;
-        uint4 k = kn;
-        if (r + 1 < ROWS + 2 * R) {
-            const size_t off = (size_t)wrap_coord(y0 - R + r + 1, H) * W + cl;
-            tn = __ldg(reinterpret_cast<const float4*>(in + off));
-            kn = __ldg(reinterpret_cast<const uint4*>(cin + off));
-        }
-        // shift the window and add the new row
-#pragma unroll
-        for (int q = 0; q < NWIN - 1; q++) {
-            win[q] = win[q + 1];
-            if (kGauss) {
-#pragma unroll
-                for (int j = 0; j < 4; j++) hwin[q][j] = hwin[q + 1][j];
-            }
-        }
-        load_ext_row<R>(p, in, cin, wrap_coord(y0 - R + r, H), c0, active, left_edge, right_edge, t, k,
-                        win[NWIN - 1]);
-        if (kGauss) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                float acc = 0.0f;
-#pragma unroll
-                for (int q = 0; q <= 2 * R; q++) acc = slm_fma(p.w[q], win[NWIN - 1].v[j + q], acc);
-                hwin[NWIN - 1][j] = acc;
-            }
-        }
-        if (r < 2 * R) continue;
-        const int y = y0 + r - 2 * R;
-        if (!active || y >= H) continue;
-        float o[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            float center = win[R].v[R + j];
-            float blur;
-            if (kGauss) {
-                float acc = 0.0f;
-#pragma unroll
-                for (int q = 0; q <= 2 * R; q++) acc = slm_fma(p.w[q], hwin[q][j], acc);
-                blur = acc;
-            } else {
-                float sum = 0.0f;
-#pragma unroll
-                for (int dy = 0; dy < 3; dy++)
-#pragma unroll
-                    for (int dx = 0; dx < 3; dx++) sum = slm_add(sum, win[dy].v[j + dx]);
-                blur = slm_div(sum, 9.0f);
-            }
-            o[j] = slm_mix(center, blur, p.rate);
-        }
-        const size_t off = (size_t)y * W + c0;
-        *reinterpret_cast<float4*>(out + off) = make_float4(o[0], o[1], o[2], o[3]);
-        if (czero) *reinterpret_cast<uint4*>(czero + off) = make_uint4(0u, 0u, 0u, 0u);
-    }
+    process_strip<R, kGauss, ROWS>(p, in, cin, out, czero, gw % warps_x, gw / warps_x);
 }
 
 template <int R, bool kGauss, int ROWS>

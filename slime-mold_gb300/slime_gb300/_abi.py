@@ -88,7 +88,8 @@ class SlimeOptions(C.Structure):
         ("reorder_cell_log2", C.c_uint32),
         ("l2_persist", C.c_uint32),
         ("trail_tile", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("agent_shape", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -101,6 +102,8 @@ class SlimeInfo(C.Structure):
         ("kernel_launches", C.c_uint64),
         ("trail_tile", C.c_uint32),
         ("reordered", C.c_uint32),
+        ("agent_shape", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 

@@ -129,7 +129,6 @@ def _hex(s):
 
 TWO_OVER_PI_F = _hex("0x1.45f306p-1")
 PIO2 = [_hex("0x1.921fb6p+0"), _hex("-0x1.777a5cp-25"), _hex("-0x1.ee59dap-50")]
-PH_CH, PH_CL = _hex("0x1.921fb6p-63"), _hex("-0x1.777a5cp-88")
 S = [_hex("-0x1.555556p-3"), _hex("0x1.111112p-7"), _hex("-0x1.a01a02p-13"), _hex("0x1.71de3ap-19")]
 CC = [_hex("-0x1p-1"), _hex("0x1.555556p-5"), _hex("-0x1.6c16c2p-10"), _hex("0x1.a01a02p-16"),
       _hex("-0x1.27e4fcp-22")]
@@ -168,12 +167,20 @@ def reduce_pio2(x):
     c = p0 + (b >> 32)
     ipart = (c >> 30) & 3
     frac64 = (((c & 0x3FFFFFFF) << 34) | (limb1 << 2) | (limb0 >> 30)) & M64
-    fs = frac64 - (1 << 64) if frac64 >> 63 else frac64
     q = (ipart + (frac64 >> 63)) & 3
-    fs2 = fs >> 1
-    hi = round_f32(fs2)
-    lo = round_f32(fs2 - int(Fraction(float(hi))))
-    r = fma(hi, PH_CH, fma(hi, PH_CL, mul(lo, PH_CH)))
+    neg = frac64 >> 63
+    a = ((1 << 64) - frac64) & M64 if neg else frac64
+    r = f32(0.0)
+    if a != 0:
+        lz = 64 - a.bit_length()
+        t = ((a << lz) & M64) >> 34
+        hi = round_f32(t)
+        lo = round_f32(t - int(float(hi)))
+        scale = f32(2.0 ** (-30 - lz))
+        rh, rl = mul(hi, scale), mul(lo, scale)
+        r = fma(rh, PIO2[0], fma(rh, PIO2[1], mul(rl, PIO2[0])))
+        if neg:
+            r = f32(-r)
     if ix >> 31:
         r = -r
         q = (4 - q) & 3

@@ -1,0 +1,87 @@
+"""The batched ensemble (one persistent launch per step over colonies of
+uneven sizes and parameters) against one plain Simulation per colony and the
+CPU oracle, bit for bit."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import agents_uniform, config0_params
+from test_parity_gpu import assert_bitexact
+
+pytestmark = pytest.mark.gpu
+
+
+def colony_setup(seed, blur_mode, radius=1.0):
+    rng = np.random.default_rng(seed)
+    sizes = [(256, 256), (128, 64), (512, 200), (8, 8), (300, 120), (64, 333)]
+    cols = []
+    for j, (W, H) in enumerate(sizes):
+        n = int(W * H * rng.uniform(0.25, 4.0))
+        p = config0_params(W, H, decay_mode=int(rng.integers(0, 2)), blur_mode=blur_mode, blur_radius=radius,
+                           blur_sigma=float(rng.uniform(0.7, 1.5)),
+                           agent_sensor_angle=float(rng.uniform(0.2, 0.8)),
+                           agent_sensor_distance=float(rng.uniform(4, 20)),
+                           agent_turn_speed=float(rng.uniform(0.1, 0.6)), agent_jitter=float(rng.uniform(0, 0.1)),
+                           decay_factor=float(rng.uniform(0.9, 0.995)), diffusion_rate=float(rng.uniform(0.1, 0.9)),
+                           pheromone_deposition_amount=float(rng.uniform(0.5, 2.0)),
+                           agent_speed_min=30.0, agent_speed_max=60.0)
+        if p.decay_mode == 0:
+            p.decay_factor = float(rng.uniform(1, 20))
+        agents = agents_uniform(n, W, H, 30.0, 60.0, seed=seed * 100 + j)
+        trail = rng.random((H, W), dtype=np.float32)
+        cols.append((W, H, n, p, agents, trail))
+    return cols
+
+
+@pytest.mark.parametrize("blur_mode,radius", [(1, 1.0), (0, 1.0), (1, 2.0)])
+def test_ensemble_matches_plain_runs(gpu, blur_mode, radius):
+    import slime_gb300 as sg
+    cols = colony_setup(7, blur_mode, radius)
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        ens.upload_agents(j, agents)
+        ens.upload_trail(j, trail)
+    ens.step(7)
+    ens.sync()
+    assert ens.launch_count() == 7
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        with sg.Simulation(W, H, n, p) as sim:
+            sim.upload_agents(agents)
+            sim.upload_trail(trail)
+            sim.step(7)
+            assert_bitexact(ens.download_agents(j), sim.download_agents(), f"colony {j} agents")
+            assert_bitexact(ens.download_trail(j), sim.download_trail(), f"colony {j} trail")
+        if W * H <= 40000:
+            ca, ct = agents.copy(), trail.copy()
+            oracle.run(p, W, H, ca, ct, 7)
+            assert_bitexact(ens.download_trail(j), ct, f"colony {j} trail vs oracle")
+
+
+def test_ensemble_autotune_and_params_update(gpu):
+    import slime_gb300 as sg
+    cols = colony_setup(11, 1)
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        ens.upload_agents(j, agents)
+        ens.upload_trail(j, trail)
+    ens.autotune(1)
+    q = cols[2][3].copy()
+    q.agent_jitter = 0.5
+    ens.set_params(2, q)
+    ens.step(4)
+    ens.sync()
+    W, H, n, p, agents, trail = cols[2]
+    ca, ct = agents.copy(), trail.copy()
+    oracle.run(q, W, H, ca, ct, 4)
+    assert_bitexact(ens.download_trail(2), ct, "colony 2 after set_params")
+    assert_bitexact(ens.download_agents(2), ca, "colony 2 agents after set_params")
+
+
+def test_ensemble_rejects_mixed_blur_and_bad_widths(gpu):
+    import slime_gb300 as sg
+    p1 = config0_params(64, 64, blur_mode=1)
+    p2 = config0_params(64, 64, blur_mode=0)
+    with pytest.raises(sg.SlimeError):
+        sg.Ensemble([64, 64], [64, 64], [10, 10], [p1, p2])
+    with pytest.raises(sg.SlimeError):
+        sg.Ensemble([66], [64], [10], [config0_params(66, 64)])

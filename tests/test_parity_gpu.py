@@ -117,6 +117,38 @@ def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
         assert_bitexact(sim.download_agents(), ca, "agents")
 
 
+@pytest.mark.parametrize("shape", range(1, 6))
+def test_every_agent_shape_is_bitexact(gpu, shape):
+    W, H = 200, 150
+    for n in (1, 3, 4097, 20001):
+        p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, agent_speed_min=30.0,
+                           agent_speed_max=50.0, agent_jitter=0.3)
+        agents = agents_uniform(n, W, H, 30.0, 50.0, seed=n)
+        trail = np.random.default_rng(n).random((H, W), dtype=np.float32)
+        sim = make_sim(W, H, n, p, agents, trail)
+        sim.set_options(agent_shape=shape)
+        assert sim.info().agent_shape == shape - 1
+        sim.step(3)
+        ca, ct = agents.copy(), trail.copy()
+        oracle.run(p, W, H, ca, ct, 3)
+        assert_bitexact(sim.download_agents(), ca, f"agents shape {shape} n {n}")
+        assert_bitexact(sim.download_trail(), ct, f"trail shape {shape} n {n}")
+
+
+def test_autotune_keeps_state(gpu):
+    W, H, n = 512, 256, 40000
+    p = config0_params(W, H)
+    agents = agents_uniform(n, W, H, 1.0, 2.0, seed=21)
+    trail = np.random.default_rng(21).random((H, W), dtype=np.float32)
+    a = make_sim(W, H, n, p, agents, trail)
+    a.autotune(2)
+    a.step(5)
+    ca, ct = agents.copy(), trail.copy()
+    oracle.run(p, W, H, ca, ct, 5)
+    assert_bitexact(a.download_agents(), ca, "agents after autotune")
+    assert_bitexact(a.download_trail(), ct, "trail after autotune")
+
+
 @pytest.mark.parametrize("W,H", [(1, 1), (2, 3), (3, 2), (5, 3), (4, 4), (17, 1), (1, 19)])
 def test_tiny_toroidal_grids(gpu, W, H):
     n = 64
