@@ -46,6 +46,11 @@ CONFIGS = {
 }
 
 
+def metric_name(cfg_name):
+    W, H, n = CONFIGS[cfg_name][:3]
+    return f"agent-steps/s (plain step, {n:,} agents on {W}x{H})"
+
+
 def make_params(W, H, speed_lo, speed_hi, dist):
     import slime_gb300 as sg
     p = sg.SlimeParams()
@@ -184,9 +189,11 @@ def run_reference(args, cfg_name):
     threads = oracle.num_threads()
     a = agents.copy()
     t = np.zeros((H, W), np.float32)
-    # warm-up steps (bounded), then timed steps bounded to ~90 s of CPU work
-    for _ in range(min(args.warmup, 1)):
+    # warm-up steps (bounded to ~20 s), then timed steps bounded to ~90 s of CPU work
+    warm, t0 = 0, time.perf_counter()
+    while warm < args.warmup and time.perf_counter() - t0 < 20.0:
         oracle.run(params, W, H, a, t, 1, threads=threads)
+        warm += 1
     steps, t0 = 0, time.perf_counter()
     while steps < args.steps:
         oracle.run(params, W, H, a, t, 1, threads=threads)
@@ -196,14 +203,14 @@ def run_reference(args, cfg_name):
     dt = time.perf_counter() - t0
     value = n * steps / dt
     line = {
-        "impl": "reference", "metric": "agent-steps/s", "value": value, "unit": "agent-steps/s",
-        "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000 * dt / steps,
+        "impl": "reference", "metric": metric_name(cfg_name), "value": value, "unit": "agent-steps/s",
+        "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1000 * dt / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": cfg_name, "width": W, "height": H, "n_agents": n},
         "cells_per_s": W * H * steps / dt,
         "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": threads, "kind": "port",
                          "sample": f"{steps} of {args.steps} requested full steps (time-bounded at 90 s) after "
-                                   f"{min(args.warmup, 1)} warm-up step; the reference's wgpu path cannot run here "
+                                   f"{warm} warm-up steps; the reference's wgpu path cannot run here "
                                    "(no Rust toolchain, no graphics stack), so the CPU restatement of its shader "
                                    "is the reference implementation"},
         "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -246,6 +253,7 @@ def main():
     sim.set_options(reorder_every=args.reorder_every, reorder_cell_log2=2, graph_chunk=50)
     sim.autotune(5)
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
+    tuned = sim.info()
 
     def barrier():
         if ws > 1:
@@ -331,7 +339,7 @@ def main():
         if not args.no_cpu_baseline:
             cpu = cpu_baseline(params, W, H, n, agents)
         line = {
-            "metric": f"agent-steps/s (plain step, {n:,} agents on {W}x{H})",
+            "metric": metric_name(args.config),
             "value": value, "unit": "agent-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded)",
@@ -342,6 +350,7 @@ def main():
                              f"trail {4 * W * H / 1e6:.0f} MB kept L2-resident by design",
                        "parallelism": f"replicas x{ws}"},
             "cells_per_s": cells, "pct_roofline_step": pct_roofline,
+            "tuned": {"trail_tile": tuned.trail_tile, "agent_shape": tuned.agent_shape},
             "kernels": {"agents": k_agents, "trail": k_trail, "other_ms_per_step": other_ms / kern_steps},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
             "cpu_baseline": cpu,

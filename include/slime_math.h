@@ -285,6 +285,27 @@ SLM_FN float slm_sin(float x) { float s, c; slm_sincos(x, &s, &c); return s; }
 SLM_FN float slm_cos(float x) { float s, c; slm_sincos(x, &s, &c); return c; }
 
 /* ---------------------------------------------- composite shader pieces */
+/* Sensor directions of compute.wgsl:79-90: cos/sin of angle - a, angle + a
+ * and angle.  The centre direction is slm_sincos(angle); the side directions
+ * are that vector rotated by -a and +a with (sin a, cos a) =
+ * slm_sincos(sensor_angle), a fixed sequence of binary32 products and fused
+ * multiply-adds.  WGSL bounds cos and sin only to an absolute error of 2^-11;
+ * the rotation is within a few 1e-8 of cos/sin of the rounded sum, i.e. it is
+ * one conforming evaluation of cos(angle -/+ a), shared by host and device. */
+SLM_FN void slm_sensor_dirs(float angle, float sa, float ca, float* cl, float* sl, float* cc, float* sc, float* cr,
+                            float* sr) {
+    float s, c;
+    slm_sincos(angle, &s, &c);
+    *cc = c;
+    *sc = s;
+    /* rotate (c, s) by -a: (c ca + s sa, s ca - c sa); by +a: (c ca - s sa, s ca + c sa) */
+    float cca = slm_mul(c, ca), sca = slm_mul(s, ca);
+    *cl = slm_fma(s, sa, cca);
+    *sl = slm_fma(-c, sa, sca);
+    *cr = slm_fma(-s, sa, cca);
+    *sr = slm_fma(c, sa, sca);
+}
+
 /* The shader's per-agent jitter hash (compute.wgsl:117):
  *   fract(sin(f32(agent_index) * 12.9898 + x * 78.233 + y * 37.719) * 43758.5453)
  * evaluated left to right, unfused. */

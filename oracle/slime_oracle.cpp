@@ -74,14 +74,13 @@ inline int64_t agent_update(const SlimeParams* p, int32_t W, int32_t H, int32_t 
 
     speed = slm_clamp(speed, p->agent_speed_min, p->agent_speed_max); /* :72 */
 
-    float sensor_angle_left = slm_sub(angle, p->agent_sensor_angle); /* :75 */
-    float sensor_angle_right = slm_add(angle, p->agent_sensor_angle); /* :76 */
-    float sensor_angle_center = angle;                                /* :77 */
+    /* :75-77 sensor angles angle - a, angle + a, angle; their cos/sin as the
+     * centre direction and its rotations by -a and +a (slm_sensor_dirs) */
     float dist = p->agent_sensor_distance;
+    float sa, ca;
+    slm_sincos(p->agent_sensor_angle, &sa, &ca);
     float sl, cl, sr, cr, sc, cc;
-    slm_sincos(sensor_angle_left, &sl, &cl);
-    slm_sincos(sensor_angle_right, &sr, &cr);
-    slm_sincos(sensor_angle_center, &sc, &cc);
+    slm_sensor_dirs(angle, sa, ca, &cl, &sl, &cc, &sc, &cr, &sr);
     float lpx = slm_add(x, slm_mul(dist, cl)); /* :79-82 */
     float lpy = slm_add(y, slm_mul(dist, sl));
     float rpx = slm_add(x, slm_mul(dist, cr)); /* :83-86 */

@@ -32,9 +32,7 @@ __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y
     speed = slm_clamp(speed, p.speed_min, p.speed_max);
 
     float sl, cl, sr, cr, sc, cc;
-    slm_sincos(slm_sub(angle, p.sensor_angle), &sl, &cl);
-    slm_sincos(slm_add(angle, p.sensor_angle), &sr, &cr);
-    slm_sincos(angle, &sc, &cc);
+    slm_sensor_dirs(angle, p.sensor_sin, p.sensor_cos, &cl, &sl, &cc, &sc, &cr, &sr);
     float left = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)),
                               slm_add(y, slm_mul(p.sensor_dist, sl)));
     float right = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)),

@@ -64,6 +64,7 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
     d.speed_max = p.agent_speed_max;
     d.turn = p.agent_turn_speed;
     d.sensor_angle = p.agent_sensor_angle;
+    slm_sincos(p.agent_sensor_angle, &d.sensor_sin, &d.sensor_cos);
     d.sensor_dist = p.agent_sensor_distance;
     d.jitter = p.agent_jitter;
     d.time_step = p.time_step;

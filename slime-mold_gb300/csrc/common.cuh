@@ -22,6 +22,7 @@ struct DevParams {
     float speed_min, speed_max;
     float turn;
     float sensor_angle, sensor_dist;
+    float sensor_sin, sensor_cos; // slm_sincos(sensor_angle)
     float jitter;
     float time_step;
     float dep;

@@ -84,3 +84,30 @@ def test_backward_without_record_is_an_error(gpu):
         with pytest.raises(sg.SlimeError) as e:
             sim.backward(np.zeros((16, 16), np.float32))
         assert e.value.status == -4
+
+
+def test_autograd_function_role(gpu):
+    """TrailChain wires the C ABI backward into torch.autograd."""
+    import torch
+    import slime_gb300 as sg
+    from slime_gb300.autograd import trail_chain
+    W, H, n, steps = 64, 48, 1200, 20
+    p = config0_params(W, H, pheromone_deposition_amount=0.05, agent_speed_min=30.0, agent_speed_max=50.0)
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=8)
+    rng = np.random.default_rng(8)
+    t0 = torch.tensor((0.2 + 0.3 * rng.random((H, W))).astype(np.float32), requires_grad=True)
+    target = torch.tensor(rng.random((H, W)).astype(np.float32))
+    decay = torch.tensor(0.97, dtype=torch.float64, requires_grad=True)
+    rate = torch.tensor(0.5, dtype=torch.float64, requires_grad=True)
+    dep = torch.tensor(0.05, dtype=torch.float64, requires_grad=True)
+    with sg.Simulation(W, H, n, p) as sim:
+        out = trail_chain(t0, decay, rate, dep, sim, steps, 6, agents)
+        loss = 0.5 * ((out - target) ** 2).sum()
+        loss.backward()
+    counts = oracle.run(p, W, H, agents.copy(), t0.detach().numpy().copy(), steps, record_counts=True)
+    theta = [float(np.float32(0.97)), float(np.float32(0.5)), float(np.float32(0.05))]
+    _, ref, d0_ref = oracle.chain_adjoint_f64(p, W, H, *theta, t0.detach().numpy(), counts,
+                                              target=target.numpy().astype(np.float64))
+    for got, want in zip((decay.grad, rate.grad, dep.grad), ref):
+        assert abs(float(got) - want) <= 1e-5 * max(1.0, abs(want))
+    assert np.abs(t0.grad.numpy() - d0_ref).max() <= 1e-5 * max(1.0, np.abs(d0_ref).max())
