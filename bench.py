@@ -226,7 +226,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="plain-4096", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--reorder-every", type=int, default=50)
+    ap.add_argument("--reorder-every", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

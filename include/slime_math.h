@@ -144,16 +144,17 @@ SLM_FN float slm_mix(float a, float b, float t) {
 SLM_FN float slm_fmod(float x, float y) {
     /* For y > 0 and |x| < 2y the remainder is one of x, x - y, x + y, each
      * exact (Sterbenz), which is what every exact fmodf returns; the
-     * remainder of -y is -0.  Everything else goes to fmodf. */
-    if (y > 0.0f) {
-        if (slm_abs(x) < y) return x;
-        if (x >= y && x < slm_add(y, y)) return slm_sub(x, y);
-        if (x <= -y && x > -slm_add(y, y)) {
-            float r = slm_add(x, y);
-            return r == 0.0f ? -0.0f : r;
-        }
-    }
-    return fmodf(x, y);
+     * remainder of -y is -0.  Written as selects; everything else goes to
+     * fmodf. */
+    float y2 = slm_add(y, y);
+    int in0 = slm_abs(x) < y;
+    int in1 = (x >= y) && (x < y2);
+    int in2 = (x <= -y) && (x > -y2);
+    if (!(y > 0.0f) || !(in0 || in1 || in2)) return fmodf(x, y);
+    float r1 = slm_sub(x, y);
+    float r2 = slm_add(x, y);
+    r2 = (r2 == 0.0f) ? -0.0f : r2;
+    return in0 ? x : (in1 ? r1 : r2);
 }
 
 /* WGSL i32(f32): truncate toward zero, saturate to the i32 range, NaN -> 0.

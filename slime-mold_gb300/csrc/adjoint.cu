@@ -249,7 +249,9 @@ int slime_backward(slime_ctx* ctx, const float* dl_dtrail_final, SlimeGrads* gra
     const uint32_t K = a.ckpt_every;
     cudaError_t e;
     if (!a.seg_trail) {
-        if ((e = cudaMalloc(&a.seg_trail, (size_t)K * cells * sizeof(float))) != cudaSuccess ||
+        // W + 2 zero floats past the last trail: the sampler's discarded taps
+        if ((e = cudaMalloc(&a.seg_trail, ((size_t)K * cells + ctx->W + 2) * sizeof(float))) != cudaSuccess ||
+            (e = cudaMemset(a.seg_trail, 0, ((size_t)K * cells + ctx->W + 2) * sizeof(float))) != cudaSuccess ||
             (e = cudaMalloc(&a.seg_counts, (size_t)K * cells * sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaMalloc(&a.g[0], cells * sizeof(float))) != cudaSuccess ||
             (e = cudaMalloc(&a.g[1], cells * sizeof(float))) != cudaSuccess ||

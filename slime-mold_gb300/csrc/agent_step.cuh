@@ -7,23 +7,26 @@
 namespace slime {
 
 // sample_trail_map, compute.wgsl:7-29 (x1 >= W written as x0 >= W - 1).
+// The trail buffers carry W + 2 zero floats past their last cell, so the four
+// taps at index 0 are always in bounds: an out-of-grid sample loads from cell
+// 0 and is discarded, which keeps the sampler free of branches.
 __device__ __forceinline__ float sample_trail(const float* __restrict__ trail, int W, int H, float px, float py) {
     float fx = floorf(px), fy = floorf(py);
     int x0 = slm_f2i(fx);
     int y0 = slm_f2i(fy);
     // x0 < 0 || x0 + 1 >= W  (and the same for y) as one unsigned compare each
-    if ((unsigned)x0 >= (unsigned)(W - 1) || (unsigned)y0 >= (unsigned)(H - 1)) return 0.0f;
+    bool ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
     // in range, f32(x0) == floor(px) exactly
     float dx = slm_sub(px, fx);
     float dy = slm_sub(py, fy);
-    const float* r0 = trail + (y0 * W + x0);
+    const float* r0 = trail + (ok ? y0 * W + x0 : 0);
     float v00 = __ldg(r0);
     float v10 = __ldg(r0 + 1);
     float v01 = __ldg(r0 + W);
     float v11 = __ldg(r0 + W + 1);
     float v0 = slm_mix(v00, v10, dx);
     float v1 = slm_mix(v01, v11, dx);
-    return slm_mix(v0, v1, dy);
+    return ok ? slm_mix(v0, v1, dy) : 0.0f;
 }
 
 // One agent, compute.wgsl:65-144.  Returns the deposit cell or -1.
@@ -40,15 +43,13 @@ __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y
     float center = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)),
                                 slm_add(y, slm_mul(p.sensor_dist, sc)));
 
-    if (center > left && center > right) {
-        // straight
-    } else if (left > right) {
-        float diff = slm_sub(slm_sub(angle, SLM_WGSL_TAU), angle);
-        angle = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
-    } else if (right > left) {
-        float diff = slm_sub(slm_add(angle, SLM_WGSL_TAU), angle);
-        angle = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
-    }
+    // compute.wgsl:98-112 as selects: straight, turn left, turn right, or keep
+    float diff_l = slm_sub(slm_sub(angle, SLM_WGSL_TAU), angle);
+    float diff_r = slm_sub(slm_add(angle, SLM_WGSL_TAU), angle);
+    float turn_l = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff_l)), slm_sign(diff_l)));
+    float turn_r = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff_r)), slm_sign(diff_r)));
+    bool straight = center > left && center > right;
+    angle = straight ? angle : (left > right ? turn_l : (right > left ? turn_r : angle));
 
     float rv = slm_jitter_hash(index, x, y);
     angle = slm_add(angle, slm_mul(slm_sub(slm_mul(rv, 2.0f), 1.0f), p.jitter));

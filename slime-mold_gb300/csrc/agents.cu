@@ -86,9 +86,15 @@ __global__ void __launch_bounds__(BS) agents_kernel(const __grid_constant__ DevP
         for (int j = 0; j < APT; j++) id[j] = (uint32_t)(base + j);
     }
     int cell[APT];
+    if (base + APT <= n) {
+        // full group: no per-agent branch, so the agents' work can interleave
 #pragma unroll
-    for (int j = 0; j < APT; j++)
-        cell[j] = (base + j < n) ? agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail) : -1;
+        for (int j = 0; j < APT; j++) cell[j] = agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail);
+    } else {
+#pragma unroll
+        for (int j = 0; j < APT; j++)
+            cell[j] = (base + j < n) ? agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail) : -1;
+    }
 #pragma unroll
     for (int j = 0; j < APT; j++)
         if (cell[j] >= 0) atomicAdd(counts + cell[j], 1u);

@@ -160,9 +160,10 @@ int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
     free_trail(ctx);
     size_t cells = (size_t)W * H;
     for (int i = 0; i < 2; i++) {
-        CK(cudaMalloc(&ctx->trail[i], cells * sizeof(float)), "allocating trail");
+        // W + 2 zero floats past the last cell: the sampler's discarded taps
+        CK(cudaMalloc(&ctx->trail[i], (cells + W + 2) * sizeof(float)), "allocating trail");
         CK(cudaMalloc(&ctx->counts[i], cells * sizeof(uint32_t)), "allocating deposit counts");
-        CK(cudaMemsetAsync(ctx->trail[i], 0, cells * sizeof(float), ctx->stream), "clearing trail");
+        CK(cudaMemsetAsync(ctx->trail[i], 0, (cells + W + 2) * sizeof(float), ctx->stream), "clearing trail");
         CK(cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream), "clearing counts");
     }
     ctx->cur = 0;

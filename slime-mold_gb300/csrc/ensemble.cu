@@ -117,11 +117,18 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
         float4 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
         const float* trail = trail_in + c.trail_off;
         uint32_t* counts = counts_in + c.trail_off;
-        int c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)base, trail);
-        int c1 = -1, c2 = -1, c3 = -1;
-        if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)(base + 1), trail);
-        if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)(base + 2), trail);
-        if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)(base + 3), trail);
+        int c0, c1 = -1, c2 = -1, c3 = -1;
+        if (base + 4 <= c.n) { // full group: no per-agent branch
+            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)base, trail);
+            c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)(base + 1), trail);
+            c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)(base + 2), trail);
+            c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)(base + 3), trail);
+        } else {
+            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)base, trail);
+            if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)(base + 1), trail);
+            if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)(base + 2), trail);
+            if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)(base + 3), trail);
+        }
         if (c0 >= 0) atomicAdd(counts + c0, 1u);
         if (c1 >= 0) atomicAdd(counts + c1, 1u);
         if (c2 >= 0) atomicAdd(counts + c2, 1u);
@@ -413,7 +420,11 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         return nullptr;
     }
     e->total_slots = slots ? slots : kAgentPad;
-    e->total_cells = cells;
+    // every colony's sampler may read W + 1 floats past its own cell 0; the
+    // last colony's are covered by this zero tail
+    uint32_t maxw = 0;
+    for (const Colony& c : e->colonies) maxw = c.W > maxw ? c.W : maxw;
+    e->total_cells = cells + maxw + 4;
     // agent work items: 1,024 agents of one colony each
     std::vector<uint2> ai;
     for (uint32_t j = 0; j < k; j++) {
