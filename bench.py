@@ -227,6 +227,7 @@ def main():
     ap.add_argument("--config", default="plain-4096", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reorder-every", type=int, default=200)
+    ap.add_argument("--no-l2-persist", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -250,7 +251,8 @@ def main():
     agents = make_agents(n, W, H, lo, hi, seed=rank)
     sim = sg.Simulation(W, H, n, params)
     sim.upload_agents(agents)
-    sim.set_options(reorder_every=args.reorder_every, reorder_cell_log2=2, graph_chunk=50)
+    sim.set_options(reorder_every=args.reorder_every, reorder_cell_log2=2, graph_chunk=50,
+                    l2_persist=0 if args.no_l2_persist else 1)
     sim.autotune(5)
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
     tuned = sim.info()
@@ -346,6 +348,7 @@ def main():
             "config": {"workload": args.config, "width": W, "height": H, "n_agents": n,
                        "decay": "multiply 0.97", "blur": "gauss r=1 sigma=1 rate 0.5",
                        "reorder_every": args.reorder_every, "graph_chunk": 50,
+                       "l2_persist": not args.no_l2_persist,
                        "l2": f"agent state {16 * n / 1e6:.0f} MB streamed per step (> 129 MB L2); "
                              f"trail {4 * W * H / 1e6:.0f} MB kept L2-resident by design",
                        "parallelism": f"replicas x{ws}"},

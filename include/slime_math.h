@@ -114,18 +114,28 @@ SLM_FN uint32_t slm_f2u_bits(float x) { uint32_t u; memcpy(&u, &x, 4); return u;
 SLM_FN float slm_u2f_bits(uint32_t u) { float x; memcpy(&x, &u, 4); return x; }
 SLM_FN int slm_isnan(float x) { return x != x; }
 
-/* WGSL min/max: the non-NaN operand if exactly one is NaN; for equal operands
- * (including +0/-0) the first one.  Written with comparisons so that the host
- * and the device pick the same zero. */
+/* WGSL min/max, pinned as IEEE 754-2019 minimumNumber/maximumNumber: a NaN
+ * operand is ignored, and -0 orders below +0.  The device's fminf/fmaxf
+ * (min.f32/max.f32) implement exactly this; the host spells it out. */
 SLM_FN float slm_min(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return fminf(a, b);
+#else
     if (slm_isnan(a)) return b;
     if (slm_isnan(b)) return a;
+    if (a == b) return (slm_f2u_bits(a) >> 31) ? a : b; /* -0 before +0 */
     return (b < a) ? b : a;
+#endif
 }
 SLM_FN float slm_max(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return fmaxf(a, b);
+#else
     if (slm_isnan(a)) return b;
     if (slm_isnan(b)) return a;
+    if (a == b) return (slm_f2u_bits(a) >> 31) ? b : a; /* +0 after -0 */
     return (b > a) ? b : a;
+#endif
 }
 /* WGSL clamp(e, low, high) = min(max(e, low), high). */
 SLM_FN float slm_clamp(float e, float lo, float hi) { return slm_min(slm_max(e, lo), hi); }
@@ -155,6 +165,18 @@ SLM_FN float slm_fmod(float x, float y) {
     float r2 = slm_add(x, y);
     r2 = (r2 == 0.0f) ? -0.0f : r2;
     return in0 ? x : (in1 ? r1 : r2);
+}
+
+/* The shader's toroidal wrap, `v = v % n; if (v < 0.0) { v = v + n; }`
+ * (compute.wgsl:121-122, :130-133), for n > 0.  Values within one period of
+ * [0, n) take the exact short paths; -n and -0 give -0 as the remainder does. */
+SLM_FN float slm_wrap(float v, float n) {
+    if (v >= 0.0f && v < n) return v;
+    if (v >= n && v < slm_add(n, n)) return slm_sub(v, n);
+    if (v < 0.0f && v > -n) return slm_add(v, n);
+    float r = slm_fmod(v, n);
+    if (r < 0.0f) r = slm_add(r, n);
+    return r;
 }
 
 /* WGSL i32(f32): truncate toward zero, saturate to the i32 range, NaN -> 0.

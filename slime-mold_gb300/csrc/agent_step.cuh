@@ -43,28 +43,25 @@ __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y
     float center = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)),
                                 slm_add(y, slm_mul(p.sensor_dist, sc)));
 
-    // compute.wgsl:98-112 as selects: straight, turn left, turn right, or keep
-    float diff_l = slm_sub(slm_sub(angle, SLM_WGSL_TAU), angle);
-    float diff_r = slm_sub(slm_add(angle, SLM_WGSL_TAU), angle);
-    float turn_l = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff_l)), slm_sign(diff_l)));
-    float turn_r = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff_r)), slm_sign(diff_r)));
-    bool straight = center > left && center > right;
-    angle = straight ? angle : (left > right ? turn_l : (right > left ? turn_r : angle));
+    // compute.wgsl:98-112: keep straight, or turn toward target = angle -/+ TAU
+    bool turn_left = !(center > left && center > right) && (left > right);
+    bool turn_right = !(center > left && center > right) && !(left > right) && (right > left);
+    float target = turn_left ? slm_sub(angle, SLM_WGSL_TAU) : slm_add(angle, SLM_WGSL_TAU);
+    float diff = slm_sub(target, angle);
+    float turned = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
+    angle = (turn_left || turn_right) ? turned : angle;
 
     float rv = slm_jitter_hash(index, x, y);
     angle = slm_add(angle, slm_mul(slm_sub(slm_mul(rv, 2.0f), 1.0f), p.jitter));
-    angle = slm_fmod(angle, SLM_WGSL_TWO_PI);
-    if (angle < 0.0f) angle = slm_add(angle, SLM_WGSL_TWO_PI);
+    angle = slm_wrap(angle, SLM_WGSL_TWO_PI);
 
     float move = slm_mul(speed, p.time_step);
     float sm, cm;
     slm_sincos(angle, &sm, &cm);
     x = slm_add(x, slm_mul(move, cm));
     y = slm_add(y, slm_mul(move, sm));
-    x = slm_fmod(x, p.Wf);
-    if (x < 0.0f) x = slm_add(x, p.Wf);
-    y = slm_fmod(y, p.Hf);
-    if (y < 0.0f) y = slm_add(y, p.Hf);
+    x = slm_wrap(x, p.Wf);
+    y = slm_wrap(y, p.Hf);
 
     int dx = slm_f2i(x);
     int dy = slm_f2i(y);

@@ -162,16 +162,14 @@ __global__ void scale_positions_kernel(float* __restrict__ x, float* __restrict_
 
 template <int APT, int BS>
 cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, const cudaAccessPolicyWindow* win) {
     uint32_t n_groups = (uint32_t)((a.n + APT - 1) / APT);
-    unsigned blocks = blocks_for(n_groups, BS);
+    dim3 grid(blocks_for(n_groups, BS));
     if (a.ids)
-        agents_kernel<APT, BS, true><<<blocks, BS, 0, s>>>(p, a.x, a.y, a.th, a.v, a.ids, trail, counts, n_groups,
-                                                           a.n);
-    else
-        agents_kernel<APT, BS, false><<<blocks, BS, 0, s>>>(p, a.x, a.y, a.th, a.v, nullptr, trail, counts,
-                                                            n_groups, a.n);
-    return cudaGetLastError();
+        return launch_k(agents_kernel<APT, BS, true>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+                        (const uint32_t*)a.ids, trail, counts, n_groups, a.n);
+    return launch_k(agents_kernel<APT, BS, false>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+                    (const uint32_t*)nullptr, trail, counts, n_groups, a.n);
 }
 
 } // namespace
@@ -183,14 +181,14 @@ int agent_shape_count() { return (int)(sizeof(kAgentShapes) / sizeof(kAgentShape
 AgentShape agent_shape(int i) { return kAgentShapes[(i >= 0 && i < agent_shape_count()) ? i : 0]; }
 
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
-                          cudaStream_t s, int shape) {
+                          cudaStream_t s, int shape, const cudaAccessPolicyWindow* win) {
     if (a.n == 0) return cudaSuccess;
     switch (shape) {
-    case 1: return launch_agents_variant<2, 256>(p, a, trail, counts, s);
-    case 2: return launch_agents_variant<1, 256>(p, a, trail, counts, s);
-    case 3: return launch_agents_variant<4, 128>(p, a, trail, counts, s);
-    case 4: return launch_agents_variant<1, 128>(p, a, trail, counts, s);
-    default: return launch_agents_variant<4, 256>(p, a, trail, counts, s);
+    case 1: return launch_agents_variant<2, 256>(p, a, trail, counts, s, win);
+    case 2: return launch_agents_variant<1, 256>(p, a, trail, counts, s, win);
+    case 3: return launch_agents_variant<4, 128>(p, a, trail, counts, s, win);
+    case 4: return launch_agents_variant<1, 128>(p, a, trail, counts, s, win);
+    default: return launch_agents_variant<4, 256>(p, a, trail, counts, s, win);
     }
 }
 

@@ -209,14 +209,56 @@ void invalidate_graphs(slime_ctx* ctx) {
     ctx->graphs.clear();
 }
 
-// Enqueue one step on the context's stream (also used under capture).
+// Size the persisting-L2 carve-out for the trail (the context's limit, gone
+// with the context) and remember the largest window the device accepts.
+void setup_l2(slime_ctx* ctx) {
+    ctx->l2_persist_bytes = 0;
+    ctx->l2_max_window = 0;
+    if (!ctx->opt.l2_persist) return;
+    int max_persist = 0, max_window = 0;
+    if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device) != cudaSuccess ||
+        max_persist <= 0 || max_window <= 0) {
+        cudaGetLastError();
+        return;
+    }
+    size_t want = (size_t)ctx->W * ctx->H * sizeof(float);
+    size_t grant = want < (size_t)max_persist ? want : (size_t)max_persist;
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, grant) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    ctx->l2_persist_bytes = grant;
+    ctx->l2_max_window = (size_t)max_window;
+}
+
+// The access window for a launch that reads (or writes) trail buffer `t`.
+bool trail_window(const slime_ctx* ctx, const float* t, cudaAccessPolicyWindow* w) {
+    if (!ctx->l2_persist_bytes) return false;
+    size_t bytes = (size_t)ctx->W * ctx->H * sizeof(float);
+    if (bytes > ctx->l2_max_window) bytes = ctx->l2_max_window;
+    w->base_ptr = (void*)t;
+    w->num_bytes = bytes;
+    float ratio = (float)ctx->l2_persist_bytes / (float)bytes;
+    w->hitRatio = ratio < 1.0f ? ratio : 1.0f;
+    w->hitProp = cudaAccessPropertyPersisting;
+    w->missProp = cudaAccessPropertyStreaming;
+    return true;
+}
+
+// Enqueue one step on the context's stream (also used under capture).  The
+// agent pass keeps the trail it senses resident; the trail pass marks the
+// trail it writes, which the next agent pass senses.
 cudaError_t enqueue_step(slime_ctx* ctx) {
     const int cur = ctx->cur;
-    cudaError_t e =
-        launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, ctx->agent_shape);
+    cudaAccessPolicyWindow wa, wt;
+    bool ha = trail_window(ctx, ctx->trail[cur], &wa);
+    bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt);
+    cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream,
+                                  ctx->agent_shape, ha ? &wa : nullptr);
     if (e != cudaSuccess) return e;
     e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                     ctx->counts[1 - cur], ctx->stream);
+                     ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr);
     if (e != cudaSuccess) return e;
     ctx->cur = 1 - cur;
     return cudaSuccess;
@@ -358,6 +400,7 @@ slime_ctx* slime_create(uint32_t width, uint32_t height, uint64_t n_agents, int*
         const char* why = nullptr;
         if (!make_dev_params(ctx->params, width, height, &ctx->dev, &why)) rc = SLIME_ERR_INVALID_ARGUMENT;
         else if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = SLIME_ERR_CUDA;
+        else setup_l2(ctx);
     }
     if (rc != SLIME_OK) {
         slime_destroy(ctx);
@@ -418,8 +461,13 @@ int slime_set_options(slime_ctx* ctx, const SlimeOptions* o) {
         return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "agent_shape out of range (0..%d)",
                          agent_shape_count());
     if (o->reserved != 0) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "options.reserved must be 0");
+    const bool l2_changed = (o->l2_persist != 0) != (ctx->opt.l2_persist != 0);
     ctx->opt = *o;
     if (ctx->opt.graph_chunk == 0) ctx->opt.graph_chunk = 50;
+    if (l2_changed) {
+        setup_l2(ctx);
+        invalidate_graphs(ctx);
+    }
     int tile = o->trail_tile ? (int)o->trail_tile - 1 : (ctx->tuned_tile >= 0 ? ctx->tuned_tile : trail_tile_default());
     int shape = o->agent_shape ? (int)o->agent_shape - 1 : (ctx->tuned_shape >= 0 ? ctx->tuned_shape : 0);
     if (tile != ctx->tile || shape != ctx->agent_shape) {
@@ -557,6 +605,7 @@ int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height) {
     ctx->params = np;
     ctx->dev = d;
     ctx->tuned_tile = -1;
+    setup_l2(ctx);
     CK(cudaStreamSynchronize(ctx->stream), "resizing");
     return SLIME_OK;
 }
@@ -634,12 +683,15 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
             rc = do_reorder(ctx);
         cudaEventRecord(ev[1], ctx->stream);
         const int cur = ctx->cur;
-        cudaError_t e =
-            launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, ctx->agent_shape);
+        cudaAccessPolicyWindow wa, wt;
+        bool ha = trail_window(ctx, ctx->trail[cur], &wa);
+        bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt);
+        cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream,
+                                      ctx->agent_shape, ha ? &wa : nullptr);
         cudaEventRecord(ev[2], ctx->stream);
         if (e == cudaSuccess)
             e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                             ctx->counts[1 - cur], ctx->stream);
+                             ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr);
         cudaEventRecord(ev[3], ctx->stream);
         if (e != cudaSuccess) {
             rc = cuda_error(ctx->err, e, "profiling a step");

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/slime.h"
 #include "../../include/slime_math.h"
 
@@ -35,6 +37,26 @@ struct DevParams {
     float w[2 * kMaxR + 1];
     float w2sum_m1; // (sum of w)^2 - 1 in binary64, rounded: B(u) - u = sum w w (u_n - u_c) + this * u_c
 };
+
+// Launch `k` with an optional persisting-L2 access window attached to this
+// launch (captured into graphs as a kernel-node attribute).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                     const cudaAccessPolicyWindow* win, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    if (win) {
+        attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[0].val.accessPolicyWindow = *win;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // Translate SlimeParams into DevParams; returns false (with a message) on
 // values the kernels cannot honour.

@@ -33,6 +33,10 @@ struct slime_ctx {
     int agent_shape = 0; // index into the agent-kernel shape table
     int tuned_shape = -1;
 
+    // Persisting-L2 window over the trail being sensed (0 = off).
+    size_t l2_persist_bytes = 0; // carve-out granted to this context
+    size_t l2_max_window = 0;    // cudaDevAttrMaxAccessPolicyWindowSize
+
     std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs; // (steps, start parity) -> graph
 
     uint64_t steps_done = 0;
@@ -76,5 +80,7 @@ cudaError_t enqueue_step(slime_ctx* ctx);
 uint64_t kernels_per_step(const slime_ctx* ctx);
 int run_steps(slime_ctx* ctx, uint32_t n);
 void free_adjoint(slime_ctx* ctx);
+void setup_l2(slime_ctx* ctx);
+bool trail_window(const slime_ctx* ctx, const float* t, cudaAccessPolicyWindow* w);
 
 } // namespace slime

@@ -32,7 +32,7 @@ int agent_shape_count();
 AgentShape agent_shape(int index);
 // One agent pass (compute.wgsl:57-145): reads trail, adds deposit counts.
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
-                          cudaStream_t s, int shape = 0);
+                          cudaStream_t s, int shape = 0, const cudaAccessPolicyWindow* win = nullptr);
 // AoS staging (x, y, angle, speed per agent, id order) <-> SoA slots.
 cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const AgentsSoA& a, float4* aos, cudaStream_t s);
@@ -55,7 +55,7 @@ bool trail_tile_supported(const DevParams& p, int tile);
 // Fused trail pass: out = Diffuse(Decay(Fold(in, counts_in))); zeroes
 // counts_zero (the other step's count buffer, may be null) over the same cells.
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
-                         uint32_t* counts_zero, cudaStream_t s);
+                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr);
 
 // ---- adjoint.cu
 // One backward step of the frozen-trajectory chain: from g_in = dL/dT_{s+1}

@@ -115,20 +115,20 @@ __global__ void __launch_bounds__(128) trail_stream_kernel(const __grid_constant
 
 template <int R, bool kGauss, int ROWS>
 cudaError_t launch_stream(const DevParams& p, const float* in, const uint32_t* cin, float* out, uint32_t* cz,
-                          cudaStream_t s) {
+                          cudaStream_t s, const cudaAccessPolicyWindow* win) {
     int warps_x = (p.W + 127) / 128;
     long long warps = (long long)warps_x * ((p.H + ROWS - 1) / ROWS);
     unsigned blocks = (unsigned)((warps + 3) / 4);
-    trail_stream_kernel<R, kGauss, ROWS><<<blocks, 128, 0, s>>>(p, in, cin, out, cz, warps_x);
-    return cudaGetLastError();
+    return launch_k(trail_stream_kernel<R, kGauss, ROWS>, dim3(blocks), dim3(128), 0, s, win, p, in, cin, out, cz,
+                    warps_x);
 }
 
 template <int ROWS>
 cudaError_t launch_stream_rows(const DevParams& p, const float* in, const uint32_t* cin, float* out, uint32_t* cz,
-                               cudaStream_t s) {
-    if (p.blur_mode != SLIME_BLUR_GAUSS) return launch_stream<1, false, ROWS>(p, in, cin, out, cz, s);
-    if (p.R == 1) return launch_stream<1, true, ROWS>(p, in, cin, out, cz, s);
-    return launch_stream<2, true, ROWS>(p, in, cin, out, cz, s);
+                               cudaStream_t s, const cudaAccessPolicyWindow* win) {
+    if (p.blur_mode != SLIME_BLUR_GAUSS) return launch_stream<1, false, ROWS>(p, in, cin, out, cz, s, win);
+    if (p.R == 1) return launch_stream<1, true, ROWS>(p, in, cin, out, cz, s, win);
+    return launch_stream<2, true, ROWS>(p, in, cin, out, cz, s, win);
 }
 
 const TrailTile kTiles[] = {{32, 8}, {64, 8}, {32, 16}, {64, 16}, {128, 8}, {128, 16}, {256, 8}};
@@ -136,7 +136,7 @@ constexpr int kNumTiles = (int)(sizeof(kTiles) / sizeof(kTiles[0]));
 
 template <int TW, int TH>
 cudaError_t launch_tile(const DevParams& p, const float* in, const uint32_t* cin, float* out, uint32_t* cz,
-                        cudaStream_t s) {
+                        cudaStream_t s, const cudaAccessPolicyWindow* win) {
     dim3 grid((p.W + TW - 1) / TW, (p.H + TH - 1) / TH);
     if (p.blur_mode == SLIME_BLUR_GAUSS && p.R > 0) {
         size_t smem;
@@ -148,7 +148,11 @@ cudaError_t launch_tile(const DevParams& p, const float* in, const uint32_t* cin
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);    \
             if (e != cudaSuccess) return e;                                                                  \
         }                                                                                                    \
-        trail_gauss_kernel<TW, TH, RR><<<grid, kThreads, smem, s>>>(p, in, cin, out, cz);                    \
+        {                                                                                                    \
+            cudaError_t le = launch_k(trail_gauss_kernel<TW, TH, RR>, grid, dim3(kThreads), smem, s, win, p, in,  \
+                                      cin, out, cz);                                                         \
+            if (le != cudaSuccess) return le;                                                                \
+        }                                                                                                    \
         break;
         switch (p.R) {
             SLIME_GAUSS_CASE(1)
@@ -166,10 +170,10 @@ cudaError_t launch_tile(const DevParams& p, const float* in, const uint32_t* cin
     } else if (p.blur_mode == SLIME_BLUR_GAUSS) {
         // Radius 0: the blur is the identity; weights are {1}.
         size_t smem = sizeof(float) * (TH * TW + TH * TW);
-        trail_gauss_kernel<TW, TH, 0><<<grid, kThreads, smem, s>>>(p, in, cin, out, cz);
+        return launch_k(trail_gauss_kernel<TW, TH, 0>, grid, dim3(kThreads), smem, s, win, p, in, cin, out, cz);
     } else {
         size_t smem = sizeof(float) * (TH + 2) * (TW + 2);
-        trail_box3_kernel<TW, TH><<<grid, kThreads, smem, s>>>(p, in, cin, out, cz);
+        return launch_k(trail_box3_kernel<TW, TH>, grid, dim3(kThreads), smem, s, win, p, in, cin, out, cz);
     }
     return cudaGetLastError();
 }
@@ -195,19 +199,19 @@ bool trail_tile_supported(const DevParams& p, int tile) {
 }
 
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
-                         uint32_t* counts_zero, cudaStream_t s) {
+                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win) {
     if (!trail_tile_supported(p, tile)) tile = trail_tile_default();
     switch (tile) {
-    case 0: return launch_tile<32, 8>(p, in, counts_in, out, counts_zero, s);
-    case 1: return launch_tile<64, 8>(p, in, counts_in, out, counts_zero, s);
-    case 2: return launch_tile<32, 16>(p, in, counts_in, out, counts_zero, s);
-    case 3: return launch_tile<64, 16>(p, in, counts_in, out, counts_zero, s);
-    case 4: return launch_tile<128, 8>(p, in, counts_in, out, counts_zero, s);
-    case 5: return launch_tile<128, 16>(p, in, counts_in, out, counts_zero, s);
-    case 6: return launch_tile<256, 8>(p, in, counts_in, out, counts_zero, s);
-    case 7: return launch_stream_rows<8>(p, in, counts_in, out, counts_zero, s);
-    case 8: return launch_stream_rows<16>(p, in, counts_in, out, counts_zero, s);
-    case 9: return launch_stream_rows<32>(p, in, counts_in, out, counts_zero, s);
+    case 0: return launch_tile<32, 8>(p, in, counts_in, out, counts_zero, s, win);
+    case 1: return launch_tile<64, 8>(p, in, counts_in, out, counts_zero, s, win);
+    case 2: return launch_tile<32, 16>(p, in, counts_in, out, counts_zero, s, win);
+    case 3: return launch_tile<64, 16>(p, in, counts_in, out, counts_zero, s, win);
+    case 4: return launch_tile<128, 8>(p, in, counts_in, out, counts_zero, s, win);
+    case 5: return launch_tile<128, 16>(p, in, counts_in, out, counts_zero, s, win);
+    case 6: return launch_tile<256, 8>(p, in, counts_in, out, counts_zero, s, win);
+    case 7: return launch_stream_rows<8>(p, in, counts_in, out, counts_zero, s, win);
+    case 8: return launch_stream_rows<16>(p, in, counts_in, out, counts_zero, s, win);
+    case 9: return launch_stream_rows<32>(p, in, counts_in, out, counts_zero, s, win);
     default: return cudaErrorInvalidValue;
     }
 }

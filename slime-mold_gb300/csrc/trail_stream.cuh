@@ -31,16 +31,42 @@ __device__ __forceinline__ uint4 load_count4(const uint4* p) {
     return kCoherent ? __ldcg(p) : __ldg(p);
 }
 
+// One input row as a lane sees it: its four cells and, for the first lane and
+// the last active lane of the warp, the R wrapped halo cells on its open side.
+template <int R>
+struct RowFetch {
+    float4 t;
+    uint4 k;
+    float ht[R];
+    uint32_t hk[R];
+};
+
 template <int R, bool kCoherent>
-__device__ __forceinline__ void load_ext_row(const DevParams& p, const float* __restrict__ in,
-                                             const uint32_t* __restrict__ cin, int row, int c0, bool active,
-                                             bool left_edge, bool right_edge, const float4& t, const uint4& k,
-                                             ExtRow<R>& e) {
-    float d0 = apply_decay(p, fold_deposits(t.x, k.x, p.dep));
-    float d1 = apply_decay(p, fold_deposits(t.y, k.y, p.dep));
-    float d2 = apply_decay(p, fold_deposits(t.z, k.z, p.dep));
-    float d3 = apply_decay(p, fold_deposits(t.w, k.w, p.dep));
-    float d[4] = {d0, d1, d2, d3};
+__device__ __forceinline__ void fetch_row(const DevParams& p, const float* __restrict__ in,
+                                          const uint32_t* __restrict__ cin, int row, int cl, bool has_halo,
+                                          int hcol0, RowFetch<R>& f) {
+    const size_t base = (size_t)row * p.W;
+    f.t = __ldg(reinterpret_cast<const float4*>(in + base + cl));
+    f.k = load_count4<kCoherent>(reinterpret_cast<const uint4*>(cin + base + cl));
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        f.ht[j] = 0.0f;
+        f.hk[j] = 0u;
+        if (has_halo) {
+            int col = wrap_coord(hcol0 + j, p.W);
+            f.ht[j] = __ldg(in + base + col);
+            f.hk[j] = load_count<kCoherent>(cin + base + col);
+        }
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch<R>& f, bool left_edge,
+                                              bool right_edge, ExtRow<R>& e) {
+    float d[4] = {apply_decay(p, fold_deposits(f.t.x, f.k.x, p.dep)),
+                  apply_decay(p, fold_deposits(f.t.y, f.k.y, p.dep)),
+                  apply_decay(p, fold_deposits(f.t.z, f.k.z, p.dep)),
+                  apply_decay(p, fold_deposits(f.t.w, f.k.w, p.dep))};
 #pragma unroll
     for (int j = 0; j < 4; j++) e.v[R + j] = d[j];
 #pragma unroll
@@ -48,20 +74,11 @@ __device__ __forceinline__ void load_ext_row(const DevParams& p, const float* __
         e.v[j] = __shfl_up_sync(0xffffffffu, d[4 - R + j], 1);
         e.v[R + 4 + j] = __shfl_down_sync(0xffffffffu, d[j], 1);
     }
-    const size_t base = (size_t)row * p.W;
-    if (active && left_edge) {
 #pragma unroll
-        for (int j = 0; j < R; j++) {
-            int col = wrap_coord(c0 - R + j, p.W);
-            e.v[j] = apply_decay(p, fold_deposits(__ldg(in + base + col), load_count<kCoherent>(cin + base + col), p.dep));
-        }
-    }
-    if (right_edge) {
-#pragma unroll
-        for (int j = 0; j < R; j++) {
-            int col = wrap_coord(c0 + 4 + j, p.W);
-            e.v[R + 4 + j] = apply_decay(p, fold_deposits(__ldg(in + base + col), load_count<kCoherent>(cin + base + col), p.dep));
-        }
+    for (int j = 0; j < R; j++) {
+        float h = apply_decay(p, fold_deposits(f.ht[j], f.hk[j], p.dep));
+        if (left_edge) e.v[j] = h;
+        if (right_edge) e.v[R + 4 + j] = h;
     }
 }
 
@@ -85,22 +102,18 @@ __device__ __forceinline__ void process_strip(const DevParams& p, const float* _
     ExtRow<R> win[NWIN];
     float hwin[NWIN][4];
 
-    float4 tn;
-    uint4 kn;
-    {
-        const size_t off = (size_t)wrap_coord(y0 - R, H) * W + cl;
-        tn = __ldg(reinterpret_cast<const float4*>(in + off));
-        kn = load_count4<kCoherent>(reinterpret_cast<const uint4*>(cin + off));
-    }
-#pragma unroll 2
-    for (int r = 0; r < ROWS + 2 * R; r++) {
-        float4 t = tn;
-        uint4 k = kn;
-        if (r + 1 < ROWS + 2 * R) {
-            const size_t off = (size_t)wrap_coord(y0 - R + r + 1, H) * W + cl;
-            tn = __ldg(reinterpret_cast<const float4*>(in + off));
-            kn = load_count4<kCoherent>(reinterpret_cast<const uint4*>(cin + off));
-        }
+    // rows are fetched two ahead of their use, halo cells with them
+    constexpr int NR = ROWS + 2 * R;
+    const bool has_halo = active && (left_edge || right_edge);
+    const int hcol0 = left_edge ? c0 - R : c0 + 4;
+    RowFetch<R> fa, fb;
+    fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R, H), cl, has_halo, hcol0, fa);
+    fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R + 1, H), cl, has_halo, hcol0, fb);
+#pragma unroll 1
+    for (int r = 0; r < NR; r++) {
+        RowFetch<R> cur = fa;
+        fa = fb;
+        if (r + 2 < NR) fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R + r + 2, H), cl, has_halo, hcol0, fb);
         // shift the window and add the new row
 #pragma unroll
         for (int q = 0; q < NWIN - 1; q++) {
@@ -110,8 +123,7 @@ __device__ __forceinline__ void process_strip(const DevParams& p, const float* _
                 for (int j = 0; j < 4; j++) hwin[q][j] = hwin[q + 1][j];
             }
         }
-        load_ext_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R + r, H), c0, active, left_edge, right_edge, t, k,
-                        win[NWIN - 1]);
+        build_ext_row<R>(p, cur, left_edge && active, right_edge, win[NWIN - 1]);
         if (kGauss) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {

@@ -68,18 +68,24 @@ def isnan(x):
 
 
 def fmin(a, b):
+    """minimumNumber: NaN ignored, -0 below +0."""
     if isnan(a):
         return f32(b)
     if isnan(b):
         return f32(a)
+    if a == b:
+        return f32(a) if np.signbit(a) else f32(b)
     return f32(b) if b < a else f32(a)
 
 
 def fmax(a, b):
+    """maximumNumber: NaN ignored, +0 above -0."""
     if isnan(a):
         return f32(b)
     if isnan(b):
         return f32(a)
+    if a == b:
+        return f32(b) if np.signbit(a) else f32(a)
     return f32(b) if b > a else f32(a)
 
 

@@ -21,8 +21,11 @@ def bits(a):
 
 
 def assert_bitexact(gpu_arr, cpu_arr, what):
-    g, c = bits(gpu_arr), bits(cpu_arr)
-    bad = np.flatnonzero(g.reshape(-1) != c.reshape(-1))
+    """Bit-for-bit equality; two NaNs match whatever their payloads (the GPU
+    produces the canonical NaN, a CPU propagates the operand's payload)."""
+    g, c = bits(gpu_arr).reshape(-1), bits(cpu_arr).reshape(-1)
+    both_nan = np.isnan(np.asarray(gpu_arr, np.float32).reshape(-1)) & np.isnan(np.asarray(cpu_arr, np.float32).reshape(-1))
+    bad = np.flatnonzero((g != c) & ~both_nan)
     assert bad.size == 0, (f"{what}: {bad.size} mismatches, first at {bad[:5]}: "
                            f"gpu={np.asarray(gpu_arr).reshape(-1)[bad[:5]]} cpu={np.asarray(cpu_arr).reshape(-1)[bad[:5]]}")
 
@@ -178,12 +181,20 @@ def test_edge_positions_and_sensor_bounds(gpu):
         (-1e-8, 5.0, np.pi, 1.0), (5.0, -1e-8, 1.5 * np.pi, 1.0), (W - 0.5, H - 0.5, 0.785, 60.0),
         (31.5, 23.5, -7.0, 40.0), (10.0, 10.0, 1e6, 40.0), (10.0, 10.0, -1e7, 40.0), (0.0, 0.0, 0.0, 0.0),
         (Wf - np.float32(2e-6), Hf - np.float32(2e-6), 0.01, 1.0),
+        (3.0, 3.0, -0.0, -0.0), (4.0, 4.0, 0.0, -0.0), (5.0, 5.0, np.nan, 40.0), (6.0, np.nan, 1.0, 40.0),
+        (np.inf, 7.0, 1.0, 40.0), (8.0, 8.0, 1.0, np.nan),
     ]
     agents = np.array(rows, np.float32)
     n = agents.shape[0]
     trail = np.random.default_rng(8).random((H, W), dtype=np.float32)
-    p = config0_params(W, H, decay_mode=0, blur_mode=0, agent_sensor_distance=20.0, agent_speed_min=0.5,
-                       agent_speed_max=100.0, agent_jitter=1.0, agent_turn_speed=0.43)
+    for smin in (0.5, 0.0):
+        p = config0_params(W, H, decay_mode=0, blur_mode=0, agent_sensor_distance=20.0, agent_speed_min=smin,
+                           agent_speed_max=100.0, agent_jitter=1.0, agent_turn_speed=0.43)
+        _edge_case(W, H, agents, trail, p)
+
+
+def _edge_case(W, H, agents, trail, p):
+    n = agents.shape[0]
     sim = make_sim(W, H, n, p, agents, trail)
     for s in range(5):
         sim.step(1)
