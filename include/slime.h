@@ -257,6 +257,26 @@ int slime_ensemble_autotune(slime_ensemble* ens, uint32_t reps);
 /* Total kernels enqueued so far. */
 int slime_ensemble_launch_count(const slime_ensemble* ens, uint64_t* out);
 
+/* ------------------------------------------------ step without allocation */
+/* No counterpart in the reference.  One step (agents, then deposit fold +
+ * decay + diffuse) over caller-owned device buffers, for callers that may not
+ * allocate device memory while they run (an engine that owns all device
+ * memory in a pre-reserved arena, a frame loop that cannot afford the device
+ * synchronisation a cudaMalloc may cause).  It calls no cudaMalloc/cudaFree:
+ * the deposit counts live in a fixed array inside the library, sized for
+ * trails of at most 1,048,576 cells (4 MiB, held on every GPU that loads the
+ * library until the process exits); larger trails, width or height < 2 and
+ * d_trail_in == d_trail_out return SLIME_ERR_INVALID_ARGUMENT.  d_x, d_y,
+ * d_angle, d_speed: n_agents floats each (agent i has id i), updated in place;
+ * d_trail_in / d_trail_out: width*height floats.  Work is enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and not waited for.
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture).  All calls share the array and clear it at
+ * their start, so calls that overlap on the GPU race. */
+int slime_step_noalloc(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents, float* d_x,
+                       float* d_y, float* d_angle, float* d_speed, const float* d_trail_in, float* d_trail_out,
+                       void* stream);
+
 /* ------------------------------------------------ display feed */
 /* Headless equivalent of src/display.wgsl:44-86: colourise the current trail
  * through a 256-entry LUT (768 bytes: R[256] G[256] B[256], the .lut format)

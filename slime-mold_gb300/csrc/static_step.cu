@@ -1,0 +1,101 @@
+// static_step.cu - one simulation step over caller-owned device buffers that
+// allocates no device memory.
+//
+// Some callers cannot allocate device memory while they run: a host engine
+// that reserves all device memory up front in its own arena and forbids
+// allocations afterwards, a real-time display loop where a cudaMalloc (which
+// can synchronise the device) would stall a frame, or a process whose device
+// memory is already held by another allocator.  For them this file offers
+// slime_step_noalloc: the caller passes the agents and both trails as device
+// pointers, and the per-cell deposit counts that the agent pass hands to the
+// trail pass live in a fixed array compiled into the library
+// (slime_noalloc_counts below), so no call allocates.
+//
+// The array has room for kNoAllocMaxCells cells (1,048,576, e.g. a 1024 x
+// 1024 trail; 4 MiB) and every GPU that loads the library keeps it until the
+// process exits.  Every call uses the same array: it is cleared at the start
+// of each call, and calls whose work overlaps on the GPU (different streams,
+// or different host threads on one device) race on it and give wrong counts.
+#include <mutex>
+
+#include "kernels.h"
+
+namespace {
+
+constexpr uint64_t kNoAllocMaxCells = 1ull << 20;
+constexpr int kMaxDevices = 64;
+
+// The deposit counts of the step in flight.  In host code this name is only a
+// host-side stand-in, never a device address: the address is looked up once
+// per device with cudaGetSymbolAddress.
+static __device__ __align__(256) uint32_t slime_noalloc_counts[kNoAllocMaxCells];
+
+std::mutex g_setup_mutex;
+uint32_t* g_counts_addr[kMaxDevices] = {};
+
+// Per-device set-up, done on the first call on each device with that device
+// current.
+int counts_address(int device, uint32_t** out) {
+    if (device < 0 || device >= kMaxDevices) return SLIME_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_counts_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, slime_noalloc_counts);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return SLIME_ERR_CUDA;
+        }
+        g_counts_addr[device] = (uint32_t*)p;
+    }
+    *out = g_counts_addr[device];
+    return SLIME_OK;
+}
+
+} // namespace
+
+extern "C" int slime_step_noalloc(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents,
+                                  float* d_x, float* d_y, float* d_angle, float* d_speed, const float* d_trail_in,
+                                  float* d_trail_out, void* stream) {
+    using namespace slime;
+    if (!params || !d_trail_in || !d_trail_out || d_trail_in == d_trail_out) return SLIME_ERR_INVALID_ARGUMENT;
+    if (n_agents && (!d_x || !d_y || !d_angle || !d_speed)) return SLIME_ERR_INVALID_ARGUMENT;
+    // The sampler reads up to width + 1 cells past a discarded tap's cell 0,
+    // which stays inside the trail only for width, height >= 2.
+    if (width < 2 || height < 2 || (uint64_t)width * height > kNoAllocMaxCells || n_agents >= (1ull << 31))
+        return SLIME_ERR_INVALID_ARGUMENT;
+    DevParams d;
+    const char* why = nullptr;
+    if (!make_dev_params(*params, width, height, &d, &why)) return SLIME_ERR_INVALID_ARGUMENT;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        return SLIME_ERR_NO_DEVICE;
+    }
+    uint32_t* counts = nullptr;
+    int rc = counts_address(device, &counts);
+    if (rc != SLIME_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t cells = (size_t)width * height;
+    if (cudaMemsetAsync(counts, 0, cells * sizeof(uint32_t), s) != cudaSuccess) {
+        cudaGetLastError();
+        return SLIME_ERR_CUDA;
+    }
+    AgentsSoA a;
+    a.x = d_x;
+    a.y = d_y;
+    a.th = d_angle;
+    a.v = d_speed;
+    a.ids = nullptr;
+    a.n = n_agents;
+    a.n_pad = n_agents;
+    // One agent per thread (scalar loads need no padding or 16-byte
+    // alignment of the caller's arrays) and the shared-memory trail tile.
+    const int kScalarShape = 2;
+    cudaError_t e = launch_agents(d, a, d_trail_in, counts, s, kScalarShape, nullptr);
+    if (e == cudaSuccess) e = launch_trail(d, trail_tile_default(), d_trail_in, counts, d_trail_out, nullptr, s, nullptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return SLIME_ERR_CUDA;
+    }
+    return SLIME_OK;
+}
