@@ -43,7 +43,9 @@ CONFIGS = {
     "plain-4096": (4096, 4096, 16_777_216, 1.0, 2.0, 9.0),
     "plain-512": (512, 512, 65_536, 1.0, 2.0, 9.0),
     "plain-8192": (8192, 8192, 67_108_864, 1.5, 3.0, 18.0),
+    "adjoint-1024": (1024, 1024, 1_048_576, 1.0, 2.0, 9.0),
 }
+EXTRA_CONFIGS = ["ensemble-64", "adjoint-1024"]
 
 
 def metric_name(cfg_name):
@@ -170,6 +172,165 @@ def cpu_baseline(params, W, H, n, agents, budget_s=12.0, max_steps=20):
             "cells_per_s": W * H * steps / dt}
 
 
+def ensemble_colonies(seed=1, k=64):
+    """64 independent colonies: side ~ U{256, 512, 1024, 2048}, density ~ U[0.25, 4]
+    agents/cell, per-colony sensor angle [0.2,0.8], distance [4,20], turn
+    [0.1,0.6], jitter [0,0.1], decay [0.90,0.995], diffusion [0.1,0.9],
+    deposition [0.5,2.0]; fp32, seed 1."""
+    import slime_gb300 as sg
+    rng = np.random.default_rng(seed)
+    cols = []
+    for j in range(k):
+        side = int(rng.choice([256, 512, 1024, 2048]))
+        n = int(side * side * rng.uniform(0.25, 4.0))
+        p = make_params(side, side, 1.0, 2.0, float(rng.uniform(4, 20)))
+        p.agent_sensor_angle = float(rng.uniform(0.2, 0.8))
+        p.agent_turn_speed = float(rng.uniform(0.1, 0.6))
+        p.agent_jitter = float(rng.uniform(0.0, 0.1))
+        p.decay_factor = float(rng.uniform(0.90, 0.995))
+        p.diffusion_rate = float(rng.uniform(0.1, 0.9))
+        p.pheromone_deposition_amount = float(rng.uniform(0.5, 2.0))
+        cols.append((side, side, n, p, j))
+    return cols
+
+
+def run_ensemble(args):
+    """Batched ensemble: one persistent launch per step over 64 colonies,
+    against the same colonies run one after the other with the plain path,
+    and against the plain 4096^2 per-cell throughput."""
+    import torch
+    import slime_gb300 as sg
+    torch.cuda.set_device(0)
+    cols = ensemble_colonies()
+    cells = sum(c[0] * c[1] for c in cols)
+    agents_total = sum(c[2] for c in cols)
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    for j, (W, H, n, p, seed) in enumerate(cols):
+        ens.seed_agents(j, 1000 + seed)
+    ens.autotune(2)
+    stream = torch.cuda.ExternalStream(ens.stream_ptr())
+    ens.step(args.warmup)
+    ens.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ens.launch_count()
+    with ClockSampler(0) as clocks:
+        e0.record(stream)
+        ens.step(args.steps)
+        e1.record(stream)
+        ens.sync()
+    ms = e0.elapsed_time(e1)
+    launches = ens.launch_count() - l0
+    ens_cells = cells * args.steps / (ms / 1e3)
+    ens_agents = agents_total * args.steps / (ms / 1e3)
+    del ens
+    # the same colonies, one plain Simulation after the other
+    seq_steps = max(3, min(args.steps, 50))
+    seq_ms = 0.0
+    for W, H, n, p, seed in cols:
+        sim = sg.Simulation(W, H, n, p)
+        sim.seed_agents(1000 + seed)
+        sim.set_options(reorder_every=0)
+        sim.step(3)
+        sim.sync()
+        st = torch.cuda.ExternalStream(sim.stream_ptr())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        sim.step(seq_steps)
+        b.record(st)
+        sim.sync()
+        seq_ms += a.elapsed_time(b)
+        sim.close()
+    seq_cells = cells * seq_steps / (seq_ms / 1e3)
+    # plain single-colony per-cell throughput at 4096^2 (short run)
+    W, H, n, lo, hi, dist = CONFIGS["plain-4096"]
+    sim = sg.Simulation(W, H, n, make_params(W, H, lo, hi, dist))
+    sim.seed_agents(0)
+    sim.set_options(reorder_every=200)
+    sim.autotune(3)
+    sim.step(5)
+    sim.sync()
+    st = torch.cuda.ExternalStream(sim.stream_ptr())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    sim.step(50)
+    b.record(st)
+    sim.sync()
+    plain_cells = W * H * 50 / (a.elapsed_time(b) / 1e3)
+    sim.close()
+    line = {
+        "metric": "trail cells/s (batched ensemble, 64 colonies, one persistent launch per step)",
+        "value": ens_cells, "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "ensemble-64", "colonies": len(cols), "cells": cells, "agents": agents_total,
+                   "sides": sorted(set(c[0] for c in cols))},
+        "agent_steps_per_s": ens_agents,
+        "sequential_plain_cells_per_s": seq_cells, "ensemble_over_sequential": ens_cells / seq_cells,
+        "plain_4096_cells_per_s": plain_cells, "ensemble_over_plain_per_cell": ens_cells / plain_cells,
+        "gpu_launches": launches, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """Adjoint of the trail chain at 1024^2 / 1,048,576 agents: the forward
+    with checkpoints every 50 steps against the backward (segment replay +
+    adjoint stencil), 2000 steps; loss 0.5*||T_2000 - T_target||^2 with the
+    target from a run at decay 0.975, diffusion 0.55, deposition 1.1."""
+    import torch
+    import slime_gb300 as sg
+    torch.cuda.set_device(0)
+    W, H, n, lo, hi, dist = CONFIGS["adjoint-1024"]
+    steps = 2000
+    p = make_params(W, H, lo, hi, dist)
+    agents = make_agents(n, W, H, lo, hi, seed=0)
+    sim = sg.Simulation(W, H, n, p)
+    # target
+    pt = p.copy()
+    pt.decay_factor, pt.diffusion_rate, pt.pheromone_deposition_amount = 0.975, 0.55, 1.1
+    sim.set_params(pt)
+    sim.upload_agents(agents)
+    sim.step(steps)
+    target = sim.download_trail()
+    sim.set_params(p)
+    sim.upload_agents(agents)
+    sim.clear_trail()
+    sim.set_options(reorder_every=0)
+    sim.autotune(2)
+    sim.upload_agents(agents)
+    sim.clear_trail()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.forward_record(steps, 50)
+    t_fwd = time.perf_counter() - t0
+    tn = sim.download_trail()
+    g = tn - target
+    loss = 0.5 * float((g.astype(np.float64) ** 2).sum())
+    t0 = time.perf_counter()
+    grads, d0 = sim.backward(g)
+    t_bwd = time.perf_counter() - t0
+    # plain forward (graphs, no checkpoints) for reference
+    sim.upload_agents(agents)
+    sim.clear_trail()
+    sim.sync()
+    t0 = time.perf_counter()
+    sim.step(steps)
+    sim.sync()
+    t_plain = time.perf_counter() - t0
+    line = {
+        "metric": "adjoint cost / forward cost (1024x1024, 1,048,576 agents, 2000 steps, checkpoints every 50)",
+        "value": t_bwd / t_fwd, "unit": "ratio", "n_gpus": 1, "steps": steps, "warmup": 0,
+        "ms_per_step": 1000 * t_bwd / steps, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "adjoint-1024", "width": W, "height": H, "n_agents": n, "ckpt_every": 50},
+        "forward_record_s": t_fwd, "backward_s": t_bwd, "plain_forward_s": t_plain,
+        "backward_over_plain_forward": t_bwd / t_plain, "loss": loss,
+        "grads": {"d_decay_factor": grads.d_decay_factor, "d_diffusion_rate": grads.d_diffusion_rate,
+                  "d_deposition_amount": grads.d_deposition_amount, "d_trail0_abs_max": float(np.abs(d0).max())},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -224,7 +385,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="plain-4096", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="plain-4096", choices=sorted(set(CONFIGS) | set(EXTRA_CONFIGS)))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reorder-every", type=int, default=200)
     ap.add_argument("--no-l2-persist", action="store_true")
@@ -232,7 +393,14 @@ def main():
     args.warmup = max(args.warmup, 3)
 
     if args.impl == "reference":
-        run_reference(args, args.config)
+        run_reference(args, args.config if args.config in CONFIGS and args.config != "adjoint-1024"
+                      else "plain-4096")
+        return
+    if args.config == "ensemble-64":
+        run_ensemble(args)
+        return
+    if args.config == "adjoint-1024":
+        run_adjoint(args)
         return
 
     import torch
