@@ -481,28 +481,32 @@ def main():
     step_bytes = bytes_agents + bytes_trail
     pct_roofline = step_bytes / (ms_per_step * 1e-3) / 1e9 / peak
 
-    # -- end to end through the C ABI with host buffers
-    host_trail = torch.empty((H, W), dtype=torch.float32, pin_memory=True)
-    host_np = host_trail.numpy()
+    # -- end to end through the C ABI with host buffers: every step uploads the
+    # parameter block and the new trail reaches pinned host memory; the copy of
+    # step s overlaps step s+1 (double-buffered host trails)
+    host = [torch.empty((H, W), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
     e2e_steps = max(3, min(args.steps, 50))
     sim.set_params(params)
     sim.step(1)
-    sim.download_trail(out=host_np)
+    sim.download_trail_async(host[0])
+    sim.wait_download()
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for i in range(e2e_steps):
         sim.set_params(params)
         sim.step(1)
-        sim.download_trail(out=host_np)
+        sim.download_trail_async(host[i % 2])
+    sim.wait_download()
     dt = time.perf_counter() - t0
     if ws > 1:
         t = torch.tensor([dt], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dt = float(t.item())
     e2e = {"value": ws * n * e2e_steps / dt, "unit": "agent-steps/s",
-           "h2d_bytes_per_step": int(np.dtype(np.uint8).itemsize * 72), "d2h_bytes_per_step": 4 * W * H,
+           "h2d_bytes_per_step": 72, "d2h_bytes_per_step": 4 * W * H,
            "steps": e2e_steps, "what": "per step: slime_set_params (72-byte parameter block), slime_step(1), "
-                                       "slime_download_trail into pinned host memory"}
+                                       "slime_download_trail_async of the new trail into pinned host memory "
+                                       "(copy overlapped with the next step; all copies waited for)"}
 
     if rank == 0:
         cpu = None

@@ -199,6 +199,15 @@ int slime_step(slime_ctx* ctx, uint32_t n_steps);
 int slime_sync(slime_ctx* ctx);
 /* The cudaStream_t the context enqueues on. */
 int slime_get_stream(slime_ctx* ctx, void** stream);
+/* Display feed without stalling the step loop: snapshot the current trail on
+ * the device and copy it to `trail` (width*height floats) on a separate copy
+ * stream, so the copy overlaps the steps enqueued after it.  Returns at once;
+ * `trail` is complete after slime_wait_download (or the next
+ * slime_download_trail_async, which first waits for the previous copy).  With
+ * page-locked `trail` the copy is asynchronous; with pageable memory the CUDA
+ * runtime performs it synchronously. */
+int slime_download_trail_async(slime_ctx* ctx, float* trail, uint64_t n_cells);
+int slime_wait_download(slime_ctx* ctx);
 /* Deposit counts of the most recent step (cells receiving k agents hold k). */
 int slime_download_deposit_counts(slime_ctx* ctx, uint32_t* counts, uint64_t n_cells);
 /* Reorder agents in Morton order of their cell now (results are unchanged:

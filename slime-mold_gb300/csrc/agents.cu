@@ -64,8 +64,9 @@ struct Lanes<4> {
 };
 
 // A thread moves APT consecutive slots with one vector load/store per field.
-template <int APT, int BS, bool kIds>
-__global__ void __launch_bounds__(BS) agents_kernel(const __grid_constant__ DevParams p, float* __restrict__ X,
+// MINB > 0 asks the compiler to fit MINB blocks per SM (caps registers).
+template <int APT, int BS, int MINB, bool kIds>
+__global__ void __launch_bounds__(BS, MINB) agents_kernel(const __grid_constant__ DevParams p, float* __restrict__ X,
                                                     float* __restrict__ Y, float* __restrict__ TH,
                                                     float* __restrict__ V, const uint32_t* __restrict__ ids,
                                                     const float* __restrict__ trail, uint32_t* __restrict__ counts,
@@ -160,22 +161,23 @@ __global__ void scale_positions_kernel(float* __restrict__ x, float* __restrict_
     y[i] = slm_mul(y[i], sy);
 }
 
-template <int APT, int BS>
+template <int APT, int BS, int MINB>
 cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
                                   cudaStream_t s, const cudaAccessPolicyWindow* win) {
     uint32_t n_groups = (uint32_t)((a.n + APT - 1) / APT);
     dim3 grid(blocks_for(n_groups, BS));
     if (a.ids)
-        return launch_k(agents_kernel<APT, BS, true>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+        return launch_k(agents_kernel<APT, BS, MINB, true>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
                         (const uint32_t*)a.ids, trail, counts, n_groups, a.n);
-    return launch_k(agents_kernel<APT, BS, false>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+    return launch_k(agents_kernel<APT, BS, MINB, false>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
                     (const uint32_t*)nullptr, trail, counts, n_groups, a.n);
 }
 
 } // namespace
 
-// Agent-kernel shapes: (agents per thread, threads per block).
-const AgentShape kAgentShapes[] = {{4, 256}, {2, 256}, {1, 256}, {4, 128}, {1, 128}};
+// Agent-kernel shapes: (agents per thread, threads per block, min blocks/SM).
+const AgentShape kAgentShapes[] = {{4, 256, 0}, {2, 256, 0}, {1, 256, 0}, {4, 128, 0}, {1, 128, 0},
+                                   {2, 256, 5}, {2, 256, 6}, {4, 256, 4}, {1, 256, 8}};
 
 int agent_shape_count() { return (int)(sizeof(kAgentShapes) / sizeof(kAgentShapes[0])); }
 AgentShape agent_shape(int i) { return kAgentShapes[(i >= 0 && i < agent_shape_count()) ? i : 0]; }
@@ -184,11 +186,15 @@ cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* t
                           cudaStream_t s, int shape, const cudaAccessPolicyWindow* win) {
     if (a.n == 0) return cudaSuccess;
     switch (shape) {
-    case 1: return launch_agents_variant<2, 256>(p, a, trail, counts, s, win);
-    case 2: return launch_agents_variant<1, 256>(p, a, trail, counts, s, win);
-    case 3: return launch_agents_variant<4, 128>(p, a, trail, counts, s, win);
-    case 4: return launch_agents_variant<1, 128>(p, a, trail, counts, s, win);
-    default: return launch_agents_variant<4, 256>(p, a, trail, counts, s, win);
+    case 1: return launch_agents_variant<2, 256, 0>(p, a, trail, counts, s, win);
+    case 2: return launch_agents_variant<1, 256, 0>(p, a, trail, counts, s, win);
+    case 3: return launch_agents_variant<4, 128, 0>(p, a, trail, counts, s, win);
+    case 4: return launch_agents_variant<1, 128, 0>(p, a, trail, counts, s, win);
+    case 5: return launch_agents_variant<2, 256, 5>(p, a, trail, counts, s, win);
+    case 6: return launch_agents_variant<2, 256, 6>(p, a, trail, counts, s, win);
+    case 7: return launch_agents_variant<4, 256, 4>(p, a, trail, counts, s, win);
+    case 8: return launch_agents_variant<1, 256, 8>(p, a, trail, counts, s, win);
+    default: return launch_agents_variant<4, 256, 0>(p, a, trail, counts, s, win);
     }
 }
 

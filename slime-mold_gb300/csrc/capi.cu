@@ -422,6 +422,11 @@ void slime_destroy(slime_ctx* ctx) {
     if (ctx->staging) cudaFree(ctx->staging);
     if (ctx->reorder.buf) cudaFree(ctx->reorder.buf);
     if (ctx->aux) cudaFree(ctx->aux);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->display_snap) cudaFree(ctx->display_snap);
+    if (ctx->snap_ready) cudaEventDestroy(ctx->snap_ready);
+    if (ctx->copy_done) cudaEventDestroy(ctx->copy_done);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -640,6 +645,48 @@ int slime_sync(slime_ctx* ctx) {
 int slime_get_stream(slime_ctx* ctx, void** stream) {
     if (!ctx || !stream) return SLIME_ERR_INVALID_ARGUMENT;
     *stream = (void*)ctx->stream;
+    return SLIME_OK;
+}
+
+int slime_download_trail_async(slime_ctx* ctx, float* trail, uint64_t n_cells) {
+    if (!ctx || !trail) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    const size_t cells = (size_t)ctx->W * ctx->H;
+    if (n_cells != cells)
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "trail has %llu cells, context has %llu",
+                         (unsigned long long)n_cells, (unsigned long long)cells);
+    if (!ctx->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "creating copy stream");
+        CK(cudaEventCreateWithFlags(&ctx->snap_ready, cudaEventDisableTiming), "creating event");
+        CK(cudaEventCreateWithFlags(&ctx->copy_done, cudaEventDisableTiming), "creating event");
+    }
+    if (ctx->display_cells != cells) {
+        if (ctx->copy_pending) CK(cudaEventSynchronize(ctx->copy_done), "waiting for the previous copy");
+        ctx->copy_pending = false;
+        if (ctx->display_snap) cudaFree(ctx->display_snap);
+        ctx->display_snap = nullptr;
+        ctx->display_cells = 0;
+        CK(cudaMalloc(&ctx->display_snap, cells * sizeof(float)), "allocating display snapshot");
+        ctx->display_cells = cells;
+    }
+    // the previous host copy reads the snapshot: finish it before overwriting
+    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_done, 0), "ordering copies");
+    CK(cudaMemcpyAsync(ctx->display_snap, ctx->trail[ctx->cur], cells * sizeof(float), cudaMemcpyDeviceToDevice,
+                       ctx->stream), "snapshotting trail");
+    CK(cudaEventRecord(ctx->snap_ready, ctx->stream), "recording snapshot");
+    CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->snap_ready, 0), "ordering copies");
+    CK(cudaMemcpyAsync(trail, ctx->display_snap, cells * sizeof(float), cudaMemcpyDeviceToHost, ctx->copy_stream),
+       "copying trail to the host");
+    CK(cudaEventRecord(ctx->copy_done, ctx->copy_stream), "recording copy");
+    ctx->copy_pending = true;
+    return SLIME_OK;
+}
+
+int slime_wait_download(slime_ctx* ctx) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->copy_pending) CK(cudaEventSynchronize(ctx->copy_done), "waiting for the trail copy");
+    ctx->copy_pending = false;
     return SLIME_OK;
 }
 

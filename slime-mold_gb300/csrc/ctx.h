@@ -47,6 +47,14 @@ struct slime_ctx {
     void* aux = nullptr; // display buffer
     size_t aux_bytes = 0;
 
+    // Asynchronous display feed: device snapshot + copy stream.
+    cudaStream_t copy_stream = nullptr;
+    float* display_snap = nullptr;
+    size_t display_cells = 0;
+    cudaEvent_t snap_ready = nullptr;  // snapshot written (main stream)
+    cudaEvent_t copy_done = nullptr;   // host copy finished (copy stream)
+    bool copy_pending = false;
+
     // Adjoint recording (adjoint.cu).
     struct Adjoint {
         bool recorded = false;

@@ -26,7 +26,7 @@ struct AgentsSoA {
 // ---- agents.cu
 // Launch shapes of the agent kernel: agents per thread and threads per block.
 struct AgentShape {
-    int apt, threads;
+    int apt, threads, min_blocks;
 };
 int agent_shape_count();
 AgentShape agent_shape(int index);

@@ -165,6 +165,15 @@ class Simulation:
         self._check(self._L.slime_download_trail(self._h, _f32p(t), self.width * self.height), "download_trail")
         return t
 
+    def download_trail_async(self, out):
+        """Start copying the current trail into `out` (a C-contiguous float32
+        array, ideally page-locked); complete after wait_download()."""
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == self.width * self.height
+        self._check(self._L.slime_download_trail_async(self._h, _f32p(out), out.size), "download_trail_async")
+
+    def wait_download(self):
+        self._check(self._L.slime_wait_download(self._h), "wait_download")
+
     def download_deposit_counts(self):
         c = np.empty((self.height, self.width), np.uint32)
         self._check(self._L.slime_download_deposit_counts(self._h, c.ctypes.data_as(_abi.U32P), c.size),

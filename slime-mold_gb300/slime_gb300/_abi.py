@@ -151,6 +151,8 @@ SIGNATURES = {
     "slime_sync": (C.c_int, [P]),
     "slime_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
     "slime_download_deposit_counts": (C.c_int, [P, U32P, C.c_uint64]),
+    "slime_download_trail_async": (C.c_int, [P, F32P, C.c_uint64]),
+    "slime_wait_download": (C.c_int, [P]),
     "slime_reorder_agents": (C.c_int, [P]),
     "slime_profile_steps": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)]),

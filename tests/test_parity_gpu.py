@@ -120,7 +120,7 @@ def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
         assert_bitexact(sim.download_agents(), ca, "agents")
 
 
-@pytest.mark.parametrize("shape", range(1, 6))
+@pytest.mark.parametrize("shape", range(1, 10))
 def test_every_agent_shape_is_bitexact(gpu, shape):
     W, H = 200, 150
     for n in (1, 3, 4097, 20001):
@@ -320,3 +320,28 @@ def test_colorize_matches_display_pass(gpu):
     sim = make_sim(W, H, 4, config0_params(W, H), agents_uniform(4, W, H, 1, 2), trail)
     for tw, th in ((160, 90), (200, 90), (160, 200), (37, 11)):
         assert np.array_equal(sim.colorize(lut, tw, th), oracle.colorize(W, H, trail, lut, tw, th)), (tw, th)
+
+
+def test_async_display_feed_snapshots_the_current_trail(gpu):
+    """slime_download_trail_async copies the trail as it was at the call,
+    while later steps proceed."""
+    import torch
+    W, H, n = 256, 128, 20000
+    p = config0_params(W, H)
+    agents = agents_uniform(n, W, H, 1.0, 2.0, seed=31)
+    sim = make_sim(W, H, n, p, agents, np.random.default_rng(31).random((H, W), dtype=np.float32))
+    sim.step(3)
+    want = sim.download_trail()
+    host = torch.empty((H, W), dtype=torch.float32, pin_memory=True).numpy()
+    sim.download_trail_async(host)
+    sim.step(5)  # the copy must still deliver the step-3 trail
+    sim.wait_download()
+    assert_bitexact(host, want, "async snapshot")
+    later = sim.download_trail()
+    assert not np.array_equal(later, want)
+    pageable = np.empty((H, W), np.float32)
+    sim.download_trail_async(pageable)
+    sim.download_trail_async(host)
+    sim.wait_download()
+    assert_bitexact(pageable, later, "pageable copy")
+    assert_bitexact(host, later, "second pinned copy")
