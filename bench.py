@@ -207,6 +207,7 @@ def run_ensemble(args):
     ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
     for j, (W, H, n, p, seed) in enumerate(cols):
         ens.seed_agents(j, 1000 + seed)
+    ens.set_reorder(args.reorder_every, 2)
     ens.autotune(2)
     stream = torch.cuda.ExternalStream(ens.stream_ptr())
     ens.step(args.warmup)
@@ -229,7 +230,8 @@ def run_ensemble(args):
     for W, H, n, p, seed in cols:
         sim = sg.Simulation(W, H, n, p)
         sim.seed_agents(1000 + seed)
-        sim.set_options(reorder_every=0)
+        sim.set_options(reorder_every=args.reorder_every)
+        sim.autotune(2)
         sim.step(3)
         sim.sync()
         st = torch.cuda.ExternalStream(sim.stream_ptr())
@@ -263,7 +265,7 @@ def run_ensemble(args):
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": "ensemble-64", "colonies": len(cols), "cells": cells, "agents": agents_total,
-                   "sides": sorted(set(c[0] for c in cols))},
+                   "sides": sorted(set(c[0] for c in cols)), "reorder_every": args.reorder_every},
         "agent_steps_per_s": ens_agents,
         "sequential_plain_cells_per_s": seq_cells, "ensemble_over_sequential": ens_cells / seq_cells,
         "plain_4096_cells_per_s": plain_cells, "ensemble_over_plain_per_cell": ens_cells / plain_cells,

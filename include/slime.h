@@ -259,6 +259,9 @@ int slime_ensemble_seed_agents(slime_ensemble* ens, uint32_t colony, uint64_t se
                                float heading_max);
 int slime_ensemble_upload_trail(slime_ensemble* ens, uint32_t colony, const float* trail, uint64_t n_cells);
 int slime_ensemble_download_trail(slime_ensemble* ens, uint32_t colony, float* trail, uint64_t n_cells);
+/* Morton-reorder every colony's agents every `every` steps (0 = never);
+ * results do not change, only the memory order of the agents. */
+int slime_ensemble_set_reorder(slime_ensemble* ens, uint32_t every, uint32_t cell_log2);
 int slime_ensemble_step(slime_ensemble* ens, uint32_t n_steps);
 int slime_ensemble_sync(slime_ensemble* ens);
 int slime_ensemble_get_stream(slime_ensemble* ens, void** stream);

@@ -161,6 +161,102 @@ __global__ void scale_positions_kernel(float* __restrict__ x, float* __restrict_
     y[i] = slm_mul(y[i], sy);
 }
 
+// Persistent variant: a grid sized to the resident capacity walks the groups
+// with a stride, loading the next group's state while the current one is
+// computed, so the stream of agent state does not wait on DRAM latency.
+template <int APT, int BS, int MINB, bool kIds>
+__global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
+    const __grid_constant__ DevParams p, float* __restrict__ X, float* __restrict__ Y, float* __restrict__ TH,
+    float* __restrict__ V, const uint32_t* __restrict__ ids, const float* __restrict__ trail,
+    uint32_t* __restrict__ counts, uint32_t n_groups, uint64_t n) {
+    const uint32_t stride = gridDim.x * BS;
+    uint32_t g = blockIdx.x * BS + threadIdx.x;
+    if (g >= n_groups) return;
+    float x[APT], y[APT], th[APT], v[APT];
+    uint32_t id[APT];
+    uint64_t base = (uint64_t)g * APT;
+    Lanes<APT>::load(X + base, x);
+    Lanes<APT>::load(Y + base, y);
+    Lanes<APT>::load(TH + base, th);
+    Lanes<APT>::load(V + base, v);
+    if (kIds) Lanes<APT>::load_ids(ids + base, id);
+    while (true) {
+        const uint32_t gn = g + stride;
+        const bool more = gn < n_groups;
+        const uint64_t bn = (uint64_t)gn * APT;
+        float xn[APT], yn[APT], thn[APT], vn[APT];
+        uint32_t idn[APT];
+        if (more) {
+            Lanes<APT>::load(X + bn, xn);
+            Lanes<APT>::load(Y + bn, yn);
+            Lanes<APT>::load(TH + bn, thn);
+            Lanes<APT>::load(V + bn, vn);
+            if (kIds) Lanes<APT>::load_ids(ids + bn, idn);
+        }
+        if (!kIds) {
+#pragma unroll
+            for (int j = 0; j < APT; j++) id[j] = (uint32_t)(base + j);
+        }
+        int cell[APT];
+        if (base + APT <= n) {
+#pragma unroll
+            for (int j = 0; j < APT; j++) cell[j] = agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail);
+        } else {
+#pragma unroll
+            for (int j = 0; j < APT; j++)
+                cell[j] = (base + j < n) ? agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail) : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < APT; j++)
+            if (cell[j] >= 0) atomicAdd(counts + cell[j], 1u);
+        Lanes<APT>::store(X + base, x);
+        Lanes<APT>::store(Y + base, y);
+        Lanes<APT>::store(TH + base, th);
+        Lanes<APT>::store(V + base, v);
+        if (!more) break;
+        g = gn;
+        base = bn;
+#pragma unroll
+        for (int j = 0; j < APT; j++) {
+            x[j] = xn[j];
+            y[j] = yn[j];
+            th[j] = thn[j];
+            v[j] = vn[j];
+            if (kIds) id[j] = idn[j];
+        }
+    }
+}
+
+template <int APT, int BS, int MINB>
+cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
+                                     cudaStream_t s, const cudaAccessPolicyWindow* win) {
+    static int per_sm[2] = {0, 0};
+    static int sms = 0;
+    const int k = a.ids ? 1 : 0;
+    if (!per_sm[k]) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (a.ids)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k], agents_persistent_kernel<APT, BS, MINB, true>, BS,
+                                                          0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k], agents_persistent_kernel<APT, BS, MINB, false>,
+                                                          BS, 0);
+        if (per_sm[k] < 1) per_sm[k] = 1;
+        if (sms < 1) sms = 1;
+    }
+    uint32_t n_groups = (uint32_t)((a.n + APT - 1) / APT);
+    unsigned want = (unsigned)(per_sm[k] * sms);
+    unsigned need = blocks_for(n_groups, BS);
+    dim3 grid(want < need ? want : need);
+    if (a.ids)
+        return launch_k(agents_persistent_kernel<APT, BS, MINB, true>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th,
+                        a.v, (const uint32_t*)a.ids, trail, counts, n_groups, a.n);
+    return launch_k(agents_persistent_kernel<APT, BS, MINB, false>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th,
+                    a.v, (const uint32_t*)nullptr, trail, counts, n_groups, a.n);
+}
+
 template <int APT, int BS, int MINB>
 cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
                                   cudaStream_t s, const cudaAccessPolicyWindow* win) {
@@ -176,8 +272,10 @@ cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const 
 } // namespace
 
 // Agent-kernel shapes: (agents per thread, threads per block, min blocks/SM).
+// Entries 9.. are the persistent, prefetching variant.
 const AgentShape kAgentShapes[] = {{4, 256, 0}, {2, 256, 0}, {1, 256, 0}, {4, 128, 0}, {1, 128, 0},
-                                   {2, 256, 5}, {2, 256, 6}, {4, 256, 4}, {1, 256, 8}};
+                                   {2, 256, 5}, {2, 256, 6}, {4, 256, 4}, {1, 256, 8},
+                                   {2, 256, 0}, {1, 256, 0}, {2, 128, 0}};
 
 int agent_shape_count() { return (int)(sizeof(kAgentShapes) / sizeof(kAgentShapes[0])); }
 AgentShape agent_shape(int i) { return kAgentShapes[(i >= 0 && i < agent_shape_count()) ? i : 0]; }
@@ -194,6 +292,9 @@ cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* t
     case 6: return launch_agents_variant<2, 256, 6>(p, a, trail, counts, s, win);
     case 7: return launch_agents_variant<4, 256, 4>(p, a, trail, counts, s, win);
     case 8: return launch_agents_variant<1, 256, 8>(p, a, trail, counts, s, win);
+    case 9: return launch_agents_persistent<2, 256, 0>(p, a, trail, counts, s, win);
+    case 10: return launch_agents_persistent<1, 256, 0>(p, a, trail, counts, s, win);
+    case 11: return launch_agents_persistent<2, 128, 0>(p, a, trail, counts, s, win);
     default: return launch_agents_variant<4, 256, 0>(p, a, trail, counts, s, win);
     }
 }

@@ -801,7 +801,13 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
         }
     }
     // 2. agent-kernel shapes, on a snapshot of the agents that is put back
-    // afterwards (the trial passes write agents and counts[cur]).
+    // afterwards (the trial passes write agents and counts[cur]).  With
+    // reordering on, the agents are put in Morton order first, as the steps
+    // will have them.
+    if (ctx->opt.reorder_every && ctx->agents.n > 0) {
+        int rrc = do_reorder(ctx);
+        if (rrc != SLIME_OK) return rrc;
+    }
     int best_shape = ctx->agent_shape;
     if (ctx->agents.n > 0) {
         const size_t abytes = 4 * ctx->agents.n_pad * sizeof(float);

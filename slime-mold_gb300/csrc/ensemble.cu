@@ -92,8 +92,8 @@ template <int R, bool kGauss, int ROWS>
 __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
     const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
     const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
-    float* __restrict__ TH, float* __restrict__ V, const float* __restrict__ trail_in, uint32_t* counts_in,
-    float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar) {
+    float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS, const float* __restrict__ trail_in,
+    uint32_t* counts_in, float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar) {
     __shared__ DevParams sp;
     // ---- phase 1: agents
     for (uint32_t item = blockIdx.x; item < n_agent_items; item += gridDim.x) {
@@ -115,19 +115,20 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
         float4* pt = reinterpret_cast<float4*>(TH + slot);
         float4* pv = reinterpret_cast<float4*>(V + slot);
         float4 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
+        const uint4 id = __ldcs(reinterpret_cast<const uint4*>(IDS + slot)); // colony-local agent ids
         const float* trail = trail_in + c.trail_off;
         uint32_t* counts = counts_in + c.trail_off;
         int c0, c1 = -1, c2 = -1, c3 = -1;
         if (base + 4 <= c.n) { // full group: no per-agent branch
-            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)base, trail);
-            c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)(base + 1), trail);
-            c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)(base + 2), trail);
-            c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)(base + 3), trail);
+            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+            c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
+            c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
+            c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
         } else {
-            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)base, trail);
-            if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)(base + 1), trail);
-            if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)(base + 2), trail);
-            if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)(base + 3), trail);
+            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+            if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
+            if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
+            if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
         }
         if (c0 >= 0) atomicAdd(counts + c0, 1u);
         if (c1 >= 0) atomicAdd(counts + c1, 1u);
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
 }
 
 typedef void (*EnsKernel)(const DevColony*, const uint2*, uint32_t, const uint4*, uint32_t, float*, float*, float*,
-                          float*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*);
+                          float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*);
 
 template <int ROWS>
 EnsKernel pick_rows(int R, bool gauss) {
@@ -179,6 +180,12 @@ struct slime_ensemble {
     std::vector<Colony> colonies;
     uint64_t total_slots = 0, total_cells = 0;
     float* agent_block = nullptr; // x | y | angle | speed, total_slots each
+    uint32_t* ids = nullptr;      // slot -> colony-local agent id (identity until reordered)
+    uint32_t reorder_every = 0;
+    int reorder_cell_log2 = 2;
+    uint64_t steps_done = 0;
+    uint64_t last_reorder_step = ~0ull;
+    ReorderScratch reorder;
     float* trail[2] = {nullptr, nullptr};
     uint32_t* counts[2] = {nullptr, nullptr};
     int cur = 0;
@@ -281,7 +288,8 @@ cudaError_t enqueue_ens_step(slime_ensemble* e) {
     float* tout = e->trail[1 - cur];
     uint32_t* cz = e->counts[1 - cur];
     GridBarrier* bar = e->d_bar;
-    void* args[] = {&cols, &ai, &nai, &si, &nsi, &X, &Y, &TH, &V, &tin, &cin, &tout, &cz, &bar};
+    const uint32_t* ids = e->ids;
+    void* args[] = {&cols, &ai, &nai, &si, &nsi, &X, &Y, &TH, &V, &ids, &tin, &cin, &tout, &cz, &bar};
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3(e->grid);
@@ -297,6 +305,31 @@ cudaError_t enqueue_ens_step(slime_ensemble* e) {
     if (err != cudaSuccess) return err;
     e->cur = 1 - cur;
     return cudaSuccess;
+}
+
+AgentsSoA colony_soa(slime_ensemble* e, const Colony& c) {
+    AgentsSoA a;
+    a.x = e->agent_block + c.agent_off;
+    a.y = e->agent_block + e->total_slots + c.agent_off;
+    a.th = e->agent_block + 2 * e->total_slots + c.agent_off;
+    a.v = e->agent_block + 3 * e->total_slots + c.agent_off;
+    a.ids = e->ids + c.agent_off;
+    a.n = c.n;
+    a.n_pad = c.n_pad;
+    return a;
+}
+
+// Morton-reorder every colony's slots (results are unchanged: each slot keeps
+// its colony-local id).
+int reorder_all(slime_ensemble* e) {
+    for (const Colony& c : e->colonies) {
+        if (c.n == 0) continue;
+        AgentsSoA a = colony_soa(e, c);
+        ECK(launch_reorder(a, c.W, c.H, e->reorder_cell_log2, e->reorder, e->stream), "reordering agents");
+        e->launches += 5;
+    }
+    e->last_reorder_step = e->steps_done;
+    return SLIME_OK;
 }
 
 int check_barrier(slime_ensemble* e) {
@@ -315,6 +348,14 @@ int run_ens_steps(slime_ensemble* e, uint32_t n) {
     const uint32_t chunk = 50;
     while (n > 0) {
         uint32_t m = n < chunk ? n : chunk;
+        if (e->reorder_every) {
+            if (e->steps_done % e->reorder_every == 0 && e->last_reorder_step != e->steps_done) {
+                int rc = reorder_all(e);
+                if (rc != SLIME_OK) return rc;
+            }
+            uint64_t to_next = e->reorder_every - e->steps_done % e->reorder_every;
+            if (to_next < m) m = (uint32_t)to_next;
+        }
         if (e->use_graphs) {
             auto key = std::make_pair(m, e->cur);
             auto it = e->graphs.find(key);
@@ -344,6 +385,7 @@ int run_ens_steps(slime_ensemble* e, uint32_t n) {
             for (uint32_t i = 0; i < m; i++) ECK(enqueue_ens_step(e), "launching ensemble step");
         }
         e->launches += m;
+        e->steps_done += m;
         n -= m;
     }
     return SLIME_OK;
@@ -438,6 +480,8 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         if ((ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) break;
         if ((ce = cudaMalloc(&e->agent_block, 4 * e->total_slots * sizeof(float))) != cudaSuccess) break;
         if ((ce = cudaMemset(e->agent_block, 0, 4 * e->total_slots * sizeof(float))) != cudaSuccess) break;
+        if ((ce = cudaMalloc(&e->ids, e->total_slots * sizeof(uint32_t))) != cudaSuccess) break;
+        if ((ce = cudaMemset(e->ids, 0, e->total_slots * sizeof(uint32_t))) != cudaSuccess) break;
         for (int i = 0; i < 2 && ce == cudaSuccess; i++) {
             if ((ce = cudaMalloc(&e->trail[i], e->total_cells * sizeof(float))) != cudaSuccess) break;
             if ((ce = cudaMalloc(&e->counts[i], e->total_cells * sizeof(uint32_t))) != cudaSuccess) break;
@@ -455,6 +499,11 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         ce = cudaMemset(e->d_bar, 0, sizeof(GridBarrier));
     } while (0);
     if (ce != cudaSuccess) rc = cuda_error(e->err, ce, "creating the ensemble");
+    for (uint32_t j = 0; rc == SLIME_OK && j < k; j++) {
+        const Colony& c = e->colonies[j];
+        cudaError_t ie = launch_iota(e->ids + c.agent_off, c.n, e->stream);
+        if (ie != cudaSuccess) rc = cuda_error(e->err, ie, "initialising agent ids");
+    }
     if (rc == SLIME_OK) rc = upload_cols(e);
     if (rc == SLIME_OK) rc = build_strip_items(e);
     if (rc == SLIME_OK) rc = size_grid(e);
@@ -472,8 +521,8 @@ void slime_ensemble_destroy(slime_ensemble* e) {
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     ens_invalidate(e);
-    void* ptrs[] = {e->agent_block, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->d_cols,
-                    e->d_agent_items, e->d_strip_items, e->d_bar, e->staging};
+    void* ptrs[] = {e->agent_block, e->ids, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->d_cols,
+                    e->d_agent_items, e->d_strip_items, e->d_bar, e->staging, e->reorder.buf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -500,28 +549,27 @@ int slime_ensemble_set_params(slime_ensemble* e, uint32_t j, const SlimeParams* 
     return upload_cols(e); // the colony table is read by the kernel: graphs stay valid
 }
 
+int ensure_staging(slime_ensemble* e, size_t bytes) {
+    if (e->staging_bytes >= bytes) return SLIME_OK;
+    if (e->staging) cudaFree(e->staging);
+    e->staging = nullptr;
+    e->staging_bytes = 0;
+    ECK(cudaMalloc(&e->staging, bytes), "allocating staging");
+    e->staging_bytes = bytes;
+    return SLIME_OK;
+}
+
 int slime_ensemble_upload_agents(slime_ensemble* e, uint32_t j, const float* aos, uint64_t n) {
     int rc = check_colony(e, j);
     if (rc != SLIME_OK) return rc;
     Colony& c = e->colonies[j];
     if (n != c.n || (!aos && n)) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "agent count mismatch");
     if (n == 0) return SLIME_OK;
-    if (e->staging_bytes < n * sizeof(float4)) {
-        if (e->staging) cudaFree(e->staging);
-        e->staging = nullptr;
-        e->staging_bytes = 0;
-        ECK(cudaMalloc(&e->staging, n * sizeof(float4)), "allocating staging");
-        e->staging_bytes = n * sizeof(float4);
-    }
+    if ((rc = ensure_staging(e, n * sizeof(float4))) != SLIME_OK) return rc;
     ECK(cudaMemcpyAsync(e->staging, aos, n * sizeof(float4), cudaMemcpyHostToDevice, e->stream), "uploading agents");
-    AgentsSoA a;
-    a.x = e->agent_block + c.agent_off;
-    a.y = e->agent_block + e->total_slots + c.agent_off;
-    a.th = e->agent_block + 2 * e->total_slots + c.agent_off;
-    a.v = e->agent_block + 3 * e->total_slots + c.agent_off;
-    a.n = n;
-    a.n_pad = c.n_pad;
+    AgentsSoA a = colony_soa(e, c);
     ECK(launch_aos_to_soa(e->staging, a, e->stream), "converting agents");
+    ECK(launch_iota(a.ids, n, e->stream), "resetting agent ids");
     ECK(cudaStreamSynchronize(e->stream), "uploading agents");
     return SLIME_OK;
 }
@@ -532,20 +580,8 @@ int slime_ensemble_download_agents(slime_ensemble* e, uint32_t j, float* aos, ui
     Colony& c = e->colonies[j];
     if (n != c.n || (!aos && n)) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "agent count mismatch");
     if (n == 0) return SLIME_OK;
-    if (e->staging_bytes < n * sizeof(float4)) {
-        if (e->staging) cudaFree(e->staging);
-        e->staging = nullptr;
-        e->staging_bytes = 0;
-        ECK(cudaMalloc(&e->staging, n * sizeof(float4)), "allocating staging");
-        e->staging_bytes = n * sizeof(float4);
-    }
-    AgentsSoA a;
-    a.x = e->agent_block + c.agent_off;
-    a.y = e->agent_block + e->total_slots + c.agent_off;
-    a.th = e->agent_block + 2 * e->total_slots + c.agent_off;
-    a.v = e->agent_block + 3 * e->total_slots + c.agent_off;
-    a.n = n;
-    a.n_pad = c.n_pad;
+    if ((rc = ensure_staging(e, n * sizeof(float4))) != SLIME_OK) return rc;
+    AgentsSoA a = colony_soa(e, c);
     ECK(launch_soa_to_aos(a, e->staging, e->stream), "converting agents");
     ECK(cudaMemcpyAsync(aos, e->staging, n * sizeof(float4), cudaMemcpyDeviceToHost, e->stream), "downloading agents");
     ECK(cudaStreamSynchronize(e->stream), "downloading agents");
@@ -556,17 +592,19 @@ int slime_ensemble_seed_agents(slime_ensemble* e, uint32_t j, uint64_t seed, flo
     int rc = check_colony(e, j);
     if (rc != SLIME_OK) return rc;
     Colony& c = e->colonies[j];
-    AgentsSoA a;
-    a.x = e->agent_block + c.agent_off;
-    a.y = e->agent_block + e->total_slots + c.agent_off;
-    a.th = e->agent_block + 2 * e->total_slots + c.agent_off;
-    a.v = e->agent_block + 3 * e->total_slots + c.agent_off;
-    a.n = c.n;
-    a.n_pad = c.n_pad;
+    AgentsSoA a = colony_soa(e, c);
     ECK(launch_seed_agents(a, seed, (float)c.W, (float)c.H, hmin, hmax, c.params.agent_speed_min,
                            c.params.agent_speed_max, e->stream),
         "seeding agents");
+    ECK(launch_iota(a.ids, c.n, e->stream), "resetting agent ids");
     ECK(cudaStreamSynchronize(e->stream), "seeding agents");
+    return SLIME_OK;
+}
+
+int slime_ensemble_set_reorder(slime_ensemble* e, uint32_t every, uint32_t cell_log2) {
+    if (!e || cell_log2 > 15) return SLIME_ERR_INVALID_ARGUMENT;
+    e->reorder_every = every;
+    e->reorder_cell_log2 = (int)cell_log2;
     return SLIME_OK;
 }
 
@@ -627,6 +665,17 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
         cudaMemcpyAsync(s + abytes + 2 * tbytes + i * tbytes, e->counts[i], tbytes, cudaMemcpyDeviceToDevice,
                         e->stream);
     }
+    if (e->reorder_every) {
+        int rrc = reorder_all(e);
+        if (rrc != SLIME_OK) {
+            cudaFree(snap);
+            return rrc;
+        }
+        // the snapshot must hold the reordered slots
+        cudaMemcpyAsync(s, e->agent_block, abytes, cudaMemcpyDeviceToDevice, e->stream);
+    }
+    const uint64_t saved_steps = e->steps_done, saved_reorder = e->reorder_every;
+    e->reorder_every = 0;
     const int saved_cur = e->cur;
     const bool saved_graphs = e->use_graphs;
     e->use_graphs = false;
@@ -671,6 +720,8 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     cudaFree(snap);
     e->cur = saved_cur;
     e->use_graphs = saved_graphs;
+    e->steps_done = saved_steps;
+    e->reorder_every = saved_reorder;
     e->rows = best_rows;
     e->blocks_per_sm = best_bps;
     ens_invalidate(e);

@@ -298,6 +298,9 @@ class Ensemble:
         self._check(self._L.slime_ensemble_download_trail(self._h, colony, _f32p(t), t.size), "download_trail")
         return t
 
+    def set_reorder(self, every, cell_log2=2):
+        self._check(self._L.slime_ensemble_set_reorder(self._h, every, cell_log2), "set_reorder")
+
     def step(self, n_steps=1):
         self._check(self._L.slime_ensemble_step(self._h, n_steps), "step")
 

@@ -169,6 +169,7 @@ SIGNATURES = {
     "slime_ensemble_seed_agents": (C.c_int, [P, C.c_uint32, C.c_uint64, C.c_float, C.c_float]),
     "slime_ensemble_upload_trail": (C.c_int, [P, C.c_uint32, F32P, C.c_uint64]),
     "slime_ensemble_download_trail": (C.c_int, [P, C.c_uint32, F32P, C.c_uint64]),
+    "slime_ensemble_set_reorder": (C.c_int, [P, C.c_uint32, C.c_uint32]),
     "slime_ensemble_step": (C.c_int, [P, C.c_uint32]),
     "slime_ensemble_sync": (C.c_int, [P]),
     "slime_ensemble_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),

@@ -120,7 +120,7 @@ def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
         assert_bitexact(sim.download_agents(), ca, "agents")
 
 
-@pytest.mark.parametrize("shape", range(1, 10))
+@pytest.mark.parametrize("shape", range(1, 13))
 def test_every_agent_shape_is_bitexact(gpu, shape):
     W, H = 200, 150
     for n in (1, 3, 4097, 20001):
