@@ -333,6 +333,28 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def aggregate_ranks(ms, units_per_rank, seconds=None):
+    """Whole-job figures over replicas: the slowest rank's time and the sum of
+    the units every rank processed (a single colony does not shard, so each
+    rank runs an independent replica; no collective touches the data path).
+    Works with any initialised torch.distributed backend (NCCL on GPUs, gloo
+    in the CPU tests); without one it is the identity."""
+    import torch
+    import torch.distributed as dist
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    if ws > 1:
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(ms), float(units_per_rank)], dtype=torch.float64, device=dev)
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        ms, units = float(mx[0].item()), float(sm[1].item())
+    else:
+        units = float(units_per_rank)
+    return ms, units, units / (ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -450,12 +472,8 @@ def main():
     barrier()
     ms = e0.elapsed_time(e1)
     launches = sim.info().kernel_launches - info0.kernel_launches
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, _, value = aggregate_ranks(ms, n * args.steps)
     ms_per_step = ms / args.steps
-    value = ws * n * args.steps / (ms / 1e3)
     cells = ws * W * H * args.steps / (ms / 1e3)
 
     # -- per-kernel CUDA-event times over K steps (direct launches)
@@ -500,11 +518,8 @@ def main():
         sim.download_trail_async(host[i % 2])
     sim.wait_download()
     dt = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([dt], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt = float(t.item())
-    e2e = {"value": ws * n * e2e_steps / dt, "unit": "agent-steps/s",
+    _, _, e2e_value = aggregate_ranks(dt * 1e3, n * e2e_steps)
+    e2e = {"value": e2e_value, "unit": "agent-steps/s",
            "h2d_bytes_per_step": 72, "d2h_bytes_per_step": 4 * W * H,
            "steps": e2e_steps, "what": "per step: slime_set_params (72-byte parameter block), slime_step(1), "
                                        "slime_download_trail_async of the new trail into pinned host memory "

@@ -268,6 +268,11 @@ int slime_ensemble_get_stream(slime_ensemble* ens, void** stream);
 int slime_ensemble_autotune(slime_ensemble* ens, uint32_t reps);
 /* Total kernels enqueued so far. */
 int slime_ensemble_launch_count(const slime_ensemble* ens, uint64_t* out);
+/* Failure-detection self-test: runs one block at the ensemble's grid barrier
+ * sized for two, so the release never comes; the bounded wait gives up after
+ * ~0.1 s.  Returns SLIME_ERR_DEVICE_TIMEOUT when the timeout was detected and
+ * cleared (the ensemble stays usable), another code otherwise. */
+int slime_ensemble_selftest_barrier_timeout(slime_ensemble* ens);
 
 /* ------------------------------------------------ step without allocation */
 /* No counterpart in the reference.  One step (agents, then deposit fold +

@@ -175,7 +175,7 @@ void free_adjoint(slime_ctx* ctx) {
     void* ptrs[] = {a.ckpt_agents, a.ckpt_ids, a.ckpt_trail, a.seg_trail, a.seg_counts, a.g[0], a.g[1],
                     a.acc, a.agents_tmp, a.ids_tmp};
     for (void* q : ptrs)
-        if (q) cudaFree(q);
+        if (q) dev_free(q);
     a = slime_ctx::Adjoint();
 }
 
@@ -211,9 +211,9 @@ int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every) 
     a.n_pad = n_pad;
     a.with_ids = ctx->agents.ids != nullptr;
     cudaError_t e;
-    if ((e = cudaMalloc(&a.ckpt_agents, (size_t)a.n_ckpt * 4 * n_pad * sizeof(float))) != cudaSuccess ||
-        (a.with_ids && (e = cudaMalloc(&a.ckpt_ids, (size_t)a.n_ckpt * n_pad * sizeof(uint32_t))) != cudaSuccess) ||
-        (e = cudaMalloc(&a.ckpt_trail, (size_t)a.n_ckpt * cells * sizeof(float))) != cudaSuccess) {
+    if ((e = dev_alloc((void**)&a.ckpt_agents, (size_t)a.n_ckpt * 4 * n_pad * sizeof(float))) != cudaSuccess ||
+        (a.with_ids && (e = dev_alloc((void**)&a.ckpt_ids, (size_t)a.n_ckpt * n_pad * sizeof(uint32_t))) != cudaSuccess) ||
+        (e = dev_alloc((void**)&a.ckpt_trail, (size_t)a.n_ckpt * cells * sizeof(float))) != cudaSuccess) {
         free_adjoint(ctx);
         return cuda_error(ctx->err, e, "allocating checkpoints");
     }
@@ -250,14 +250,14 @@ int slime_backward(slime_ctx* ctx, const float* dl_dtrail_final, SlimeGrads* gra
     cudaError_t e;
     if (!a.seg_trail) {
         // W + 2 zero floats past the last trail: the sampler's discarded taps
-        if ((e = cudaMalloc(&a.seg_trail, ((size_t)K * cells + ctx->W + 2) * sizeof(float))) != cudaSuccess ||
+        if ((e = dev_alloc((void**)&a.seg_trail, ((size_t)K * cells + ctx->W + 2) * sizeof(float))) != cudaSuccess ||
             (e = cudaMemset(a.seg_trail, 0, ((size_t)K * cells + ctx->W + 2) * sizeof(float))) != cudaSuccess ||
-            (e = cudaMalloc(&a.seg_counts, (size_t)K * cells * sizeof(uint32_t))) != cudaSuccess ||
-            (e = cudaMalloc(&a.g[0], cells * sizeof(float))) != cudaSuccess ||
-            (e = cudaMalloc(&a.g[1], cells * sizeof(float))) != cudaSuccess ||
-            (e = cudaMalloc(&a.acc, 4 * sizeof(double))) != cudaSuccess ||
-            (e = cudaMalloc(&a.agents_tmp, 4 * a.n_pad * sizeof(float))) != cudaSuccess ||
-            (a.with_ids && (e = cudaMalloc(&a.ids_tmp, a.n_pad * sizeof(uint32_t))) != cudaSuccess))
+            (e = dev_alloc((void**)&a.seg_counts, (size_t)K * cells * sizeof(uint32_t))) != cudaSuccess ||
+            (e = dev_alloc((void**)&a.g[0], cells * sizeof(float))) != cudaSuccess ||
+            (e = dev_alloc((void**)&a.g[1], cells * sizeof(float))) != cudaSuccess ||
+            (e = dev_alloc((void**)&a.acc, 4 * sizeof(double))) != cudaSuccess ||
+            (e = dev_alloc((void**)&a.agents_tmp, 4 * a.n_pad * sizeof(float))) != cudaSuccess ||
+            (a.with_ids && (e = dev_alloc((void**)&a.ids_tmp, a.n_pad * sizeof(uint32_t))) != cudaSuccess))
             return cuda_error(ctx->err, e, "allocating adjoint buffers");
     }
     CK(cudaMemcpyAsync(a.g[0], dl_dtrail_final, cells * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),

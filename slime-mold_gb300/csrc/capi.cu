@@ -15,8 +15,12 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <stdlib.h>
+
 #include <map>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <utility>
 
 #include "ctx.h"
@@ -93,6 +97,44 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
     return true;
 }
 
+namespace {
+std::mutex g_alloc_mutex;
+std::unordered_map<void*, size_t> g_alloc_sizes;
+size_t g_alloc_live = 0;
+size_t alloc_cap() {
+    static size_t cap = [] {
+        const char* v = getenv("SLIME_DEVICE_MEMORY_CAP");
+        return (v && *v) ? (size_t)strtoull(v, nullptr, 10) : (size_t)0;
+    }();
+    return cap;
+}
+} // namespace
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    size_t cap = alloc_cap();
+    if (cap && g_alloc_live + bytes > cap) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return e;
+    g_alloc_sizes[*p] = bytes;
+    g_alloc_live += bytes;
+    return cudaSuccess;
+}
+
+void dev_free(void* p) {
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lock(g_alloc_mutex);
+        auto it = g_alloc_sizes.find(p);
+        if (it != g_alloc_sizes.end()) {
+            g_alloc_live -= it->second;
+            g_alloc_sizes.erase(it);
+        }
+    }
+    cudaFree(p);
+}
+
 int set_error(std::string& err, int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -122,8 +164,8 @@ int cuda_error(std::string& err, cudaError_t e, const char* what) {
 namespace {
 
 void free_agents(slime_ctx* ctx) {
-    if (ctx->agent_block) cudaFree(ctx->agent_block);
-    if (ctx->ids_storage) cudaFree(ctx->ids_storage);
+    if (ctx->agent_block) dev_free(ctx->agent_block);
+    if (ctx->ids_storage) dev_free(ctx->ids_storage);
     ctx->agent_block = nullptr;
     ctx->ids_storage = nullptr;
     ctx->agents = AgentsSoA();
@@ -131,8 +173,8 @@ void free_agents(slime_ctx* ctx) {
 
 void free_trail(slime_ctx* ctx) {
     for (int i = 0; i < 2; i++) {
-        if (ctx->trail[i]) cudaFree(ctx->trail[i]);
-        if (ctx->counts[i]) cudaFree(ctx->counts[i]);
+        if (ctx->trail[i]) dev_free(ctx->trail[i]);
+        if (ctx->counts[i]) dev_free(ctx->counts[i]);
         ctx->trail[i] = nullptr;
         ctx->counts[i] = nullptr;
     }
@@ -143,7 +185,7 @@ int alloc_agents(slime_ctx* ctx, uint64_t n) {
     uint64_t n_pad = (n + kAgentPad - 1) / kAgentPad * kAgentPad;
     if (n_pad == 0) n_pad = kAgentPad;
     size_t bytes = 4 * n_pad * sizeof(float);
-    CK(cudaMalloc(&ctx->agent_block, bytes), "allocating agents");
+    CK(dev_alloc((void**)&ctx->agent_block, bytes), "allocating agents");
     CK(cudaMemsetAsync(ctx->agent_block, 0, bytes, ctx->stream), "clearing agents");
     float* b = (float*)ctx->agent_block;
     ctx->agents.x = b;
@@ -161,8 +203,8 @@ int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
     size_t cells = (size_t)W * H;
     for (int i = 0; i < 2; i++) {
         // W + 2 zero floats past the last cell: the sampler's discarded taps
-        CK(cudaMalloc(&ctx->trail[i], (cells + W + 2) * sizeof(float)), "allocating trail");
-        CK(cudaMalloc(&ctx->counts[i], cells * sizeof(uint32_t)), "allocating deposit counts");
+        CK(dev_alloc((void**)&ctx->trail[i], (cells + W + 2) * sizeof(float)), "allocating trail");
+        CK(dev_alloc((void**)&ctx->counts[i], cells * sizeof(uint32_t)), "allocating deposit counts");
         CK(cudaMemsetAsync(ctx->trail[i], 0, (cells + W + 2) * sizeof(float), ctx->stream), "clearing trail");
         CK(cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream), "clearing counts");
     }
@@ -173,10 +215,10 @@ int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
 
 int ensure_staging(slime_ctx* ctx, size_t bytes) {
     if (ctx->staging_bytes >= bytes) return SLIME_OK;
-    if (ctx->staging) cudaFree(ctx->staging);
+    if (ctx->staging) dev_free(ctx->staging);
     ctx->staging = nullptr;
     ctx->staging_bytes = 0;
-    CK(cudaMalloc(&ctx->staging, bytes), "allocating staging buffer");
+    CK(dev_alloc((void**)&ctx->staging, bytes), "allocating staging buffer");
     ctx->staging_bytes = bytes;
     return SLIME_OK;
 }
@@ -311,7 +353,7 @@ int run_steps_graph(slime_ctx* ctx, uint32_t m) {
 int do_reorder(slime_ctx* ctx) {
     if (ctx->agents.n == 0) return SLIME_OK;
     if (!ctx->agents.ids) {
-        CK(cudaMalloc(&ctx->ids_storage, ctx->agents.n_pad * sizeof(uint32_t)), "allocating agent ids");
+        CK(dev_alloc((void**)&ctx->ids_storage, ctx->agents.n_pad * sizeof(uint32_t)), "allocating agent ids");
         CK(cudaMemsetAsync(ctx->ids_storage, 0, ctx->agents.n_pad * sizeof(uint32_t), ctx->stream),
            "clearing agent ids");
         ctx->agents.ids = ctx->ids_storage;
@@ -419,11 +461,11 @@ void slime_destroy(slime_ctx* ctx) {
     free_adjoint(ctx);
     free_agents(ctx);
     free_trail(ctx);
-    if (ctx->staging) cudaFree(ctx->staging);
-    if (ctx->reorder.buf) cudaFree(ctx->reorder.buf);
-    if (ctx->aux) cudaFree(ctx->aux);
+    if (ctx->staging) dev_free(ctx->staging);
+    if (ctx->reorder.buf) dev_free(ctx->reorder.buf);
+    if (ctx->aux) dev_free(ctx->aux);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
-    if (ctx->display_snap) cudaFree(ctx->display_snap);
+    if (ctx->display_snap) dev_free(ctx->display_snap);
     if (ctx->snap_ready) cudaEventDestroy(ctx->snap_ready);
     if (ctx->copy_done) cudaEventDestroy(ctx->copy_done);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -663,10 +705,10 @@ int slime_download_trail_async(slime_ctx* ctx, float* trail, uint64_t n_cells) {
     if (ctx->display_cells != cells) {
         if (ctx->copy_pending) CK(cudaEventSynchronize(ctx->copy_done), "waiting for the previous copy");
         ctx->copy_pending = false;
-        if (ctx->display_snap) cudaFree(ctx->display_snap);
+        if (ctx->display_snap) dev_free(ctx->display_snap);
         ctx->display_snap = nullptr;
         ctx->display_cells = 0;
-        CK(cudaMalloc(&ctx->display_snap, cells * sizeof(float)), "allocating display snapshot");
+        CK(dev_alloc((void**)&ctx->display_snap, cells * sizeof(float)), "allocating display snapshot");
         ctx->display_cells = cells;
     }
     // the previous host copy reads the snapshot: finish it before overwriting
@@ -812,7 +854,7 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
     if (ctx->agents.n > 0) {
         const size_t abytes = 4 * ctx->agents.n_pad * sizeof(float);
         void* snap = nullptr;
-        if (cudaMalloc(&snap, abytes) == cudaSuccess) {
+        if (dev_alloc((void**)&snap, abytes) == cudaSuccess) {
             CK(cudaMemcpyAsync(snap, ctx->agent_block, abytes, cudaMemcpyDeviceToDevice, ctx->stream), "snapshot");
             float best_a = 1e30f;
             for (int sh = 0; sh < agent_shape_count(); sh++) {
@@ -835,7 +877,7 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
             CK(cudaMemcpyAsync(ctx->agent_block, snap, abytes, cudaMemcpyDeviceToDevice, ctx->stream), "restore");
             CK(cudaMemsetAsync(ctx->counts[cur], 0, cells * sizeof(uint32_t), ctx->stream), "restore");
             CK(cudaStreamSynchronize(ctx->stream), "autotuning");
-            cudaFree(snap);
+            dev_free(snap);
         } else {
             cudaGetLastError();
         }
@@ -860,10 +902,10 @@ int slime_colorize(slime_ctx* ctx, const uint8_t* lut768, uint32_t tw, uint32_t 
     cudaSetDevice(ctx->device);
     size_t need = 768 + (size_t)tw * th * 4;
     if (ctx->aux_bytes < need) {
-        if (ctx->aux) cudaFree(ctx->aux);
+        if (ctx->aux) dev_free(ctx->aux);
         ctx->aux = nullptr;
         ctx->aux_bytes = 0;
-        CK(cudaMalloc(&ctx->aux, need), "allocating display buffer");
+        CK(dev_alloc((void**)&ctx->aux, need), "allocating display buffer");
         ctx->aux_bytes = need;
     }
     uint8_t* dlut = (uint8_t*)ctx->aux;

@@ -58,6 +58,14 @@ cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cu
     return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
 }
 
+// Device allocations of the library go through these two functions.  When
+// the environment variable SLIME_DEVICE_MEMORY_CAP holds a byte count, an
+// allocation that would take the library's live total above it fails with
+// cudaErrorMemoryAllocation (reported as SLIME_ERR_OUT_OF_MEMORY), which lets
+// the out-of-memory paths be tested without exhausting a real GPU.
+cudaError_t dev_alloc(void** p, size_t bytes);
+void dev_free(void* p);
+
 // Translate SlimeParams into DevParams; returns false (with a message) on
 // values the kernels cannot honour.
 bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* out, const char** why);

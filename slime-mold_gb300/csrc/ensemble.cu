@@ -4,7 +4,10 @@
 // All colonies' agents live in one SoA block (each colony padded to a
 // multiple of 128 slots) and all trails/counts in one ping-pong pair of
 // buffers.  One cooperative launch per step runs
-//   phase 1: agent work items (1,024 agents of one colony per block item),
+//   phase 1: agents, two per thread per step of a grid-stride walk over all
+//            colonies' agents (parameters of every colony staged in shared
+//            memory; the next pair's state is loaded while the current pair
+//            is computed),
 //   a grid-wide barrier (bounded spin: gives up after about a second and
 //            reports SLIME_ERR_DEVICE_TIMEOUT instead of hanging),
 //   phase 2: trail strips (128 columns x ROWS rows of one colony per warp
@@ -30,7 +33,6 @@ using namespace slime;
 namespace {
 
 constexpr int kEnsThreads = 256;
-constexpr int kAgentsPerItem = 4 * kEnsThreads; // one float4 group per thread
 
 struct DevColony {
     DevParams p;
@@ -58,7 +60,7 @@ struct Colony {
 // Bounded grid barrier: every block arrives once; the last one to arrive
 // releases the others.  A waiter gives up after ~1 s of clock64() cycles,
 // flags the error and returns false (the kernel then skips its second phase).
-__device__ bool grid_barrier(GridBarrier* b, unsigned nblocks) {
+__device__ bool grid_barrier(GridBarrier* b, unsigned nblocks, long long limit_cycles = 2000000000ll) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -74,7 +76,7 @@ __device__ bool grid_barrier(GridBarrier* b, unsigned nblocks) {
         } else {
             long long t0 = clock64();
             while (*vgen == gen) {
-                if (clock64() - t0 > 2000000000ll) {
+                if (clock64() - t0 > limit_cycles) {
                     atomicExch(&b->error, 1);
                     ok = 0;
                     break;
@@ -88,56 +90,105 @@ __device__ bool grid_barrier(GridBarrier* b, unsigned nblocks) {
     return ok != 0;
 }
 
+// Self-test of the bounded wait: one block waits at a barrier sized for two,
+// so the release never comes and the wait must give up by itself.
+__global__ void barrier_timeout_kernel(GridBarrier* bar, long long limit_cycles, int* reached_after) {
+    bool ok = grid_barrier(bar, 2, limit_cycles);
+    if (threadIdx.x == 0) *reached_after = ok ? 1 : 2;
+}
+
+// Colony of global group gg: the last c with goff[c] <= gg (binary search in
+// shared memory; consecutive groups of a thread usually stay in one colony).
+__device__ __forceinline__ int colony_of(const uint32_t* goff, int n_cols, uint32_t gg, int hint) {
+    if (gg >= goff[hint] && gg < goff[hint + 1]) return hint;
+    int lo = 0, hi = n_cols;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (goff[mid] <= gg) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 template <int R, bool kGauss, int ROWS>
 __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
-    const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
+    const DevColony* __restrict__ cols, const uint32_t* __restrict__ group_off, uint32_t n_cols,
     const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
     float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS, const float* __restrict__ trail_in,
     uint32_t* counts_in, float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar) {
-    __shared__ DevParams sp;
-    // ---- phase 1: agents
-    for (uint32_t item = blockIdx.x; item < n_agent_items; item += gridDim.x) {
-        const uint2 it = agent_items[item];
-        __syncthreads();
-        {
-            const uint32_t* src = reinterpret_cast<const uint32_t*>(&cols[it.x].p);
-            uint32_t* dst = reinterpret_cast<uint32_t*>(&sp);
-            for (int w = threadIdx.x; w < (int)(sizeof(DevParams) / 4); w += kEnsThreads) dst[w] = src[w];
+    // every colony's parameter block and the group offsets, staged once
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DevParams* sp = reinterpret_cast<DevParams*>(smem_raw);
+    uint32_t* goff = reinterpret_cast<uint32_t*>(sp + n_cols);
+    constexpr int PW = (int)(sizeof(DevParams) / 4);
+    for (int i = threadIdx.x; i < (int)n_cols * PW; i += kEnsThreads) {
+        int c = i / PW, w = i - c * PW;
+        reinterpret_cast<uint32_t*>(&sp[c])[w] = reinterpret_cast<const uint32_t*>(&cols[c].p)[w];
+    }
+    for (int i = threadIdx.x; i <= (int)n_cols; i += kEnsThreads) goff[i] = group_off[i];
+    __syncthreads();
+    const uint32_t total_groups = goff[n_cols];
+
+    // ---- phase 1: agents, two per thread per group, the next group's state
+    // loaded while the current one is computed
+    constexpr int APT = 2;
+    const uint32_t stride = gridDim.x * kEnsThreads;
+    uint32_t gg = blockIdx.x * kEnsThreads + threadIdx.x;
+    if (gg < total_groups) {
+        int c = colony_of(goff, (int)n_cols, gg, 0);
+        uint64_t local = 2ull * (gg - goff[c]);
+        uint64_t slot = cols[c].agent_off + local;
+        float2 x = __ldcs(reinterpret_cast<const float2*>(X + slot));
+        float2 y = __ldcs(reinterpret_cast<const float2*>(Y + slot));
+        float2 th = __ldcs(reinterpret_cast<const float2*>(TH + slot));
+        float2 v = __ldcs(reinterpret_cast<const float2*>(V + slot));
+        uint2 id = __ldcs(reinterpret_cast<const uint2*>(IDS + slot));
+        while (true) {
+            const uint32_t gn = gg + stride;
+            const bool more = gn < total_groups;
+            int cn = c;
+            uint64_t localn = 0, slotn = 0;
+            float2 xn, yn, thn, vn;
+            uint2 idn;
+            if (more) {
+                cn = colony_of(goff, (int)n_cols, gn, c);
+                localn = 2ull * (gn - goff[cn]);
+                slotn = cols[cn].agent_off + localn;
+                xn = __ldcs(reinterpret_cast<const float2*>(X + slotn));
+                yn = __ldcs(reinterpret_cast<const float2*>(Y + slotn));
+                thn = __ldcs(reinterpret_cast<const float2*>(TH + slotn));
+                vn = __ldcs(reinterpret_cast<const float2*>(V + slotn));
+                idn = __ldcs(reinterpret_cast<const uint2*>(IDS + slotn));
+            }
+            const DevParams& p = sp[c];
+            const uint64_t n = cols[c].n;
+            const uint64_t toff = cols[c].trail_off;
+            const float* trail = trail_in + toff;
+            uint32_t* counts = counts_in + toff;
+            int c0 = -1, c1 = -1;
+            if (local + APT <= n) {
+                c0 = agent_step(p, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+                c1 = agent_step(p, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
+            } else if (local < n) {
+                c0 = agent_step(p, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+            }
+            if (c0 >= 0) atomicAdd(counts + c0, 1u);
+            if (c1 >= 0) atomicAdd(counts + c1, 1u);
+            __stcs(reinterpret_cast<float2*>(X + slot), x);
+            __stcs(reinterpret_cast<float2*>(Y + slot), y);
+            __stcs(reinterpret_cast<float2*>(TH + slot), th);
+            __stcs(reinterpret_cast<float2*>(V + slot), v);
+            if (!more) break;
+            gg = gn;
+            c = cn;
+            local = localn;
+            slot = slotn;
+            x = xn;
+            y = yn;
+            th = thn;
+            v = vn;
+            id = idn;
         }
-        __syncthreads();
-        const DevColony& c = cols[it.x];
-        const uint64_t g = (uint64_t)it.y + threadIdx.x; // float4 group within the colony
-        const uint64_t base = 4 * g;
-        if (base >= c.n) continue;
-        const uint64_t slot = c.agent_off + base;
-        float4* px = reinterpret_cast<float4*>(X + slot);
-        float4* py = reinterpret_cast<float4*>(Y + slot);
-        float4* pt = reinterpret_cast<float4*>(TH + slot);
-        float4* pv = reinterpret_cast<float4*>(V + slot);
-        float4 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
-        const uint4 id = __ldcs(reinterpret_cast<const uint4*>(IDS + slot)); // colony-local agent ids
-        const float* trail = trail_in + c.trail_off;
-        uint32_t* counts = counts_in + c.trail_off;
-        int c0, c1 = -1, c2 = -1, c3 = -1;
-        if (base + 4 <= c.n) { // full group: no per-agent branch
-            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
-            c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
-            c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
-            c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
-        } else {
-            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
-            if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
-            if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
-            if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
-        }
-        if (c0 >= 0) atomicAdd(counts + c0, 1u);
-        if (c1 >= 0) atomicAdd(counts + c1, 1u);
-        if (c2 >= 0) atomicAdd(counts + c2, 1u);
-        if (c3 >= 0) atomicAdd(counts + c3, 1u);
-        __stcs(px, x);
-        __stcs(py, y);
-        __stcs(pt, th);
-        __stcs(pv, v);
     }
     // ---- grid-wide barrier: all deposits of this step are counted
     __threadfence();
@@ -154,8 +205,10 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
     }
 }
 
-typedef void (*EnsKernel)(const DevColony*, const uint2*, uint32_t, const uint4*, uint32_t, float*, float*, float*,
-                          float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*);
+typedef void (*EnsKernel)(const DevColony*, const uint32_t*, uint32_t, const uint4*, uint32_t, float*, float*,
+                          float*, float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*);
+
+size_t ens_smem_bytes(size_t n_cols) { return n_cols * sizeof(DevParams) + (n_cols + 1) * sizeof(uint32_t); }
 
 template <int ROWS>
 EnsKernel pick_rows(int R, bool gauss) {
@@ -190,8 +243,8 @@ struct slime_ensemble {
     uint32_t* counts[2] = {nullptr, nullptr};
     int cur = 0;
     DevColony* d_cols = nullptr;
-    uint2* d_agent_items = nullptr;
-    uint32_t n_agent_items = 0;
+    uint32_t* d_group_off = nullptr; // per colony: first global 2-agent group; [k] = total groups
+    uint32_t n_cols = 0;
     uint4* d_strip_items = nullptr;
     uint32_t n_strip_items = 0;
     GridBarrier* d_bar = nullptr;
@@ -251,9 +304,9 @@ int build_strip_items(slime_ensemble* e) {
         for (uint32_t rs = 0; rs < strips; rs++)
             for (uint32_t cw = 0; cw < wx; cw++) items.push_back(make_uint4((uint32_t)j, cw, rs, 0));
     }
-    if (e->d_strip_items) cudaFree(e->d_strip_items);
+    if (e->d_strip_items) dev_free(e->d_strip_items);
     e->d_strip_items = nullptr;
-    ECK(cudaMalloc(&e->d_strip_items, items.size() * sizeof(uint4)), "allocating strip table");
+    ECK(dev_alloc((void**)&e->d_strip_items, items.size() * sizeof(uint4)), "allocating strip table");
     ECK(cudaMemcpy(e->d_strip_items, items.data(), items.size() * sizeof(uint4), cudaMemcpyHostToDevice),
         "uploading strip table");
     e->n_strip_items = (uint32_t)items.size();
@@ -263,7 +316,11 @@ int build_strip_items(slime_ensemble* e) {
 int size_grid(slime_ensemble* e) {
     EnsKernel k = pick_kernel(e->rows, e->R, e->gauss);
     int per_sm = 0, sms = 0;
-    ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEnsThreads, 0), "occupancy query");
+    size_t smem = ens_smem_bytes(e->n_cols);
+    if (smem > 48 * 1024)
+        ECK(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            "shared memory attribute");
+    ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEnsThreads, smem), "occupancy query");
     ECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device), "SM count");
     if (per_sm < 1) return ens_fail(e, SLIME_ERR_CUDA, "ensemble kernel cannot be resident");
     int want = e->blocks_per_sm > 0 ? (e->blocks_per_sm < per_sm ? e->blocks_per_sm : per_sm) : per_sm;
@@ -279,8 +336,8 @@ cudaError_t enqueue_ens_step(slime_ensemble* e) {
     float* TH = Y + e->total_slots;
     float* V = TH + e->total_slots;
     const DevColony* cols = e->d_cols;
-    const uint2* ai = e->d_agent_items;
-    uint32_t nai = e->n_agent_items;
+    const uint32_t* goff = e->d_group_off;
+    uint32_t ncols = e->n_cols;
     const uint4* si = e->d_strip_items;
     uint32_t nsi = e->n_strip_items;
     const float* tin = e->trail[cur];
@@ -289,12 +346,12 @@ cudaError_t enqueue_ens_step(slime_ensemble* e) {
     uint32_t* cz = e->counts[1 - cur];
     GridBarrier* bar = e->d_bar;
     const uint32_t* ids = e->ids;
-    void* args[] = {&cols, &ai, &nai, &si, &nsi, &X, &Y, &TH, &V, &ids, &tin, &cin, &tout, &cz, &bar};
+    void* args[] = {&cols, &goff, &ncols, &si, &nsi, &X, &Y, &TH, &V, &ids, &tin, &cin, &tout, &cz, &bar};
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3(e->grid);
     cfg.blockDim = dim3(kEnsThreads);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = ens_smem_bytes(e->n_cols);
     cfg.stream = e->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -467,35 +524,42 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
     uint32_t maxw = 0;
     for (const Colony& c : e->colonies) maxw = c.W > maxw ? c.W : maxw;
     e->total_cells = cells + maxw + 4;
-    // agent work items: 1,024 agents of one colony each
-    std::vector<uint2> ai;
+    // 2-agent groups per colony, as prefix offsets
+    std::vector<uint32_t> goff(k + 1, 0);
+    uint64_t groups = 0;
     for (uint32_t j = 0; j < k; j++) {
-        uint64_t groups = (e->colonies[j].n + 3) / 4;
-        for (uint64_t g0 = 0; g0 < groups; g0 += kEnsThreads) ai.push_back(make_uint2(j, (uint32_t)g0));
+        goff[j] = (uint32_t)groups;
+        groups += (e->colonies[j].n + 1) / 2;
     }
-    e->n_agent_items = (uint32_t)ai.size();
+    goff[k] = (uint32_t)groups;
+    e->n_cols = k;
+    if (groups >= (1ull << 32) || k > 1024) {
+        e->err = "ensemble too large (at most 1024 colonies and 2^33 agents)";
+        *status = SLIME_ERR_INVALID_ARGUMENT;
+        slime_ensemble_destroy(e);
+        return nullptr;
+    }
     int rc = SLIME_OK;
     cudaError_t ce = cudaSuccess;
     do {
         if ((ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) break;
-        if ((ce = cudaMalloc(&e->agent_block, 4 * e->total_slots * sizeof(float))) != cudaSuccess) break;
+        if ((ce = dev_alloc((void**)&e->agent_block, 4 * e->total_slots * sizeof(float))) != cudaSuccess) break;
         if ((ce = cudaMemset(e->agent_block, 0, 4 * e->total_slots * sizeof(float))) != cudaSuccess) break;
-        if ((ce = cudaMalloc(&e->ids, e->total_slots * sizeof(uint32_t))) != cudaSuccess) break;
+        if ((ce = dev_alloc((void**)&e->ids, e->total_slots * sizeof(uint32_t))) != cudaSuccess) break;
         if ((ce = cudaMemset(e->ids, 0, e->total_slots * sizeof(uint32_t))) != cudaSuccess) break;
         for (int i = 0; i < 2 && ce == cudaSuccess; i++) {
-            if ((ce = cudaMalloc(&e->trail[i], e->total_cells * sizeof(float))) != cudaSuccess) break;
-            if ((ce = cudaMalloc(&e->counts[i], e->total_cells * sizeof(uint32_t))) != cudaSuccess) break;
+            if ((ce = dev_alloc((void**)&e->trail[i], e->total_cells * sizeof(float))) != cudaSuccess) break;
+            if ((ce = dev_alloc((void**)&e->counts[i], e->total_cells * sizeof(uint32_t))) != cudaSuccess) break;
             if ((ce = cudaMemset(e->trail[i], 0, e->total_cells * sizeof(float))) != cudaSuccess) break;
             ce = cudaMemset(e->counts[i], 0, e->total_cells * sizeof(uint32_t));
         }
         if (ce != cudaSuccess) break;
-        if ((ce = cudaMalloc(&e->d_cols, k * sizeof(DevColony))) != cudaSuccess) break;
-        if ((ce = cudaMalloc(&e->d_agent_items, (ai.size() ? ai.size() : 1) * sizeof(uint2))) != cudaSuccess) break;
-        if (ai.size() &&
-            (ce = cudaMemcpy(e->d_agent_items, ai.data(), ai.size() * sizeof(uint2), cudaMemcpyHostToDevice)) !=
-                cudaSuccess)
+        if ((ce = dev_alloc((void**)&e->d_cols, k * sizeof(DevColony))) != cudaSuccess) break;
+        if ((ce = dev_alloc((void**)&e->d_group_off, (k + 1) * sizeof(uint32_t))) != cudaSuccess) break;
+        if ((ce = cudaMemcpy(e->d_group_off, goff.data(), (k + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
             break;
-        if ((ce = cudaMalloc(&e->d_bar, sizeof(GridBarrier))) != cudaSuccess) break;
+        if ((ce = dev_alloc((void**)&e->d_bar, sizeof(GridBarrier))) != cudaSuccess) break;
         ce = cudaMemset(e->d_bar, 0, sizeof(GridBarrier));
     } while (0);
     if (ce != cudaSuccess) rc = cuda_error(e->err, ce, "creating the ensemble");
@@ -522,9 +586,9 @@ void slime_ensemble_destroy(slime_ensemble* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     ens_invalidate(e);
     void* ptrs[] = {e->agent_block, e->ids, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->d_cols,
-                    e->d_agent_items, e->d_strip_items, e->d_bar, e->staging, e->reorder.buf};
+                    e->d_group_off, e->d_strip_items, e->d_bar, e->staging, e->reorder.buf};
     for (void* p : ptrs)
-        if (p) cudaFree(p);
+        if (p) dev_free(p);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -551,10 +615,10 @@ int slime_ensemble_set_params(slime_ensemble* e, uint32_t j, const SlimeParams* 
 
 int ensure_staging(slime_ensemble* e, size_t bytes) {
     if (e->staging_bytes >= bytes) return SLIME_OK;
-    if (e->staging) cudaFree(e->staging);
+    if (e->staging) dev_free(e->staging);
     e->staging = nullptr;
     e->staging_bytes = 0;
-    ECK(cudaMalloc(&e->staging, bytes), "allocating staging");
+    ECK(dev_alloc((void**)&e->staging, bytes), "allocating staging");
     e->staging_bytes = bytes;
     return SLIME_OK;
 }
@@ -657,7 +721,7 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     if (reps == 0) reps = 3;
     size_t abytes = 4 * e->total_slots * sizeof(float), tbytes = e->total_cells * sizeof(float);
     void* snap = nullptr;
-    ECK(cudaMalloc(&snap, abytes + 2 * tbytes + 2 * tbytes), "allocating autotune snapshot");
+    ECK(dev_alloc((void**)&snap, abytes + 2 * tbytes + 2 * tbytes), "allocating autotune snapshot");
     char* s = (char*)snap;
     cudaMemcpyAsync(s, e->agent_block, abytes, cudaMemcpyDeviceToDevice, e->stream);
     for (int i = 0; i < 2; i++) {
@@ -668,7 +732,7 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     if (e->reorder_every) {
         int rrc = reorder_all(e);
         if (rrc != SLIME_OK) {
-            cudaFree(snap);
+            dev_free(snap);
             return rrc;
         }
         // the snapshot must hold the reordered slots
@@ -717,7 +781,7 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
                         e->stream);
     }
     cudaStreamSynchronize(e->stream);
-    cudaFree(snap);
+    dev_free(snap);
     e->cur = saved_cur;
     e->use_graphs = saved_graphs;
     e->steps_done = saved_steps;
@@ -728,6 +792,27 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     if (rc == SLIME_OK) rc = build_strip_items(e);
     if (rc == SLIME_OK) rc = size_grid(e);
     return rc;
+}
+
+int slime_ensemble_selftest_barrier_timeout(slime_ensemble* e) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(e->device);
+    ECK(cudaStreamSynchronize(e->stream), "self-test");
+    int* flag = nullptr;
+    ECK(dev_alloc((void**)&flag, sizeof(int)), "self-test");
+    cudaMemsetAsync(flag, 0, sizeof(int), e->stream);
+    // about 0.1 s at the GB300's clock
+    barrier_timeout_kernel<<<1, 32, 0, e->stream>>>(e->d_bar, 200000000ll, flag);
+    cudaError_t le = cudaGetLastError();
+    int after = 0;
+    if (le == cudaSuccess) le = cudaMemcpyAsync(&after, flag, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
+    if (le == cudaSuccess) le = cudaStreamSynchronize(e->stream);
+    dev_free(flag);
+    if (le != cudaSuccess) return cuda_error(e->err, le, "self-test");
+    int rc = check_barrier(e); // reads and clears the error flag, resets the barrier
+    if (after != 2 || rc != SLIME_ERR_DEVICE_TIMEOUT)
+        return ens_fail(e, SLIME_ERR_STATE, "the bounded barrier did not time out as expected");
+    return SLIME_ERR_DEVICE_TIMEOUT;
 }
 
 int slime_ensemble_launch_count(const slime_ensemble* e, uint64_t* out) {

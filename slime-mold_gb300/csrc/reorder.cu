@@ -162,10 +162,10 @@ cudaError_t launch_reorder(AgentsSoA& a, uint32_t W, uint32_t H, int cell_log2, 
     size_t need = align256(4 * n) /*keys*/ + align256(4 * nb) /*hist*/ + align256(4 * nblk) /*block sums*/ +
                   4 * align256(4 * n) /*x y th v*/ + align256(4 * n) /*ids*/;
     if (scratch.bytes < need) {
-        if (scratch.buf) cudaFree(scratch.buf);
+        if (scratch.buf) dev_free(scratch.buf);
         scratch.buf = nullptr;
         scratch.bytes = 0;
-        cudaError_t e = cudaMalloc(&scratch.buf, need);
+        cudaError_t e = dev_alloc((void**)&scratch.buf, need);
         if (e != cudaSuccess) return e;
         scratch.bytes = need;
     }

@@ -215,6 +215,26 @@ class Simulation:
     def autotune(self, reps=5):
         self._check(self._L.slime_autotune(self._h, reps), "autotune")
 
+    # -- checkpoint / resume
+    def save_state(self, path):
+        """Write agents (id order, AoS), trail, parameters and the step
+        counter to an .npz file."""
+        p = self.params()
+        np.savez(path, agents=self.download_agents(), trail=self.download_trail(),
+                 params=np.frombuffer(bytes(p), dtype=np.uint8), steps_done=np.uint64(self.info().steps_done),
+                 size=np.array([self.width, self.height, self.n_agents], np.uint64))
+
+    @classmethod
+    def load_state(cls, path):
+        """A new Simulation holding the state saved by save_state."""
+        d = np.load(path)
+        W, H, n = (int(v) for v in d["size"])
+        p = SlimeParams.from_buffer_copy(d["params"].tobytes())
+        sim = cls(W, H, n, p)
+        sim.upload_agents(d["agents"])
+        sim.upload_trail(d["trail"])
+        return sim
+
     # -- adjoint
     def forward_record(self, n_steps, ckpt_every=50):
         self._check(self._L.slime_forward_record(self._h, n_steps, ckpt_every), "forward_record")
@@ -314,6 +334,11 @@ class Ensemble:
 
     def autotune(self, reps=5):
         self._check(self._L.slime_ensemble_autotune(self._h, reps), "autotune")
+
+    def selftest_barrier_timeout(self):
+        """Make the grid barrier's bounded wait run out; returns the status
+        (SLIME_ERR_DEVICE_TIMEOUT = -5 when detected and cleared)."""
+        return self._L.slime_ensemble_selftest_barrier_timeout(self._h)
 
     def launch_count(self):
         v = C.c_uint64()

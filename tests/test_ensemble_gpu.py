@@ -87,3 +87,22 @@ def test_ensemble_rejects_mixed_blur_and_bad_widths(gpu):
         sg.Ensemble([64, 64], [64, 64], [10, 10], [p1, p2])
     with pytest.raises(sg.SlimeError):
         sg.Ensemble([66], [64], [10], [config0_params(66, 64)])
+
+
+def test_bounded_barrier_times_out_and_recovers(gpu):
+    """The grid barrier's wait is bounded: a barrier that can never be
+    released gives SLIME_ERR_DEVICE_TIMEOUT (no hang, no trap), and the
+    ensemble keeps stepping correctly afterwards."""
+    import slime_gb300 as sg
+    cols = colony_setup(13, 1)[:2]
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        ens.upload_agents(j, agents)
+        ens.upload_trail(j, trail)
+    assert ens.selftest_barrier_timeout() == -5
+    ens.step(2)
+    ens.sync()
+    W, H, n, p, agents, trail = cols[0]
+    ca, ct = agents.copy(), trail.copy()
+    oracle.run(p, W, H, ca, ct, 2)
+    assert_bitexact(ens.download_trail(0), ct, "colony 0 after the timeout self-test")

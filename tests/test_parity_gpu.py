@@ -345,3 +345,42 @@ def test_async_display_feed_snapshots_the_current_trail(gpu):
     sim.wait_download()
     assert_bitexact(pageable, later, "pageable copy")
     assert_bitexact(host, later, "second pinned copy")
+
+
+def test_checkpoint_resume_continues_bit_identically(gpu, tmp_path):
+    import slime_gb300 as sg
+    W, H, n = 200, 120, 15000
+    p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, agent_speed_min=30.0,
+                       agent_speed_max=50.0, agent_jitter=0.2)
+    a = make_sim(W, H, n, p, agents_uniform(n, W, H, 30.0, 50.0, seed=41))
+    a.set_options(reorder_every=4)
+    a.step(6)
+    path = str(tmp_path / "state.npz")
+    a.save_state(path)
+    b = sg.Simulation.load_state(path)
+    a.step(5)
+    b.step(5)
+    assert_bitexact(a.download_agents(), b.download_agents(), "agents after resume")
+    assert_bitexact(a.download_trail(), b.download_trail(), "trail after resume")
+
+
+def test_memory_cap_reports_out_of_memory(gpu):
+    """Out-of-memory paths through a capped allocator (SLIME_DEVICE_MEMORY_CAP):
+    the failing call returns SLIME_ERR_OUT_OF_MEMORY and nothing leaks into
+    later calls."""
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    code = (
+        "import sys; sys.path.insert(0, %r); import slime_gb300 as sg\n"
+        "try:\n"
+        "    sg.Simulation(1024, 1024, 1000)\n"
+        "    print('created')\n"
+        "except sg.SlimeError as e:\n"
+        "    print('status', e.status)\n"
+        "s = sg.Simulation(64, 64, 100)\n"
+        "s.step(2); print('small ok')\n" % os.path.join(ROOT, "slime-mold_gb300"))
+    env = dict(os.environ, SLIME_DEVICE_MEMORY_CAP=str(2 * 1024 * 1024))
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+    assert "status -2" in out.stdout and "small ok" in out.stdout, out.stdout + out.stderr
