@@ -542,7 +542,8 @@ def main():
                              f"trail {4 * W * H / 1e6:.0f} MB kept L2-resident by design",
                        "parallelism": f"replicas x{ws}"},
             "cells_per_s": cells, "pct_roofline_step": pct_roofline,
-            "tuned": {"trail_tile": tuned.trail_tile, "agent_shape": tuned.agent_shape},
+            "tuned": {"trail_tile": tuned.trail_tile, "agent_shape": tuned.agent_shape,
+                      "l2_persist_bytes": tuned.l2_persist_bytes},
             "kernels": {"agents": k_agents, "trail": k_trail, "other_ms_per_step": other_ms / kern_steps},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
             "cpu_baseline": cpu,

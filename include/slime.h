@@ -134,6 +134,7 @@ typedef struct SlimeInfo {
     uint32_t reordered;       /* 1 if device agent order differs from id order */
     uint32_t agent_shape;     /* agent-kernel shape index in use */
     uint32_t reserved;
+    uint64_t l2_persist_bytes; /* persisting-L2 carve-out granted for the trail (0 = none) */
 } SlimeInfo;
 
 const char* slime_version(void);

@@ -540,6 +540,8 @@ int slime_get_info(const slime_ctx* ctx, SlimeInfo* out) {
     out->kernel_launches = ctx->launches;
     out->trail_tile = (uint32_t)ctx->tile;
     out->agent_shape = (uint32_t)ctx->agent_shape;
+    out->reserved = 0;
+    out->l2_persist_bytes = ctx->l2_persist_bytes;
     out->reordered = ctx->reordered ? 1u : 0u;
     return SLIME_OK;
 }

@@ -104,6 +104,7 @@ class SlimeInfo(C.Structure):
         ("reordered", C.c_uint32),
         ("agent_shape", C.c_uint32),
         ("reserved", C.c_uint32),
+        ("l2_persist_bytes", C.c_uint64),
     ]
 
 
