@@ -5,10 +5,10 @@
 // multiple of 128 slots, with a slot -> colony-local id map for Morton
 // reordering) and all trails/counts in one ping-pong pair of buffers.  One
 // persistent launch per step (grid = resident capacity) works through a queue
-// built colony by colony: that colony's agent items (512 agents per warp,
-// the next pair's state loaded while the current pair is computed), then its
-// trail strips (128 columns x ROWS rows per warp, the streaming code of the
-// single-colony kernel).  Warps take items with an atomic ticket; a strip of
+// of agent items (512 agents of one colony per warp, the next pair's state
+// loaded while the current pair is computed) and trail strips (128 columns x
+// ROWS rows per warp, the streaming code of the single-colony kernel), the
+// strips of each colony queued right after the next colony's agent items.  Warps take items with an atomic ticket; a strip of
 // colony j waits until colony j's agent items are done (bounded: it gives up
 // after about a second and the step reports SLIME_ERR_DEVICE_TIMEOUT).  Waits
 // only target items already taken by running warps, and each colony's two
@@ -20,6 +20,7 @@
 // parameters may differ.
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -275,10 +276,19 @@ int upload_cols(slime_ensemble* e) {
     return SLIME_OK;
 }
 
+// Queue order: colonies from the most agents to the fewest; the strips of a
+// colony follow the agent items of the next colony, so by the time a warp
+// reaches them the colony's deposits are (nearly always) complete and no warp
+// idles at a colony boundary.
 int build_items(slime_ensemble* e) {
+    const size_t k = e->colonies.size();
+    std::vector<size_t> order(k);
+    for (size_t j = 0; j < k; j++) order[j] = j;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return e->colonies[a].n > e->colonies[b].n; });
     std::vector<uint4> items;
-    std::vector<uint32_t> per(e->colonies.size(), 0);
-    for (size_t j = 0; j < e->colonies.size(); j++) {
+    std::vector<uint32_t> per(k, 0);
+    auto push_agents = [&](size_t j) {
         const Colony& c = e->colonies[j];
         uint64_t groups = (c.n + 1) / 2;
         for (uint64_t g0 = 0; g0 < groups; g0 += kGroupsPerItem) {
@@ -286,10 +296,18 @@ int build_items(slime_ensemble* e) {
             items.push_back(make_uint4(kItemAgents, (uint32_t)j, (uint32_t)g0, (uint32_t)cnt));
             per[j]++;
         }
+    };
+    auto push_strips = [&](size_t j) {
+        const Colony& c = e->colonies[j];
         uint32_t wx = (c.W + 127) / 128, strips = (c.H + e->rows - 1) / e->rows;
         for (uint32_t rs = 0; rs < strips; rs++)
             for (uint32_t cw = 0; cw < wx; cw++) items.push_back(make_uint4(kItemStrip, (uint32_t)j, cw, rs));
+    };
+    for (size_t q = 0; q < k; q++) {
+        push_agents(order[q]);
+        if (q >= 1) push_strips(order[q - 1]);
     }
+    if (k) push_strips(order[k - 1]);
     if (e->d_items) dev_free(e->d_items);
     e->d_items = nullptr;
     ECK(dev_alloc((void**)&e->d_items, (items.size() ? items.size() : 1) * sizeof(uint4)), "allocating work queue");
