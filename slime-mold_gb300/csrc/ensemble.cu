@@ -82,6 +82,14 @@ enum : uint32_t { kItemAgents = 0u, kItemStrip = 1u };
 constexpr int kGroupsPerLane = 8;                          // 2-agent groups per lane per agent item
 constexpr uint32_t kGroupsPerItem = 32u * kGroupsPerLane;  // 512 agents per agent item
 
+// Every colony's parameter block, passed as a kernel parameter (constant
+// bank): the colony of a work item is warp-uniform, so the accesses are
+// uniform constant loads.
+constexpr int kMaxColonies = 128;
+struct EnsParams {
+    DevParams p[kMaxColonies];
+};
+
 struct FlowState {
     unsigned int ticket;
     int error;
@@ -91,20 +99,11 @@ struct FlowState {
 
 template <int R, bool kGauss, int ROWS>
 __global__ void __launch_bounds__(kEnsThreads) ensemble_flow_kernel(
-    const DevColony* __restrict__ cols, const uint4* __restrict__ items, uint32_t n_items,
-    const uint32_t* __restrict__ agent_items_per_colony, uint32_t n_cols, float* __restrict__ X,
+    const __grid_constant__ EnsParams P, const DevColony* __restrict__ cols, const uint4* __restrict__ items,
+    uint32_t n_items, const uint32_t* __restrict__ agent_items_per_colony, float* __restrict__ X,
     float* __restrict__ Y, float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS,
     const float* __restrict__ trail_in, uint32_t* counts_in, float* __restrict__ trail_out,
     uint32_t* __restrict__ counts_zero, FlowState* st, long long wait_limit) {
-    // every colony's parameter block, staged once per block
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    DevParams* sp = reinterpret_cast<DevParams*>(smem_raw);
-    constexpr int PW = (int)(sizeof(DevParams) / 4);
-    for (int i = threadIdx.x; i < (int)n_cols * PW; i += kEnsThreads) {
-        int c = i / PW, w = i - c * PW;
-        reinterpret_cast<uint32_t*>(&sp[c])[w] = reinterpret_cast<const uint32_t*>(&cols[c].p)[w];
-    }
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     while (true) {
         uint32_t t = 0;
@@ -115,7 +114,7 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_flow_kernel(
         const uint32_t j = it.y;
         const DevColony& c = cols[j];
         if (it.x == kItemAgents) {
-            const DevParams& p = sp[j];
+            const DevParams& p = P.p[j];
             const uint64_t n = c.n;
             const float* trail = trail_in + c.trail_off;
             uint32_t* counts = counts_in + c.trail_off;
@@ -176,18 +175,18 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_flow_kernel(
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
             __threadfence();
             if (!ok) continue; // the host reports SLIME_ERR_DEVICE_TIMEOUT
-            process_strip<R, kGauss, ROWS, true>(c.p, trail_in + c.trail_off, counts_in + c.trail_off,
+            process_strip<R, kGauss, ROWS, true>(P.p[j], trail_in + c.trail_off, counts_in + c.trail_off,
                                                  trail_out + c.trail_off, counts_zero + c.trail_off, (int)it.z,
                                                  (int)it.w);
         }
     }
 }
 
-typedef void (*EnsKernel)(const DevColony*, const uint4*, uint32_t, const uint32_t*, uint32_t, float*, float*,
+typedef void (*EnsKernel)(const EnsParams, const DevColony*, const uint4*, uint32_t, const uint32_t*, float*, float*,
                           float*, float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, FlowState*,
                           long long);
 
-size_t ens_smem_bytes(size_t n_cols) { return n_cols * sizeof(DevParams); }
+size_t ens_smem_bytes(size_t) { return 0; }
 
 template <int ROWS>
 EnsKernel pick_rows(int R, bool gauss) {
@@ -223,6 +222,7 @@ struct slime_ensemble {
     int cur = 0;
     DevColony* d_cols = nullptr;
     uint32_t n_cols = 0;
+    EnsParams hparams; // kernel-parameter copy of every colony's DevParams
     uint4* d_items = nullptr;          // the step's work queue (agent items and strips, colony by colony)
     uint32_t n_items = 0;
     uint32_t* d_agent_items = nullptr; // per colony: number of agent items
@@ -260,6 +260,8 @@ void ens_invalidate(slime_ensemble* e) {
 }
 
 int upload_cols(slime_ensemble* e) {
+    memset(&e->hparams, 0, sizeof(e->hparams));
+    for (size_t j = 0; j < e->colonies.size() && j < (size_t)kMaxColonies; j++) e->hparams.p[j] = e->colonies[j].dev;
     std::vector<DevColony> dc(e->colonies.size());
     for (size_t j = 0; j < e->colonies.size(); j++) {
         const Colony& c = e->colonies[j];
@@ -352,8 +354,8 @@ cudaError_t enqueue_ens_step(slime_ensemble* e) {
     cfg.blockDim = dim3(kEnsThreads);
     cfg.dynamicSmemBytes = ens_smem_bytes(e->n_cols);
     cfg.stream = e->stream;
-    err = cudaLaunchKernelEx(&cfg, k, (const DevColony*)e->d_cols, (const uint4*)e->d_items, e->n_items,
-                             (const uint32_t*)e->d_agent_items, e->n_cols, X, Y, TH, V, (const uint32_t*)e->ids,
+    err = cudaLaunchKernelEx(&cfg, k, e->hparams, (const DevColony*)e->d_cols, (const uint4*)e->d_items, e->n_items,
+                             (const uint32_t*)e->d_agent_items, X, Y, TH, V, (const uint32_t*)e->ids,
                              (const float*)e->trail[cur], e->counts[cur], e->trail[1 - cur], e->counts[1 - cur],
                              e->d_flow, wait_limit);
     if (err != cudaSuccess) return err;
@@ -523,8 +525,8 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
     for (const Colony& c : e->colonies) maxw = c.W > maxw ? c.W : maxw;
     e->total_cells = cells + maxw + 4;
     e->n_cols = k;
-    if (k > 1024) {
-        e->err = "an ensemble holds at most 1024 colonies";
+    if (k > (uint32_t)kMaxColonies) {
+        e->err = "an ensemble holds at most 128 colonies";
         *status = SLIME_ERR_INVALID_ARGUMENT;
         slime_ensemble_destroy(e);
         return nullptr;
@@ -598,7 +600,9 @@ int slime_ensemble_set_params(slime_ensemble* e, uint32_t j, const SlimeParams* 
     c.params.width = c.W;
     c.params.height = c.H;
     c.dev = d;
-    return upload_cols(e); // the colony table is read by the kernel: graphs stay valid
+    int urc = upload_cols(e);
+    ens_invalidate(e); // the parameter blocks are baked into the captured launches
+    return urc;
 }
 
 int ensure_staging(slime_ensemble* e, size_t bytes) {
