@@ -79,8 +79,8 @@ __global__ void wait_timeout_kernel(const unsigned int* never, long long limit_c
 // done, so its deposit counts are complete.  Waits only ever target items
 // already taken by running warps, so no residency guarantee is needed.
 enum : uint32_t { kItemAgents = 0u, kItemStrip = 1u };
-constexpr int kGroupsPerLane = 8;                          // 2-agent groups per lane per agent item
-constexpr uint32_t kGroupsPerItem = 32u * kGroupsPerLane;  // 512 agents per agent item
+constexpr int kGroupsPerLane = 16;                         // 2-agent groups per lane per agent item
+constexpr uint32_t kGroupsPerItem = 32u * kGroupsPerLane;  // 1024 agents per agent item
 
 // Every colony's parameter block, passed as a kernel parameter (constant
 // bank): the colony of a work item is warp-uniform, so the accesses are
@@ -105,12 +105,19 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_flow_kernel(
     const float* __restrict__ trail_in, uint32_t* counts_in, float* __restrict__ trail_out,
     uint32_t* __restrict__ counts_zero, FlowState* st, long long wait_limit) {
     const int lane = threadIdx.x & 31;
+    // the next ticket and its descriptor are fetched while the current item runs
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(&st->ticket, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    uint4 it_next = t < n_items ? items[t] : make_uint4(0, 0, 0, 0);
     while (true) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(&st->ticket, 1u);
-        t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= n_items) break;
-        const uint4 it = items[t];
+        const uint4 it = it_next;
+        uint32_t tn = 0;
+        if (lane == 0) tn = atomicAdd(&st->ticket, 1u);
+        tn = __shfl_sync(0xffffffffu, tn, 0);
+        if (tn < n_items) it_next = items[tn];
+        t = tn;
         const uint32_t j = it.y;
         const DevColony& c = cols[j];
         if (it.x == kItemAgents) {
