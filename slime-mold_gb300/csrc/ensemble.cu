@@ -79,8 +79,8 @@ __global__ void wait_timeout_kernel(const unsigned int* never, long long limit_c
 // done, so its deposit counts are complete.  Waits only ever target items
 // already taken by running warps, so no residency guarantee is needed.
 enum : uint32_t { kItemAgents = 0u, kItemStrip = 1u };
-constexpr int kGroupsPerLane = 16;                         // 2-agent groups per lane per agent item
-constexpr uint32_t kGroupsPerItem = 32u * kGroupsPerLane;  // 1024 agents per agent item
+constexpr int kGroupsPerLane = 8;                          // 2-agent groups per lane per agent item
+constexpr uint32_t kGroupsPerItem = 32u * kGroupsPerLane;  // 512 agents per agent item
 
 // Every colony's parameter block, passed as a kernel parameter (constant
 // bank): the colony of a work item is warp-uniform, so the accesses are
@@ -98,7 +98,7 @@ struct FlowState {
 };
 
 template <int R, bool kGauss, int ROWS>
-__global__ void __launch_bounds__(kEnsThreads) ensemble_flow_kernel(
+__global__ void __launch_bounds__(kEnsThreads, 4) ensemble_flow_kernel(
     const __grid_constant__ EnsParams P, const DevColony* __restrict__ cols, const uint4* __restrict__ items,
     uint32_t n_items, const uint32_t* __restrict__ agent_items_per_colony, float* __restrict__ X,
     float* __restrict__ Y, float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS,
