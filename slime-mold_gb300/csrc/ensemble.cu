@@ -2,17 +2,14 @@
 // per step.
 //
 // All colonies' agents live in one SoA block (each colony padded to a
-// multiple of 128 slots, with a slot -> colony-local id map for Morton
-// reordering) and all trails/counts in one ping-pong pair of buffers.  One
-// persistent launch per step (grid = resident capacity) works through a queue
-// of agent items (512 agents of one colony per warp, the next pair's state
-// loaded while the current pair is computed) and trail strips (128 columns x
-// ROWS rows per warp, the streaming code of the single-colony kernel), the
-// strips of each colony queued right after the next colony's agent items.  Warps take items with an atomic ticket; a strip of
-// colony j waits until colony j's agent items are done (bounded: it gives up
-// after about a second and the step reports SLIME_ERR_DEVICE_TIMEOUT).  Waits
-// only target items already taken by running warps, and each colony's two
-// phases run close together in time, so its counts and trail stay in L2.
+// multiple of 128 slots) and all trails/counts in one ping-pong pair of
+// buffers.  One cooperative launch per step runs
+//   phase 1: agent work items (1,024 agents of one colony per block item),
+//   a grid-wide barrier (bounded spin: gives up after about a second and
+//            reports SLIME_ERR_DEVICE_TIMEOUT instead of hanging),
+//   phase 2: trail strips (128 columns x ROWS rows of one colony per warp
+//            item) through the same streaming code as the single-colony
+//            kernel.
 // Each colony keeps its own parameter block, so the colonies are exactly the
 // runs a single Simulation would produce for them (the tests compare bit for
 // bit).  The blur mode and radius must be common to all colonies (they select
@@ -20,7 +17,6 @@
 // parameters may differ.
 #include <string.h>
 
-#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -34,6 +30,7 @@ using namespace slime;
 namespace {
 
 constexpr int kEnsThreads = 256;
+constexpr int kAgentsPerItem = 4 * kEnsThreads; // one float4 group per thread
 
 struct DevColony {
     DevParams p;
@@ -44,6 +41,12 @@ struct DevColony {
     int32_t pad;
 };
 
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+    int error;
+    int pad;
+};
 
 struct Colony {
     uint32_t W, H;
@@ -52,154 +55,120 @@ struct Colony {
     DevParams dev;
 };
 
-// Bounded wait of one thread until *ctr >= target: gives up after
-// limit_cycles of clock64(), flags the error and returns false.
-__device__ bool bounded_wait_geq(const unsigned int* ctr, unsigned int target, long long limit_cycles, int* error) {
-    const volatile unsigned int* v = ctr;
-    if (*v >= target) return true;
-    long long t0 = clock64();
-    while (*v < target) {
-        if (clock64() - t0 > limit_cycles) {
-            atomicExch(error, 1);
-            return false;
+// Bounded grid barrier: every block arrives once; the last one to arrive
+// releases the others.  A waiter gives up after ~1 s of clock64() cycles,
+// flags the error and returns false (the kernel then skips its second phase).
+__device__ bool grid_barrier(GridBarrier* b, unsigned nblocks, long long limit_cycles = 2000000000ll) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int* vgen = &b->gen;
+        unsigned int gen = *vgen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(&b->count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            long long t0 = clock64();
+            while (*vgen == gen) {
+                if (clock64() - t0 > limit_cycles) {
+                    atomicExch(&b->error, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
         }
-        __nanosleep(64);
+        __threadfence();
     }
-    return true;
+    __syncthreads();
+    return ok != 0;
 }
 
-// Self-test of the bounded wait: waits for a counter nothing increments.
-__global__ void wait_timeout_kernel(const unsigned int* never, long long limit_cycles, int* error, int* outcome) {
-    if (threadIdx.x == 0) *outcome = bounded_wait_geq(never, 1u, limit_cycles, error) ? 1 : 2;
+// Self-test of the bounded wait: one block waits at a barrier sized for two,
+// so the release never comes and the wait must give up by itself.
+__global__ void barrier_timeout_kernel(GridBarrier* bar, long long limit_cycles, int* reached_after) {
+    bool ok = grid_barrier(bar, 2, limit_cycles);
+    if (threadIdx.x == 0) *reached_after = ok ? 1 : 2;
 }
-
-// Work queue of one step, in colony order: each colony's agent items, then its
-// trail strips.  A warp takes the next item with an atomic ticket; a strip of
-// colony j first waits (bounded) until all of colony j's agent items are
-// done, so its deposit counts are complete.  Waits only ever target items
-// already taken by running warps, so no residency guarantee is needed.
-enum : uint32_t { kItemAgents = 0u, kItemStrip = 1u };
-constexpr int kGroupsPerLane = 8;                          // 2-agent groups per lane per agent item
-constexpr uint32_t kGroupsPerItem = 32u * kGroupsPerLane;  // 512 agents per agent item
-
-// Every colony's parameter block, passed as a kernel parameter (constant
-// bank): the colony of a work item is warp-uniform, so the accesses are
-// uniform constant loads.
-constexpr int kMaxColonies = 128;
-struct EnsParams {
-    DevParams p[kMaxColonies];
-};
-
-struct FlowState {
-    unsigned int ticket;
-    int error;
-    unsigned int pad[2];
-    unsigned int done[1]; // per colony: agent items finished (sized at allocation)
-};
 
 template <int R, bool kGauss, int ROWS>
-__global__ void __launch_bounds__(kEnsThreads, 4) ensemble_flow_kernel(
-    const __grid_constant__ EnsParams P, const DevColony* __restrict__ cols, const uint4* __restrict__ items,
-    uint32_t n_items, const uint32_t* __restrict__ agent_items_per_colony, float* __restrict__ X,
-    float* __restrict__ Y, float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS,
-    const float* __restrict__ trail_in, uint32_t* counts_in, float* __restrict__ trail_out,
-    uint32_t* __restrict__ counts_zero, FlowState* st, long long wait_limit) {
-    const int lane = threadIdx.x & 31;
-    // the next ticket and its descriptor are fetched while the current item runs
-    uint32_t t = 0;
-    if (lane == 0) t = atomicAdd(&st->ticket, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    uint4 it_next = t < n_items ? items[t] : make_uint4(0, 0, 0, 0);
-    while (true) {
-        if (t >= n_items) break;
-        const uint4 it = it_next;
-        uint32_t tn = 0;
-        if (lane == 0) tn = atomicAdd(&st->ticket, 1u);
-        tn = __shfl_sync(0xffffffffu, tn, 0);
-        if (tn < n_items) it_next = items[tn];
-        t = tn;
-        const uint32_t j = it.y;
-        const DevColony& c = cols[j];
-        if (it.x == kItemAgents) {
-            const DevParams& p = P.p[j];
-            const uint64_t n = c.n;
-            const float* trail = trail_in + c.trail_off;
-            uint32_t* counts = counts_in + c.trail_off;
-            // groups it.z + lane + 32 i, i < kGroupsPerLane, within it.w groups
-            const uint32_t g_end = it.z + it.w;
-            uint32_t g = it.z + lane;
-            if (g < g_end) {
-                uint64_t slot = c.agent_off + 2ull * g;
-                float2 x = __ldcs(reinterpret_cast<const float2*>(X + slot));
-                float2 y = __ldcs(reinterpret_cast<const float2*>(Y + slot));
-                float2 th = __ldcs(reinterpret_cast<const float2*>(TH + slot));
-                float2 v = __ldcs(reinterpret_cast<const float2*>(V + slot));
-                uint2 id = __ldcs(reinterpret_cast<const uint2*>(IDS + slot));
-                while (true) {
-                    const uint32_t gn = g + 32u;
-                    const bool more = gn < g_end;
-                    const uint64_t slotn = c.agent_off + 2ull * gn;
-                    float2 xn, yn, thn, vn;
-                    uint2 idn;
-                    if (more) {
-                        xn = __ldcs(reinterpret_cast<const float2*>(X + slotn));
-                        yn = __ldcs(reinterpret_cast<const float2*>(Y + slotn));
-                        thn = __ldcs(reinterpret_cast<const float2*>(TH + slotn));
-                        vn = __ldcs(reinterpret_cast<const float2*>(V + slotn));
-                        idn = __ldcs(reinterpret_cast<const uint2*>(IDS + slotn));
-                    }
-                    const uint64_t local = 2ull * g;
-                    int c0 = -1, c1 = -1;
-                    if (local + 2 <= n) {
-                        c0 = agent_step(p, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
-                        c1 = agent_step(p, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
-                    } else if (local < n) {
-                        c0 = agent_step(p, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
-                    }
-                    if (c0 >= 0) atomicAdd(counts + c0, 1u);
-                    if (c1 >= 0) atomicAdd(counts + c1, 1u);
-                    __stcs(reinterpret_cast<float2*>(X + slot), x);
-                    __stcs(reinterpret_cast<float2*>(Y + slot), y);
-                    __stcs(reinterpret_cast<float2*>(TH + slot), th);
-                    __stcs(reinterpret_cast<float2*>(V + slot), v);
-                    if (!more) break;
-                    g = gn;
-                    slot = slotn;
-                    x = xn;
-                    y = yn;
-                    th = thn;
-                    v = vn;
-                    id = idn;
-                }
-            }
-            // publish: this item's deposits are counted
-            __threadfence();
-            __syncwarp();
-            if (lane == 0) atomicAdd(&st->done[j], 1u);
-        } else {
-            bool ok = true;
-            if (lane == 0) ok = bounded_wait_geq(&st->done[j], agent_items_per_colony[j], wait_limit, &st->error);
-            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-            __threadfence();
-            if (!ok) continue; // the host reports SLIME_ERR_DEVICE_TIMEOUT
-            process_strip<R, kGauss, ROWS, true>(P.p[j], trail_in + c.trail_off, counts_in + c.trail_off,
-                                                 trail_out + c.trail_off, counts_zero + c.trail_off, (int)it.z,
-                                                 (int)it.w);
+__global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
+    const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
+    const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
+    float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS, const float* __restrict__ trail_in,
+    uint32_t* counts_in, float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar) {
+    __shared__ DevParams sp;
+    // ---- phase 1: agents
+    for (uint32_t item = blockIdx.x; item < n_agent_items; item += gridDim.x) {
+        const uint2 it = agent_items[item];
+        __syncthreads();
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(&cols[it.x].p);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&sp);
+            for (int w = threadIdx.x; w < (int)(sizeof(DevParams) / 4); w += kEnsThreads) dst[w] = src[w];
         }
+        __syncthreads();
+        const DevColony& c = cols[it.x];
+        const uint64_t g = (uint64_t)it.y + threadIdx.x; // float4 group within the colony
+        const uint64_t base = 4 * g;
+        if (base >= c.n) continue;
+        const uint64_t slot = c.agent_off + base;
+        float4* px = reinterpret_cast<float4*>(X + slot);
+        float4* py = reinterpret_cast<float4*>(Y + slot);
+        float4* pt = reinterpret_cast<float4*>(TH + slot);
+        float4* pv = reinterpret_cast<float4*>(V + slot);
+        float4 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
+        const uint4 id = __ldcs(reinterpret_cast<const uint4*>(IDS + slot)); // colony-local agent ids
+        const float* trail = trail_in + c.trail_off;
+        uint32_t* counts = counts_in + c.trail_off;
+        int c0, c1 = -1, c2 = -1, c3 = -1;
+        if (base + 4 <= c.n) { // full group: no per-agent branch
+            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+            c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
+            c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
+            c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
+        } else {
+            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+            if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
+            if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
+            if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
+        }
+        if (c0 >= 0) atomicAdd(counts + c0, 1u);
+        if (c1 >= 0) atomicAdd(counts + c1, 1u);
+        if (c2 >= 0) atomicAdd(counts + c2, 1u);
+        if (c3 >= 0) atomicAdd(counts + c3, 1u);
+        __stcs(px, x);
+        __stcs(py, y);
+        __stcs(pt, th);
+        __stcs(pv, v);
+    }
+    // ---- grid-wide barrier: all deposits of this step are counted
+    __threadfence();
+    if (!grid_barrier(bar, gridDim.x)) return;
+    // ---- phase 2: trail strips, one warp per item
+    const uint32_t warps = gridDim.x * (kEnsThreads / 32);
+    const uint32_t gw = blockIdx.x * (kEnsThreads / 32) + (threadIdx.x >> 5);
+    for (uint32_t item = gw; item < n_strip_items; item += warps) {
+        const uint4 it = strip_items[item];
+        const DevColony& c = cols[it.x];
+        process_strip<R, kGauss, ROWS, true>(c.p, trail_in + c.trail_off, counts_in + c.trail_off,
+                                             trail_out + c.trail_off, counts_zero + c.trail_off, (int)it.y,
+                                             (int)it.z);
     }
 }
 
-typedef void (*EnsKernel)(const EnsParams, const DevColony*, const uint4*, uint32_t, const uint32_t*, float*, float*,
-                          float*, float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, FlowState*,
-                          long long);
-
-size_t ens_smem_bytes(size_t) { return 0; }
+typedef void (*EnsKernel)(const DevColony*, const uint2*, uint32_t, const uint4*, uint32_t, float*, float*, float*,
+                          float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*);
 
 template <int ROWS>
 EnsKernel pick_rows(int R, bool gauss) {
-    if (!gauss) return ensemble_flow_kernel<1, false, ROWS>;
-    if (R == 1) return ensemble_flow_kernel<1, true, ROWS>;
-    return ensemble_flow_kernel<2, true, ROWS>;
+    if (!gauss) return ensemble_step_kernel<1, false, ROWS>;
+    if (R == 1) return ensemble_step_kernel<1, true, ROWS>;
+    return ensemble_step_kernel<2, true, ROWS>;
 }
 
 EnsKernel pick_kernel(int rows, int R, bool gauss) {
@@ -228,13 +197,11 @@ struct slime_ensemble {
     uint32_t* counts[2] = {nullptr, nullptr};
     int cur = 0;
     DevColony* d_cols = nullptr;
-    uint32_t n_cols = 0;
-    EnsParams hparams; // kernel-parameter copy of every colony's DevParams
-    uint4* d_items = nullptr;          // the step's work queue (agent items and strips, colony by colony)
-    uint32_t n_items = 0;
-    uint32_t* d_agent_items = nullptr; // per colony: number of agent items
-    FlowState* d_flow = nullptr;       // ticket, error flag, per-colony done counters
-    size_t flow_bytes = 0;
+    uint2* d_agent_items = nullptr;
+    uint32_t n_agent_items = 0;
+    uint4* d_strip_items = nullptr;
+    uint32_t n_strip_items = 0;
+    GridBarrier* d_bar = nullptr;
     float4* staging = nullptr;
     size_t staging_bytes = 0;
     int rows = 16;
@@ -267,8 +234,6 @@ void ens_invalidate(slime_ensemble* e) {
 }
 
 int upload_cols(slime_ensemble* e) {
-    memset(&e->hparams, 0, sizeof(e->hparams));
-    for (size_t j = 0; j < e->colonies.size() && j < (size_t)kMaxColonies; j++) e->hparams.p[j] = e->colonies[j].dev;
     std::vector<DevColony> dc(e->colonies.size());
     for (size_t j = 0; j < e->colonies.size(); j++) {
         const Colony& c = e->colonies[j];
@@ -285,58 +250,27 @@ int upload_cols(slime_ensemble* e) {
     return SLIME_OK;
 }
 
-// Queue order: colonies from the most agents to the fewest; the strips of a
-// colony follow the agent items of the next colony, so by the time a warp
-// reaches them the colony's deposits are (nearly always) complete and no warp
-// idles at a colony boundary.
-int build_items(slime_ensemble* e) {
-    const size_t k = e->colonies.size();
-    std::vector<size_t> order(k);
-    for (size_t j = 0; j < k; j++) order[j] = j;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](size_t a, size_t b) { return e->colonies[a].n > e->colonies[b].n; });
+int build_strip_items(slime_ensemble* e) {
     std::vector<uint4> items;
-    std::vector<uint32_t> per(k, 0);
-    auto push_agents = [&](size_t j) {
-        const Colony& c = e->colonies[j];
-        uint64_t groups = (c.n + 1) / 2;
-        for (uint64_t g0 = 0; g0 < groups; g0 += kGroupsPerItem) {
-            uint64_t cnt = groups - g0 < kGroupsPerItem ? groups - g0 : kGroupsPerItem;
-            items.push_back(make_uint4(kItemAgents, (uint32_t)j, (uint32_t)g0, (uint32_t)cnt));
-            per[j]++;
-        }
-    };
-    auto push_strips = [&](size_t j) {
+    for (size_t j = 0; j < e->colonies.size(); j++) {
         const Colony& c = e->colonies[j];
         uint32_t wx = (c.W + 127) / 128, strips = (c.H + e->rows - 1) / e->rows;
         for (uint32_t rs = 0; rs < strips; rs++)
-            for (uint32_t cw = 0; cw < wx; cw++) items.push_back(make_uint4(kItemStrip, (uint32_t)j, cw, rs));
-    };
-    for (size_t q = 0; q < k; q++) {
-        push_agents(order[q]);
-        if (q >= 1) push_strips(order[q - 1]);
+            for (uint32_t cw = 0; cw < wx; cw++) items.push_back(make_uint4((uint32_t)j, cw, rs, 0));
     }
-    if (k) push_strips(order[k - 1]);
-    if (e->d_items) dev_free(e->d_items);
-    e->d_items = nullptr;
-    ECK(dev_alloc((void**)&e->d_items, (items.size() ? items.size() : 1) * sizeof(uint4)), "allocating work queue");
-    if (!items.empty())
-        ECK(cudaMemcpy(e->d_items, items.data(), items.size() * sizeof(uint4), cudaMemcpyHostToDevice),
-            "uploading work queue");
-    ECK(cudaMemcpy(e->d_agent_items, per.data(), per.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
-        "uploading work queue");
-    e->n_items = (uint32_t)items.size();
+    if (e->d_strip_items) dev_free(e->d_strip_items);
+    e->d_strip_items = nullptr;
+    ECK(dev_alloc((void**)&e->d_strip_items, items.size() * sizeof(uint4)), "allocating strip table");
+    ECK(cudaMemcpy(e->d_strip_items, items.data(), items.size() * sizeof(uint4), cudaMemcpyHostToDevice),
+        "uploading strip table");
+    e->n_strip_items = (uint32_t)items.size();
     return SLIME_OK;
 }
 
 int size_grid(slime_ensemble* e) {
     EnsKernel k = pick_kernel(e->rows, e->R, e->gauss);
     int per_sm = 0, sms = 0;
-    size_t smem = ens_smem_bytes(e->n_cols);
-    if (smem > 48 * 1024)
-        ECK(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-            "shared memory attribute");
-    ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEnsThreads, smem), "occupancy query");
+    ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEnsThreads, 0), "occupancy query");
     ECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device), "SM count");
     if (per_sm < 1) return ens_fail(e, SLIME_ERR_CUDA, "ensemble kernel cannot be resident");
     int want = e->blocks_per_sm > 0 ? (e->blocks_per_sm < per_sm ? e->blocks_per_sm : per_sm) : per_sm;
@@ -351,20 +285,30 @@ cudaError_t enqueue_ens_step(slime_ensemble* e) {
     float* Y = X + e->total_slots;
     float* TH = Y + e->total_slots;
     float* V = TH + e->total_slots;
-    // ticket, error flag and done counters start at zero every step
-    cudaError_t err = cudaMemsetAsync(e->d_flow, 0, e->flow_bytes, e->stream);
-    if (err != cudaSuccess) return err;
-    const long long wait_limit = 2000000000ll; // ~1 s of clock64() cycles
+    const DevColony* cols = e->d_cols;
+    const uint2* ai = e->d_agent_items;
+    uint32_t nai = e->n_agent_items;
+    const uint4* si = e->d_strip_items;
+    uint32_t nsi = e->n_strip_items;
+    const float* tin = e->trail[cur];
+    uint32_t* cin = e->counts[cur];
+    float* tout = e->trail[1 - cur];
+    uint32_t* cz = e->counts[1 - cur];
+    GridBarrier* bar = e->d_bar;
+    const uint32_t* ids = e->ids;
+    void* args[] = {&cols, &ai, &nai, &si, &nsi, &X, &Y, &TH, &V, &ids, &tin, &cin, &tout, &cz, &bar};
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3(e->grid);
     cfg.blockDim = dim3(kEnsThreads);
-    cfg.dynamicSmemBytes = ens_smem_bytes(e->n_cols);
+    cfg.dynamicSmemBytes = 0;
     cfg.stream = e->stream;
-    err = cudaLaunchKernelEx(&cfg, k, e->hparams, (const DevColony*)e->d_cols, (const uint4*)e->d_items, e->n_items,
-                             (const uint32_t*)e->d_agent_items, X, Y, TH, V, (const uint32_t*)e->ids,
-                             (const float*)e->trail[cur], e->counts[cur], e->trail[1 - cur], e->counts[1 - cur],
-                             e->d_flow, wait_limit);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t err = cudaLaunchKernelExC(&cfg, (const void*)k, args);
     if (err != cudaSuccess) return err;
     e->cur = 1 - cur;
     return cudaSuccess;
@@ -395,15 +339,14 @@ int reorder_all(slime_ensemble* e) {
     return SLIME_OK;
 }
 
-int check_flow(slime_ensemble* e) {
-    int error = 0;
-    ECK(cudaMemcpyAsync(&error, &e->d_flow->error, sizeof(int), cudaMemcpyDeviceToHost, e->stream),
-        "reading the step status");
-    ECK(cudaStreamSynchronize(e->stream), "reading the step status");
-    if (error) {
-        cudaMemsetAsync(e->d_flow, 0, e->flow_bytes, e->stream);
+int check_barrier(slime_ensemble* e) {
+    GridBarrier b;
+    ECK(cudaMemcpyAsync(&b, e->d_bar, sizeof b, cudaMemcpyDeviceToHost, e->stream), "reading barrier state");
+    ECK(cudaStreamSynchronize(e->stream), "reading barrier state");
+    if (b.error) {
+        cudaMemsetAsync(e->d_bar, 0, sizeof(GridBarrier), e->stream);
         cudaStreamSynchronize(e->stream);
-        return ens_fail(e, SLIME_ERR_DEVICE_TIMEOUT, "a bounded device-side wait of the ensemble step timed out");
+        return ens_fail(e, SLIME_ERR_DEVICE_TIMEOUT, "the ensemble's grid barrier timed out");
     }
     return SLIME_OK;
 }
@@ -434,7 +377,7 @@ int run_ens_steps(slime_ensemble* e, uint32_t n) {
                 if (ce == cudaSuccess && ee == cudaSuccess) ee = cudaGraphInstantiate(&exec, g, 0);
                 if (g) cudaGraphDestroy(g);
                 if (ce != cudaSuccess || ee != cudaSuccess) {
-                    // a launch that cannot be captured runs directly
+                    // cooperative launches that cannot be captured run directly
                     cudaGetLastError();
                     e->use_graphs = false;
                     continue;
@@ -531,13 +474,13 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
     uint32_t maxw = 0;
     for (const Colony& c : e->colonies) maxw = c.W > maxw ? c.W : maxw;
     e->total_cells = cells + maxw + 4;
-    e->n_cols = k;
-    if (k > (uint32_t)kMaxColonies) {
-        e->err = "an ensemble holds at most 128 colonies";
-        *status = SLIME_ERR_INVALID_ARGUMENT;
-        slime_ensemble_destroy(e);
-        return nullptr;
+    // agent work items: 1,024 agents of one colony each
+    std::vector<uint2> ai;
+    for (uint32_t j = 0; j < k; j++) {
+        uint64_t groups = (e->colonies[j].n + 3) / 4;
+        for (uint64_t g0 = 0; g0 < groups; g0 += kEnsThreads) ai.push_back(make_uint2(j, (uint32_t)g0));
     }
+    e->n_agent_items = (uint32_t)ai.size();
     int rc = SLIME_OK;
     cudaError_t ce = cudaSuccess;
     do {
@@ -554,10 +497,13 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         }
         if (ce != cudaSuccess) break;
         if ((ce = dev_alloc((void**)&e->d_cols, k * sizeof(DevColony))) != cudaSuccess) break;
-        if ((ce = dev_alloc((void**)&e->d_agent_items, k * sizeof(uint32_t))) != cudaSuccess) break;
-        e->flow_bytes = sizeof(FlowState) + k * sizeof(unsigned int);
-        if ((ce = dev_alloc((void**)&e->d_flow, e->flow_bytes)) != cudaSuccess) break;
-        ce = cudaMemset(e->d_flow, 0, e->flow_bytes);
+        if ((ce = dev_alloc((void**)&e->d_agent_items, (ai.size() ? ai.size() : 1) * sizeof(uint2))) != cudaSuccess) break;
+        if (ai.size() &&
+            (ce = cudaMemcpy(e->d_agent_items, ai.data(), ai.size() * sizeof(uint2), cudaMemcpyHostToDevice)) !=
+                cudaSuccess)
+            break;
+        if ((ce = dev_alloc((void**)&e->d_bar, sizeof(GridBarrier))) != cudaSuccess) break;
+        ce = cudaMemset(e->d_bar, 0, sizeof(GridBarrier));
     } while (0);
     if (ce != cudaSuccess) rc = cuda_error(e->err, ce, "creating the ensemble");
     for (uint32_t j = 0; rc == SLIME_OK && j < k; j++) {
@@ -566,7 +512,7 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         if (ie != cudaSuccess) rc = cuda_error(e->err, ie, "initialising agent ids");
     }
     if (rc == SLIME_OK) rc = upload_cols(e);
-    if (rc == SLIME_OK) rc = build_items(e);
+    if (rc == SLIME_OK) rc = build_strip_items(e);
     if (rc == SLIME_OK) rc = size_grid(e);
     if (rc != SLIME_OK) {
         *status = rc;
@@ -583,7 +529,7 @@ void slime_ensemble_destroy(slime_ensemble* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     ens_invalidate(e);
     void* ptrs[] = {e->agent_block, e->ids, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->d_cols,
-                    e->d_items, e->d_agent_items, e->d_flow, e->staging, e->reorder.buf};
+                    e->d_agent_items, e->d_strip_items, e->d_bar, e->staging, e->reorder.buf};
     for (void* p : ptrs)
         if (p) dev_free(p);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -607,9 +553,7 @@ int slime_ensemble_set_params(slime_ensemble* e, uint32_t j, const SlimeParams* 
     c.params.width = c.W;
     c.params.height = c.H;
     c.dev = d;
-    int urc = upload_cols(e);
-    ens_invalidate(e); // the parameter blocks are baked into the captured launches
-    return urc;
+    return upload_cols(e); // the colony table is read by the kernel: graphs stay valid
 }
 
 int ensure_staging(slime_ensemble* e, size_t bytes) {
@@ -703,7 +647,7 @@ int slime_ensemble_sync(slime_ensemble* e) {
     if (!e) return SLIME_ERR_INVALID_ARGUMENT;
     cudaSetDevice(e->device);
     ECK(cudaStreamSynchronize(e->stream), "synchronising");
-    return check_flow(e);
+    return check_barrier(e);
 }
 
 int slime_ensemble_get_stream(slime_ensemble* e, void** stream) {
@@ -754,7 +698,7 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
         for (int bo : bps_opts) {
             e->rows = ro;
             e->blocks_per_sm = bo;
-            if ((rc = build_items(e)) != SLIME_OK || (rc = size_grid(e)) != SLIME_OK) break;
+            if ((rc = build_strip_items(e)) != SLIME_OK || (rc = size_grid(e)) != SLIME_OK) break;
             run_ens_steps(e, 1); // warm-up
             cudaEventRecord(e0, e->stream);
             run_ens_steps(e, reps);
@@ -762,7 +706,7 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
             cudaEventSynchronize(e1);
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
-            if ((rc = check_flow(e)) != SLIME_OK) break;
+            if ((rc = check_barrier(e)) != SLIME_OK) break;
             if (ms < best) {
                 best = ms;
                 best_rows = ro;
@@ -788,7 +732,7 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     e->rows = best_rows;
     e->blocks_per_sm = best_bps;
     ens_invalidate(e);
-    if (rc == SLIME_OK) rc = build_items(e);
+    if (rc == SLIME_OK) rc = build_strip_items(e);
     if (rc == SLIME_OK) rc = size_grid(e);
     return rc;
 }
@@ -797,21 +741,20 @@ int slime_ensemble_selftest_barrier_timeout(slime_ensemble* e) {
     if (!e) return SLIME_ERR_INVALID_ARGUMENT;
     cudaSetDevice(e->device);
     ECK(cudaStreamSynchronize(e->stream), "self-test");
-    int* outcome = nullptr;
-    ECK(dev_alloc((void**)&outcome, sizeof(int)), "self-test");
-    cudaMemsetAsync(outcome, 0, sizeof(int), e->stream);
-    cudaMemsetAsync(e->d_flow, 0, e->flow_bytes, e->stream);
-    // waits for pad[0], which nothing increments; about 0.1 s at the GB300's clock
-    wait_timeout_kernel<<<1, 32, 0, e->stream>>>(&e->d_flow->pad[0], 200000000ll, &e->d_flow->error, outcome);
+    int* flag = nullptr;
+    ECK(dev_alloc((void**)&flag, sizeof(int)), "self-test");
+    cudaMemsetAsync(flag, 0, sizeof(int), e->stream);
+    // about 0.1 s at the GB300's clock
+    barrier_timeout_kernel<<<1, 32, 0, e->stream>>>(e->d_bar, 200000000ll, flag);
     cudaError_t le = cudaGetLastError();
     int after = 0;
-    if (le == cudaSuccess) le = cudaMemcpyAsync(&after, outcome, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
+    if (le == cudaSuccess) le = cudaMemcpyAsync(&after, flag, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
     if (le == cudaSuccess) le = cudaStreamSynchronize(e->stream);
-    dev_free(outcome);
+    dev_free(flag);
     if (le != cudaSuccess) return cuda_error(e->err, le, "self-test");
-    int rc = check_flow(e); // reads and clears the error flag
+    int rc = check_barrier(e); // reads and clears the error flag, resets the barrier
     if (after != 2 || rc != SLIME_ERR_DEVICE_TIMEOUT)
-        return ens_fail(e, SLIME_ERR_STATE, "the bounded wait did not time out as expected");
+        return ens_fail(e, SLIME_ERR_STATE, "the bounded barrier did not time out as expected");
     return SLIME_ERR_DEVICE_TIMEOUT;
 }
 
