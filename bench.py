@@ -53,6 +53,20 @@ def metric_name(cfg_name):
     return f"agent-steps/s (plain step, {n:,} agents on {W}x{H})"
 
 
+def agents_kernel_name(shape):
+    """Kernel of agent-shape table entry `shape` (agents.cu): 9-11, 13 and 14
+    are the persistent kernel (13 and 14 sample through the trail texture)."""
+    return "agents_persistent_kernel" if shape in (9, 10, 11, 13, 14) else "agents_kernel"
+
+
+def trail_kernel_name(tile, blur_mode):
+    """Kernel of trail-tile table entry `tile` (trail.cu): 7-9 stream rows,
+    0-6 are shared-memory tiles of the box or Gaussian kernel."""
+    if tile >= 7:
+        return "trail_stream_kernel"
+    return "trail_gauss_kernel" if blur_mode == 1 else "trail_box3_kernel"
+
+
 def make_params(W, H, speed_lo, speed_hi, dist):
     import slime_gb300 as sg
     p = sg.SlimeParams()
@@ -258,6 +272,14 @@ def run_ensemble(args):
     b.record(st)
     sim.sync()
     plain_cells = W * H * 50 / (a.elapsed_time(b) / 1e3)
+    # per-agent and per-cell cost of the plain path (direct launches), to
+    # compare the ensemble at equal work: its colonies average ~2 agents per
+    # cell against 1 in the plain workload, so per-cell rates alone favour
+    # the plain path
+    pa_ms, pt_ms, _ = sim.profile_steps(50)
+    t_agent = pa_ms / 50 / n
+    t_cell = pt_ms / 50 / (W * H)
+    plain_model_ms = agents_total * t_agent + cells * t_cell
     sim.close()
     line = {
         "metric": "trail cells/s (batched ensemble, 64 colonies, one persistent launch per step)",
@@ -269,6 +291,8 @@ def run_ensemble(args):
         "agent_steps_per_s": ens_agents,
         "sequential_plain_cells_per_s": seq_cells, "ensemble_over_sequential": ens_cells / seq_cells,
         "plain_4096_cells_per_s": plain_cells, "ensemble_over_plain_per_cell": ens_cells / plain_cells,
+        "plain_path_ms_for_this_work": plain_model_ms,
+        "ensemble_over_plain_equal_work": plain_model_ms / (ms / args.steps),
         "gpu_launches": launches, "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -413,6 +437,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reorder-every", type=int, default=200)
     ap.add_argument("--no-l2-persist", action="store_true")
+    ap.add_argument("--trail-tile", type=int, default=0,
+                    help="1 + tile-table index of the trail kernel (0: autotuned)")
+    ap.add_argument("--agent-shape", type=int, default=0,
+                    help="1 + shape-table index of the agent kernel (0: autotuned)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -444,8 +472,10 @@ def main():
     sim = sg.Simulation(W, H, n, params)
     sim.upload_agents(agents)
     sim.set_options(reorder_every=args.reorder_every, reorder_cell_log2=2, graph_chunk=50,
-                    l2_persist=0 if args.no_l2_persist else 1)
-    sim.autotune(5)
+                    l2_persist=0 if args.no_l2_persist else 1,
+                    trail_tile=args.trail_tile, agent_shape=args.agent_shape)
+    if not (args.trail_tile and args.agent_shape):
+        sim.autotune(5)
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
     tuned = sim.info()
 
@@ -484,10 +514,10 @@ def main():
     peak, peak_kind = load_peaks()
     bytes_agents = 32.0 * n          # agent state read + write
     bytes_trail = 8.0 * W * H        # trail read + write
-    k_agents = {"name": "agents_kernel", "ms": t_agents, "bytes": bytes_agents,
-                "gbs": bytes_agents / (t_agents * 1e-3) / 1e9}
-    k_trail = {"name": "trail_gauss_kernel", "ms": t_trail, "bytes": bytes_trail,
-               "gbs": bytes_trail / (t_trail * 1e-3) / 1e9}
+    k_agents = {"name": agents_kernel_name(tuned.agent_shape), "ms": t_agents,
+                "bytes": bytes_agents, "gbs": bytes_agents / (t_agents * 1e-3) / 1e9}
+    k_trail = {"name": trail_kernel_name(tuned.trail_tile, int(params.blur_mode)), "ms": t_trail,
+               "bytes": bytes_trail, "gbs": bytes_trail / (t_trail * 1e-3) / 1e9}
     dom = k_agents if t_agents >= t_trail else k_trail
     traffic = None
     try:
@@ -543,7 +573,7 @@ def main():
                        "parallelism": f"replicas x{ws}"},
             "cells_per_s": cells, "pct_roofline_step": pct_roofline,
             "tuned": {"trail_tile": tuned.trail_tile, "agent_shape": tuned.agent_shape,
-                      "l2_persist_bytes": tuned.l2_persist_bytes},
+                      "trail_texture": tuned.trail_texture, "l2_persist_bytes": tuned.l2_persist_bytes},
             "kernels": {"agents": k_agents, "trail": k_trail, "other_ms_per_step": other_ms / kern_steps},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
             "cpu_baseline": cpu,

@@ -9,6 +9,9 @@ nearest binary32 value, so the header carries no number of unknown origin:
   * SLM_PIO2_{1,2,3}: pi/2 split into three binary32 parts for the
     Cody-Waite reduction of small arguments.
   * SLM_S*, SLM_C*: Taylor coefficients (-1)^k / (2k+1)! and (-1)^k / (2k)!.
+  * SLM_PH_WIN_INIT: bits 19..146 of the word stream above (bit 0 = the most
+    significant bit of the zero word), the only bits of 2/pi the Payne-Hanek
+    window reads for 4096 <= |x| < 2^28.
 
 Run `python include/gen_slime_math_constants.py` to print the C block; the
 CPU test suite re-runs it and compares against the header.
@@ -79,6 +82,12 @@ def c_block():
     w = words_two_over_pi()
     lines.append("#define SLM_TWO_OVER_PI_NWORDS %d" % len(w))
     lines.append("#define SLM_TWO_OVER_PI_INIT { " + ", ".join("0x%08xu" % x for x in w) + " }")
+    stream = 0
+    for x in w:
+        stream = (stream << 32) | x
+    nbits = 32 * len(w)
+    win = [(stream >> (nbits - (19 + 32 * i) - 32)) & 0xFFFFFFFF for i in range(4)]
+    lines.append("#define SLM_PH_WIN_INIT { " + ", ".join("0x%08xu" % x for x in win) + " }")
     lines.append("/* END GENERATED CONSTANTS */")
     return "\n".join(lines)
 

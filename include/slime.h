@@ -133,7 +133,7 @@ typedef struct SlimeInfo {
     uint32_t trail_tile;      /* tile-table index in use */
     uint32_t reordered;       /* 1 if device agent order differs from id order */
     uint32_t agent_shape;     /* agent-kernel shape index in use */
-    uint32_t reserved;
+    uint32_t trail_texture;   /* 1 if the trail buffers have gather textures (texture agent shapes usable) */
     uint64_t l2_persist_bytes; /* persisting-L2 carve-out granted for the trail (0 = none) */
 } SlimeInfo;
 

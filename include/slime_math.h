@@ -22,6 +22,8 @@
  *       * otherwise: Payne-Hanek reduction (M. Payne and R. Hanek, "Radian
  *         reduction for trigonometric functions", SIGNUM Newsletter 18(1),
  *         1983) with a 96-bit window of 2/pi and 32x32->64 integer products;
+ *         below 2^28 the window comes from four fixed words of 2/pi by funnel
+ *         shifts instead of table reads (same bits, fewer instructions);
  *       * the reduced argument |r| <= pi/4 is fed to the Taylor polynomials of
  *         sin (to r^9) and cos (to r^10) in Horner form.
  *     The accuracy is a few ulp; what matters for parity is that the host and
@@ -58,6 +60,7 @@
 #define SLM_C5 (-0x1.27e4fc0000000p-22f)
 #define SLM_TWO_OVER_PI_NWORDS 10
 #define SLM_TWO_OVER_PI_INIT { 0x00000000u, 0xa2f9836eu, 0x4e441529u, 0xfc2757d1u, 0xf534ddc0u, 0xdb629599u, 0x3c439041u, 0xfe5163abu, 0xdebbc561u, 0xb7246e3au }
+#define SLM_PH_WIN_INIT { 0x000517ccu, 0x1b727220u, 0xa94fe13au, 0xbe8fa9a6u }
 /* END GENERATED CONSTANTS */
 
 /* Word 0 is zero: the bits of 2/pi "before" the binary point.  Word i >= 1
@@ -195,8 +198,7 @@ SLM_FN int32_t slm_f2i(float x) {
 SLM_FN float slm_i2f(int32_t i) { return (float)i; }
 
 /* ---------------------------------------------------------- sin and cos */
-/* Reduce x to r in about [-pi/4, pi/4] and quadrant q in 0..3 with
- * x = (4k + q) * pi/2 + r. */
+/* Leading zero bits of a nonzero 64-bit value. */
 SLM_FN int slm_clz64(uint64_t a) {
 #if defined(__CUDA_ARCH__)
     return __clzll((long long)a);
@@ -205,47 +207,21 @@ SLM_FN int slm_clz64(uint64_t a) {
 #endif
 }
 
-/* Reduce x to r in about [-pi/4, pi/4] and quadrant q in 0..3 with
- * x = (4k + q) * pi/2 + r. */
-SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
-    if (slm_abs(x) < 4096.0f) {
-        /* Cody-Waite.  j = rint(x * 2/pi) by adding and removing 1.5 * 2^23
-         * (exact round-to-nearest-even for |j| < 2^22); the low bits of the
-         * biased sum are j mod 4.  SLM_PIO2_1 has its last bit at 2^-23, so
-         * the first fma is exact for every |x| < 4096; the two later parts
-         * restore the lost bits. */
-        float biased = slm_add(slm_mul(x, SLM_TWO_OVER_PI_F), 12582912.0f);
-        float j = slm_sub(biased, 12582912.0f);
-        float r = slm_fma(-j, SLM_PIO2_1, x);
-        r = slm_fma(-j, SLM_PIO2_2, r);
-        r = slm_fma(-j, SLM_PIO2_3, r);
-        *r_out = r;
-        *q_out = (int)(slm_f2u_bits(biased) & 3u);
-        return;
-    }
-    uint32_t ix = slm_f2u_bits(x);
-    uint32_t E = (ix >> 23) & 0xffu;
-    if (E == 0xffu) { /* inf or NaN */
-        *r_out = slm_sub(x, x);
-        *q_out = 0;
-        return;
-    }
-    /* |x| = m * 2^e with 2^23 <= m < 2^24 and e >= -11. */
-    uint32_t m = (ix & 0x7fffffu) | 0x800000u;
-    int e = (int)E - 150;
-    /* Bits of 2/pi with index <= s = e - 2 contribute multiples of 4 to
-     * |x| * 2/pi and are dropped; take the 96 bits s+1 .. s+96. */
-    int u = e - 2 + 32; /* table position of bit s, >= 19 */
+/* (hi:lo) << d, upper 32 bits, for 0 <= d <= 31. */
+SLM_FN uint32_t slm_funnel_l(uint32_t lo, uint32_t hi, int d) {
 #if defined(__CUDA_ARCH__)
-    const uint32_t* T = slm_two_over_pi_dev;
+    return __funnelshift_l(lo, hi, (unsigned)d);
 #else
-    const uint32_t* T = slm_two_over_pi_host;
+    return d == 0 ? hi : ((hi << d) | (lo >> (32 - d)));
 #endif
-    int wi = u >> 5;
-    int sh = u & 31;
-    uint32_t w0 = (uint32_t)(((((uint64_t)T[wi]) << 32) | T[wi + 1]) >> (32 - sh));
-    uint32_t w1 = (uint32_t)(((((uint64_t)T[wi + 1]) << 32) | T[wi + 2]) >> (32 - sh));
-    uint32_t w2 = (uint32_t)(((((uint64_t)T[wi + 2]) << 32) | T[wi + 3]) >> (32 - sh));
+}
+
+/* Second half of the Payne-Hanek reduction: from the mantissa m of |x|
+ * (2^23 <= m < 2^24), the 96 bits w0:w1:w2 of 2/pi that follow the bits
+ * dropped as multiples of 4, and the sign of x, the reduced argument and the
+ * quadrant. */
+SLM_FN void slm_ph_finish(uint32_t m, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t sign, float* r_out,
+                          int* q_out) {
     /* Q = m * (w0:w1:w2), a 120-bit integer; |x| * 2/pi = Q * 2^-94 (mod 4). */
     uint64_t p2 = (uint64_t)m * w2;
     uint64_t p1 = (uint64_t)m * w1;
@@ -275,12 +251,82 @@ SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
         r = slm_fma(rh, SLM_PIO2_1, slm_fma(rh, SLM_PIO2_2, slm_mul(rl, SLM_PIO2_1)));
         if (neg) r = -r;
     }
-    if (ix >> 31) {
+    if (sign) {
         r = -r;
         q = (4u - q) & 3u;
     }
     *r_out = r;
     *q_out = (int)q;
+}
+
+/* Payne-Hanek for finite |x| >= 4096, window read from the table of 2/pi. */
+SLM_FN void slm_reduce_pio2_ph(float x, float* r_out, int* q_out) {
+    uint32_t ix = slm_f2u_bits(x);
+    uint32_t E = (ix >> 23) & 0xffu;
+    /* |x| = m * 2^e with 2^23 <= m < 2^24 and e >= -11. */
+    uint32_t m = (ix & 0x7fffffu) | 0x800000u;
+    int e = (int)E - 150;
+    /* Bits of 2/pi with index <= s = e - 2 contribute multiples of 4 to
+     * |x| * 2/pi and are dropped; take the 96 bits s+1 .. s+96. */
+    int u = e - 2 + 32; /* table position of bit s, >= 19 */
+#if defined(__CUDA_ARCH__)
+    const uint32_t* T = slm_two_over_pi_dev;
+#else
+    const uint32_t* T = slm_two_over_pi_host;
+#endif
+    int wi = u >> 5;
+    int sh = u & 31;
+    uint32_t w0 = (uint32_t)(((((uint64_t)T[wi]) << 32) | T[wi + 1]) >> (32 - sh));
+    uint32_t w1 = (uint32_t)(((((uint64_t)T[wi + 1]) << 32) | T[wi + 2]) >> (32 - sh));
+    uint32_t w2 = (uint32_t)(((((uint64_t)T[wi + 2]) << 32) | T[wi + 3]) >> (32 - sh));
+    slm_ph_finish(m, w0, w1, w2, ix >> 31, r_out, q_out);
+}
+
+/* The same for 4096 <= |x| < 2^28 (biased exponent 139..154): there the
+ * window starts at table position u = e + 30 in [19, 34], inside the fixed
+ * 128 bits 19..146 of the table (SLM_PH_WIN_INIT), and each window word is one
+ * funnel shift of two of them by u - 19.  Equal to slm_reduce_pio2_ph bit for
+ * bit on that range (the oracle's self-test compares all 2^28 inputs). */
+SLM_FN void slm_reduce_pio2_win(float x, float* r_out, int* q_out) {
+    const uint32_t K[4] = SLM_PH_WIN_INIT;
+    uint32_t ix = slm_f2u_bits(x);
+    uint32_t E = (ix >> 23) & 0xffu;
+    uint32_t m = (ix & 0x7fffffu) | 0x800000u;
+    int d = (int)E - 139;
+    uint32_t w0 = slm_funnel_l(K[1], K[0], d);
+    uint32_t w1 = slm_funnel_l(K[2], K[1], d);
+    uint32_t w2 = slm_funnel_l(K[3], K[2], d);
+    slm_ph_finish(m, w0, w1, w2, ix >> 31, r_out, q_out);
+}
+
+/* Reduce x to r in about [-pi/4, pi/4] and quadrant q in 0..3 with
+ * x = (4k + q) * pi/2 + r. */
+SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
+    if (slm_abs(x) < 4096.0f) {
+        /* Cody-Waite.  j = rint(x * 2/pi) by adding and removing 1.5 * 2^23
+         * (exact round-to-nearest-even for |j| < 2^22); the low bits of the
+         * biased sum are j mod 4.  SLM_PIO2_1 has its last bit at 2^-23, so
+         * the first fma is exact for every |x| < 4096; the two later parts
+         * restore the lost bits. */
+        float biased = slm_add(slm_mul(x, SLM_TWO_OVER_PI_F), 12582912.0f);
+        float j = slm_sub(biased, 12582912.0f);
+        float r = slm_fma(-j, SLM_PIO2_1, x);
+        r = slm_fma(-j, SLM_PIO2_2, r);
+        r = slm_fma(-j, SLM_PIO2_3, r);
+        *r_out = r;
+        *q_out = (int)(slm_f2u_bits(biased) & 3u);
+        return;
+    }
+    uint32_t E = (slm_f2u_bits(x) >> 23) & 0xffu;
+    if (E == 0xffu) { /* inf or NaN */
+        *r_out = slm_sub(x, x);
+        *q_out = 0;
+        return;
+    }
+    if (E <= 154u)
+        slm_reduce_pio2_win(x, r_out, q_out);
+    else
+        slm_reduce_pio2_ph(x, r_out, q_out);
 }
 
 SLM_FN void slm_sincos(float x, float* s_out, float* c_out) {

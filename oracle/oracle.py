@@ -50,6 +50,8 @@ def lib():
         L.oracle_colorize.restype = None
         L.oracle_num_threads.restype = C.c_int
         L.oracle_sincos.argtypes = [f32, C.c_uint64, f32, f32]
+        L.oracle_ph_window_mismatches.argtypes = [C.c_uint32, C.c_uint32]
+        L.oracle_ph_window_mismatches.restype = C.c_uint64
         L.oracle_jitter_hash.argtypes = [C.POINTER(C.c_int32), f32, f32, C.c_uint64, f32]
         L.oracle_uniform01.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, f32]
         L.oracle_gauss_weights.argtypes = [C.c_float, C.c_float, f32]
@@ -134,6 +136,12 @@ def colorize(W, H, trail, lut768, tw, th):
     out = np.empty((th, tw, 4), np.uint8)
     lib().oracle_colorize(W, H, _p(tr, C.c_float), _p(lut, C.c_uint8), tw, th, _p(out, C.c_uint8))
     return out
+
+
+def ph_window_mismatches(e_lo=139, e_hi=154):
+    """Inputs with biased exponent e_lo..e_hi on which the fixed-window and the
+    table-driven Payne-Hanek reductions disagree (0 expected)."""
+    return int(lib().oracle_ph_window_mismatches(e_lo, e_hi))
 
 
 def sincos(x):

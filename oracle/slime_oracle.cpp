@@ -544,6 +544,26 @@ void oracle_jitter_hash(const int32_t* index, const float* x, const float* y, ui
 void oracle_uniform01(uint64_t seed, uint64_t n, uint32_t field, float* out) {
     for (uint64_t i = 0; i < n; i++) out[i] = slm_uniform01(seed, i, field);
 }
+/* Number of binary32 inputs with biased exponent in [e_lo, e_hi] (both signs)
+ * on which the fixed-window Payne-Hanek reduction differs from the table one
+ * in the reduced argument's bits or the quadrant; e_lo >= 139, e_hi <= 154. */
+uint64_t oracle_ph_window_mismatches(uint32_t e_lo, uint32_t e_hi) {
+    if (e_lo < 139 || e_hi > 154 || e_lo > e_hi) return ~0ull;
+    const int64_t per_sign = (int64_t)(e_hi - e_lo + 1) << 23;
+    uint64_t bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+    for (int64_t i = 0; i < 2 * per_sign; i++) {
+        uint32_t sign = i >= per_sign ? 1u : 0u;
+        uint32_t rem = (uint32_t)(i - (sign ? per_sign : 0));
+        uint32_t bits = (sign << 31) | ((e_lo + (rem >> 23)) << 23) | (rem & 0x7fffffu);
+        float x = slm_u2f_bits(bits), r1, r2;
+        int q1, q2;
+        slm_reduce_pio2_ph(x, &r1, &q1);
+        slm_reduce_pio2_win(x, &r2, &q2);
+        bad += (slm_f2u_bits(r1) != slm_f2u_bits(r2) || q1 != q2) ? 1u : 0u;
+    }
+    return bad;
+}
 int oracle_gauss_weights(float radius, float sigma, float* w) {
     int R = slm_gauss_radius(radius, SLIME_MAX_BLUR_RADIUS);
     if (slm_gauss_weights(R, sigma, w) != 0) return -1;

@@ -29,19 +29,54 @@ __device__ __forceinline__ float sample_trail(const float* __restrict__ trail, i
     return ok ? slm_mix(v0, v1, dy) : 0.0f;
 }
 
+// The same sampler through the texture unit: one four-texel gather returns
+// the 2x2 footprint (raw texels, no filtering), so the interpolation below is
+// the shader's arithmetic on the same four values.  The texture is the trail
+// buffer itself (pitch-linear binary32, point filtering, clamped, unnormalised
+// coordinates); gathering at (x0 + 1, y0 + 1) selects texels x0..x0+1,
+// y0..y0+1, returned as w = (x0, y0), z = (x0+1, y0), x = (x0, y0+1),
+// y = (x0+1, y0+1).  An out-of-grid sample gathers at (1, 1) (always inside a
+// trail of at least 2x2) and is discarded.
+__device__ __forceinline__ float sample_trail_tex(cudaTextureObject_t tex, int W, int H, float px, float py) {
+    float fx = floorf(px), fy = floorf(py);
+    int x0 = slm_f2i(fx);
+    int y0 = slm_f2i(fy);
+    bool ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
+    float dx = slm_sub(px, fx);
+    float dy = slm_sub(py, fy);
+    float u = (float)(ok ? x0 + 1 : 1);
+    float v = (float)(ok ? y0 + 1 : 1);
+    float4 g = tex2Dgather<float4>(tex, u, v, 0);
+    float v0 = slm_mix(g.w, g.z, dx);
+    float v1 = slm_mix(g.x, g.y, dx);
+    return ok ? slm_mix(v0, v1, dy) : 0.0f;
+}
+
+// Trail readers for agent_step: a padded global buffer or a texture over it.
+struct TrailPtr {
+    const float* __restrict__ t;
+    __device__ __forceinline__ float operator()(int W, int H, float px, float py) const {
+        return sample_trail(t, W, H, px, py);
+    }
+};
+struct TrailTex {
+    cudaTextureObject_t t;
+    __device__ __forceinline__ float operator()(int W, int H, float px, float py) const {
+        return sample_trail_tex(t, W, H, px, py);
+    }
+};
+
 // One agent, compute.wgsl:65-144.  Returns the deposit cell or -1.
+template <class Trail>
 __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,
-                                          int32_t index, const float* __restrict__ trail) {
+                                          int32_t index, const Trail& trail) {
     speed = slm_clamp(speed, p.speed_min, p.speed_max);
 
     float sl, cl, sr, cr, sc, cc;
     slm_sensor_dirs(angle, p.sensor_sin, p.sensor_cos, &cl, &sl, &cc, &sc, &cr, &sr);
-    float left = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)),
-                              slm_add(y, slm_mul(p.sensor_dist, sl)));
-    float right = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)),
-                               slm_add(y, slm_mul(p.sensor_dist, sr)));
-    float center = sample_trail(trail, p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)),
-                                slm_add(y, slm_mul(p.sensor_dist, sc)));
+    float left = trail(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)), slm_add(y, slm_mul(p.sensor_dist, sl)));
+    float right = trail(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)), slm_add(y, slm_mul(p.sensor_dist, sr)));
+    float center = trail(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)), slm_add(y, slm_mul(p.sensor_dist, sc)));
 
     // compute.wgsl:98-112: keep straight, or turn toward target = angle -/+ TAU
     bool turn_left = !(center > left && center > right) && (left > right);
@@ -67,6 +102,11 @@ __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y
     int dy = slm_f2i(y);
     if ((unsigned)dx < (unsigned)p.W && (unsigned)dy < (unsigned)p.H) return dy * p.W + dx;
     return -1;
+}
+
+__device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,
+                                          int32_t index, const float* __restrict__ trail) {
+    return agent_step(p, x, y, angle, speed, index, TrailPtr{trail});
 }
 
 } // namespace slime

@@ -65,11 +65,12 @@ struct Lanes<4> {
 
 // A thread moves APT consecutive slots with one vector load/store per field.
 // MINB > 0 asks the compiler to fit MINB blocks per SM (caps registers).
-template <int APT, int BS, int MINB, bool kIds>
+// Trail is the reader of the sensed trail (TrailPtr or TrailTex).
+template <int APT, int BS, int MINB, bool kIds, class Trail>
 __global__ void __launch_bounds__(BS, MINB) agents_kernel(const __grid_constant__ DevParams p, float* __restrict__ X,
                                                     float* __restrict__ Y, float* __restrict__ TH,
                                                     float* __restrict__ V, const uint32_t* __restrict__ ids,
-                                                    const float* __restrict__ trail, uint32_t* __restrict__ counts,
+                                                    const Trail trail, uint32_t* __restrict__ counts,
                                                     uint32_t n_groups, uint64_t n) {
     const uint32_t g = blockIdx.x * BS + threadIdx.x;
     if (g >= n_groups) return;
@@ -164,11 +165,11 @@ __global__ void scale_positions_kernel(float* __restrict__ x, float* __restrict_
 // Persistent variant: a grid sized to the resident capacity walks the groups
 // with a stride, loading the next group's state while the current one is
 // computed, so the stream of agent state does not wait on DRAM latency.
-template <int APT, int BS, int MINB, bool kIds>
+template <int APT, int BS, int MINB, bool kIds, class Trail>
 __global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
     const __grid_constant__ DevParams p, float* __restrict__ X, float* __restrict__ Y, float* __restrict__ TH,
-    float* __restrict__ V, const uint32_t* __restrict__ ids, const float* __restrict__ trail,
-    uint32_t* __restrict__ counts, uint32_t n_groups, uint64_t n) {
+    float* __restrict__ V, const uint32_t* __restrict__ ids, const Trail trail, uint32_t* __restrict__ counts,
+    uint32_t n_groups, uint64_t n) {
     const uint32_t stride = gridDim.x * BS;
     uint32_t g = blockIdx.x * BS + threadIdx.x;
     if (g >= n_groups) return;
@@ -227,8 +228,8 @@ __global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
     }
 }
 
-template <int APT, int BS, int MINB>
-cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
+template <int APT, int BS, int MINB, class Trail>
+cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
                                      cudaStream_t s, const cudaAccessPolicyWindow* win) {
     static int per_sm[2] = {0, 0};
     static int sms = 0;
@@ -238,11 +239,11 @@ cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, con
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (a.ids)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k], agents_persistent_kernel<APT, BS, MINB, true>, BS,
-                                                          0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k],
+                                                          agents_persistent_kernel<APT, BS, MINB, true, Trail>, BS, 0);
         else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k], agents_persistent_kernel<APT, BS, MINB, false>,
-                                                          BS, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k],
+                                                          agents_persistent_kernel<APT, BS, MINB, false, Trail>, BS, 0);
         if (per_sm[k] < 1) per_sm[k] = 1;
         if (sms < 1) sms = 1;
     }
@@ -251,52 +252,109 @@ cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, con
     unsigned need = blocks_for(n_groups, BS);
     dim3 grid(want < need ? want : need);
     if (a.ids)
-        return launch_k(agents_persistent_kernel<APT, BS, MINB, true>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th,
-                        a.v, (const uint32_t*)a.ids, trail, counts, n_groups, a.n);
-    return launch_k(agents_persistent_kernel<APT, BS, MINB, false>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th,
-                    a.v, (const uint32_t*)nullptr, trail, counts, n_groups, a.n);
+        return launch_k(agents_persistent_kernel<APT, BS, MINB, true, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y,
+                        a.th, a.v, (const uint32_t*)a.ids, trail, counts, n_groups, a.n);
+    return launch_k(agents_persistent_kernel<APT, BS, MINB, false, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y,
+                    a.th, a.v, (const uint32_t*)nullptr, trail, counts, n_groups, a.n);
 }
 
-template <int APT, int BS, int MINB>
-cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
+template <int APT, int BS, int MINB, class Trail>
+cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
                                   cudaStream_t s, const cudaAccessPolicyWindow* win) {
     uint32_t n_groups = (uint32_t)((a.n + APT - 1) / APT);
     dim3 grid(blocks_for(n_groups, BS));
     if (a.ids)
-        return launch_k(agents_kernel<APT, BS, MINB, true>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+        return launch_k(agents_kernel<APT, BS, MINB, true, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
                         (const uint32_t*)a.ids, trail, counts, n_groups, a.n);
-    return launch_k(agents_kernel<APT, BS, MINB, false>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+    return launch_k(agents_kernel<APT, BS, MINB, false, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
                     (const uint32_t*)nullptr, trail, counts, n_groups, a.n);
 }
 
 } // namespace
 
 // Agent-kernel shapes: (agents per thread, threads per block, min blocks/SM).
-// Entries 9.. are the persistent, prefetching variant.
+// Entries 9..11 are the persistent, prefetching variant; 12..14 sample the
+// trail through its texture (12 regular, 13 and 14 persistent) and run as
+// their pointer twins (1, 9, 11) when the trail has no texture.
 const AgentShape kAgentShapes[] = {{4, 256, 0}, {2, 256, 0}, {1, 256, 0}, {4, 128, 0}, {1, 128, 0},
-                                   {2, 256, 5}, {2, 256, 6}, {4, 256, 4}, {1, 256, 8},
-                                   {2, 256, 0}, {1, 256, 0}, {2, 128, 0}};
+                                   {2, 256, 5}, {2, 256, 6}, {4, 256, 4}, {1, 256, 8}, {2, 256, 0},
+                                   {1, 256, 0}, {2, 128, 0}, {2, 256, 0}, {2, 256, 0}, {2, 128, 0}};
 
 int agent_shape_count() { return (int)(sizeof(kAgentShapes) / sizeof(kAgentShapes[0])); }
 AgentShape agent_shape(int i) { return kAgentShapes[(i >= 0 && i < agent_shape_count()) ? i : 0]; }
+bool agent_shape_uses_texture(int i) { return i >= 12 && i <= 14; }
 
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
-                          cudaStream_t s, int shape, const cudaAccessPolicyWindow* win) {
+                          cudaStream_t s, int shape, const cudaAccessPolicyWindow* win, cudaTextureObject_t tex) {
     if (a.n == 0) return cudaSuccess;
-    switch (shape) {
-    case 1: return launch_agents_variant<2, 256, 0>(p, a, trail, counts, s, win);
-    case 2: return launch_agents_variant<1, 256, 0>(p, a, trail, counts, s, win);
-    case 3: return launch_agents_variant<4, 128, 0>(p, a, trail, counts, s, win);
-    case 4: return launch_agents_variant<1, 128, 0>(p, a, trail, counts, s, win);
-    case 5: return launch_agents_variant<2, 256, 5>(p, a, trail, counts, s, win);
-    case 6: return launch_agents_variant<2, 256, 6>(p, a, trail, counts, s, win);
-    case 7: return launch_agents_variant<4, 256, 4>(p, a, trail, counts, s, win);
-    case 8: return launch_agents_variant<1, 256, 8>(p, a, trail, counts, s, win);
-    case 9: return launch_agents_persistent<2, 256, 0>(p, a, trail, counts, s, win);
-    case 10: return launch_agents_persistent<1, 256, 0>(p, a, trail, counts, s, win);
-    case 11: return launch_agents_persistent<2, 128, 0>(p, a, trail, counts, s, win);
-    default: return launch_agents_variant<4, 256, 0>(p, a, trail, counts, s, win);
+    const TrailPtr tp{trail};
+    if (agent_shape_uses_texture(shape) && tex) {
+        const TrailTex tt{tex};
+        switch (shape) {
+        case 12: return launch_agents_variant<2, 256, 0>(p, a, tt, counts, s, win);
+        case 13: return launch_agents_persistent<2, 256, 0>(p, a, tt, counts, s, win);
+        default: return launch_agents_persistent<2, 128, 0>(p, a, tt, counts, s, win);
+        }
     }
+    switch (shape) {
+    case 1:
+    case 12: return launch_agents_variant<2, 256, 0>(p, a, tp, counts, s, win);
+    case 2: return launch_agents_variant<1, 256, 0>(p, a, tp, counts, s, win);
+    case 3: return launch_agents_variant<4, 128, 0>(p, a, tp, counts, s, win);
+    case 4: return launch_agents_variant<1, 128, 0>(p, a, tp, counts, s, win);
+    case 5: return launch_agents_variant<2, 256, 5>(p, a, tp, counts, s, win);
+    case 6: return launch_agents_variant<2, 256, 6>(p, a, tp, counts, s, win);
+    case 7: return launch_agents_variant<4, 256, 4>(p, a, tp, counts, s, win);
+    case 8: return launch_agents_variant<1, 256, 8>(p, a, tp, counts, s, win);
+    case 9:
+    case 13: return launch_agents_persistent<2, 256, 0>(p, a, tp, counts, s, win);
+    case 10: return launch_agents_persistent<1, 256, 0>(p, a, tp, counts, s, win);
+    case 11:
+    case 14: return launch_agents_persistent<2, 128, 0>(p, a, tp, counts, s, win);
+    default: return launch_agents_variant<4, 256, 0>(p, a, tp, counts, s, win);
+    }
+}
+
+// A texture over trail buffer `t` (W x H binary32, row pitch 4W bytes) for
+// the gather sampler, or 0 when this device cannot describe the buffer as a
+// pitch-linear texture (row pitch or base not aligned to its texture pitch
+// alignment, or sides beyond its linear-texture limits).
+cudaTextureObject_t make_trail_texture(const float* t, uint32_t W, uint32_t H) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    const size_t pitch = (size_t)W * sizeof(float);
+    const size_t align = prop.texturePitchAlignment ? prop.texturePitchAlignment : 32;
+    if (W < 2 || H < 2 || pitch % align != 0 || (uintptr_t)t % align != 0) return 0;
+    if ((int64_t)W > prop.maxTexture2DLinear[0] || (int64_t)H > prop.maxTexture2DLinear[1] ||
+        (int64_t)pitch > prop.maxTexture2DLinear[2])
+        return 0;
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypePitch2D;
+    rd.res.pitch2D.devPtr = const_cast<float*>(t);
+    rd.res.pitch2D.desc = cudaCreateChannelDesc<float>();
+    rd.res.pitch2D.width = W;
+    rd.res.pitch2D.height = H;
+    rd.res.pitch2D.pitchInBytes = pitch;
+    cudaTextureDesc td = {};
+    td.addressMode[0] = cudaAddressModeClamp;
+    td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    cudaTextureObject_t tex = 0;
+    if (cudaCreateTextureObject(&tex, &rd, &td, nullptr) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return tex;
 }
 
 cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s) {

@@ -173,6 +173,8 @@ void free_agents(slime_ctx* ctx) {
 
 void free_trail(slime_ctx* ctx) {
     for (int i = 0; i < 2; i++) {
+        if (ctx->trail_tex[i]) cudaDestroyTextureObject(ctx->trail_tex[i]);
+        ctx->trail_tex[i] = 0;
         if (ctx->trail[i]) dev_free(ctx->trail[i]);
         if (ctx->counts[i]) dev_free(ctx->counts[i]);
         ctx->trail[i] = nullptr;
@@ -207,6 +209,7 @@ int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
         CK(dev_alloc((void**)&ctx->counts[i], cells * sizeof(uint32_t)), "allocating deposit counts");
         CK(cudaMemsetAsync(ctx->trail[i], 0, (cells + W + 2) * sizeof(float), ctx->stream), "clearing trail");
         CK(cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream), "clearing counts");
+        ctx->trail_tex[i] = make_trail_texture(ctx->trail[i], W, H);
     }
     ctx->cur = 0;
     ctx->last_counts_valid = false;
@@ -297,7 +300,7 @@ cudaError_t enqueue_step(slime_ctx* ctx) {
     bool ha = trail_window(ctx, ctx->trail[cur], &wa);
     bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt);
     cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream,
-                                  ctx->agent_shape, ha ? &wa : nullptr);
+                                  ctx->agent_shape, ha ? &wa : nullptr, ctx->trail_tex[cur]);
     if (e != cudaSuccess) return e;
     e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
                      ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr);
@@ -540,7 +543,7 @@ int slime_get_info(const slime_ctx* ctx, SlimeInfo* out) {
     out->kernel_launches = ctx->launches;
     out->trail_tile = (uint32_t)ctx->tile;
     out->agent_shape = (uint32_t)ctx->agent_shape;
-    out->reserved = 0;
+    out->trail_texture = ctx->trail_tex[0] && ctx->trail_tex[1] ? 1u : 0u;
     out->l2_persist_bytes = ctx->l2_persist_bytes;
     out->reordered = ctx->reordered ? 1u : 0u;
     return SLIME_OK;
@@ -778,7 +781,7 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
         bool ha = trail_window(ctx, ctx->trail[cur], &wa);
         bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt);
         cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream,
-                                      ctx->agent_shape, ha ? &wa : nullptr);
+                                      ctx->agent_shape, ha ? &wa : nullptr, ctx->trail_tex[cur]);
         cudaEventRecord(ev[2], ctx->stream);
         if (e == cudaSuccess)
             e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
@@ -860,11 +863,15 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
             CK(cudaMemcpyAsync(snap, ctx->agent_block, abytes, cudaMemcpyDeviceToDevice, ctx->stream), "snapshot");
             float best_a = 1e30f;
             for (int sh = 0; sh < agent_shape_count(); sh++) {
-                launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, sh);
+                // without a texture the gather shapes repeat their pointer twins
+                if (agent_shape_uses_texture(sh) && !ctx->trail_tex[cur]) continue;
+                launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, sh, nullptr,
+                              ctx->trail_tex[cur]);
                 cudaEventRecord(e0, ctx->stream);
                 for (uint32_t r = 0; r < reps; r++) {
                     cudaMemcpyAsync(ctx->agent_block, snap, abytes, cudaMemcpyDeviceToDevice, ctx->stream);
-                    launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, sh);
+                    launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, sh, nullptr,
+                                  ctx->trail_tex[cur]);
                 }
                 cudaEventRecord(e1, ctx->stream);
                 CK(cudaEventSynchronize(e1), "autotuning");

@@ -72,18 +72,35 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
 
 // --------------------------------------------------------------- device code
 // Deposit fold: t <- clamp(t + dep, 0, 1), k times; stops once an iteration
-// leaves the bits of t unchanged (every later iteration would too).
+// leaves the bits of t unchanged (every later iteration would too).  The
+// first two iterations are straight-line selects (most cells receive 0, 1 or
+// 2 deposits per step); only cells with k >= 3 whose value still moved after
+// two iterations enter the loop.
 __device__ __forceinline__ float fold_deposits(float t, uint32_t k, float dep) {
-    for (uint32_t i = 0; i < k; i++) {
-        float nt = slm_clamp(slm_add(t, dep), 0.0f, 1.0f);
-        if (__float_as_uint(nt) == __float_as_uint(t)) break;
-        t = nt;
+    const float t1 = slm_clamp(slm_add(t, dep), 0.0f, 1.0f);
+    const float t2 = slm_clamp(slm_add(t1, dep), 0.0f, 1.0f);
+    float r = k == 0 ? t : (k == 1 ? t1 : t2);
+    if (k >= 3 && __float_as_uint(t2) != __float_as_uint(t1)) {
+        float u = t2;
+        for (uint32_t i = 2; i < k; i++) {
+            float nu = slm_clamp(slm_add(u, dep), 0.0f, 1.0f);
+            if (__float_as_uint(nu) == __float_as_uint(u)) break;
+            u = nu;
+        }
+        r = u;
     }
-    return t;
+    return r;
 }
 
 __device__ __forceinline__ float apply_decay(const DevParams& p, float v) {
     return p.decay_mode == SLIME_DECAY_MULTIPLY ? slm_mul(v, p.decay) : slm_max(slm_sub(v, p.decay_k), 0.0f);
+}
+// The same with the decay mode fixed at compile time (kMode: a
+// SLIME_DECAY_* value, or -1 to read it from p).
+template <int kMode>
+__device__ __forceinline__ float apply_decay_m(const DevParams& p, float v) {
+    if (kMode < 0) return apply_decay(p, v);
+    return kMode == SLIME_DECAY_MULTIPLY ? slm_mul(v, p.decay) : slm_max(slm_sub(v, p.decay_k), 0.0f);
 }
 
 // Wrap g into [0, n) for g in [-n*k, n*(k+1)); the loops run at most once for

@@ -21,6 +21,7 @@ struct slime_ctx {
     slime::ReorderScratch reorder;
 
     float* trail[2] = {nullptr, nullptr};
+    cudaTextureObject_t trail_tex[2] = {0, 0}; // gather textures over trail[] (0 = none)
     uint32_t* counts[2] = {nullptr, nullptr};
     int cur = 0;
     bool last_counts_valid = false;

@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
     for (uint32_t item = gw; item < n_strip_items; item += warps) {
         const uint4 it = strip_items[item];
         const DevColony& c = cols[it.x];
-        process_strip<R, kGauss, ROWS, true>(c.p, trail_in + c.trail_off, counts_in + c.trail_off,
+        process_strip<R, kGauss, ROWS, true, false>(c.p, trail_in + c.trail_off, counts_in + c.trail_off,
                                              trail_out + c.trail_off, counts_zero + c.trail_off, (int)it.y,
                                              (int)it.z);
     }

@@ -30,9 +30,14 @@ struct AgentShape {
 };
 int agent_shape_count();
 AgentShape agent_shape(int index);
+bool agent_shape_uses_texture(int index);
 // One agent pass (compute.wgsl:57-145): reads trail, adds deposit counts.
+// `tex` is a texture over `trail` (make_trail_texture) for the shapes that
+// sample through it; 0 runs those shapes on the pointer path.
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
-                          cudaStream_t s, int shape = 0, const cudaAccessPolicyWindow* win = nullptr);
+                          cudaStream_t s, int shape = 0, const cudaAccessPolicyWindow* win = nullptr,
+                          cudaTextureObject_t tex = 0);
+cudaTextureObject_t make_trail_texture(const float* trail, uint32_t W, uint32_t H);
 // AoS staging (x, y, angle, speed per agent, id order) <-> SoA slots.
 cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const AgentsSoA& a, float4* aos, cudaStream_t s);

@@ -60,13 +60,13 @@ __device__ __forceinline__ void fetch_row(const DevParams& p, const float* __res
     }
 }
 
-template <int R>
+template <int R, int kDecay>
 __device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch<R>& f, bool left_edge,
                                               bool right_edge, ExtRow<R>& e) {
-    float d[4] = {apply_decay(p, fold_deposits(f.t.x, f.k.x, p.dep)),
-                  apply_decay(p, fold_deposits(f.t.y, f.k.y, p.dep)),
-                  apply_decay(p, fold_deposits(f.t.z, f.k.z, p.dep)),
-                  apply_decay(p, fold_deposits(f.t.w, f.k.w, p.dep))};
+    float d[4] = {apply_decay_m<kDecay>(p, fold_deposits(f.t.x, f.k.x, p.dep)),
+                  apply_decay_m<kDecay>(p, fold_deposits(f.t.y, f.k.y, p.dep)),
+                  apply_decay_m<kDecay>(p, fold_deposits(f.t.z, f.k.z, p.dep)),
+                  apply_decay_m<kDecay>(p, fold_deposits(f.t.w, f.k.w, p.dep))};
 #pragma unroll
     for (int j = 0; j < 4; j++) e.v[R + j] = d[j];
 #pragma unroll
@@ -76,18 +76,22 @@ __device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch
     }
 #pragma unroll
     for (int j = 0; j < R; j++) {
-        float h = apply_decay(p, fold_deposits(f.ht[j], f.hk[j], p.dep));
+        float h = apply_decay_m<kDecay>(p, fold_deposits(f.ht[j], f.hk[j], p.dep));
         if (left_edge) e.v[j] = h;
         if (right_edge) e.v[R + 4 + j] = h;
     }
 }
 
 // One warp processes strip (cw, rs): columns 128*cw .. 128*cw+127, output
-// rows ROWS*rs .. ROWS*rs+ROWS-1.  All 32 lanes must call it together.
-template <int R, bool kGauss, int ROWS, bool kCoherent = false>
-__device__ __forceinline__ void process_strip(const DevParams& p, const float* __restrict__ in,
-                                              const uint32_t* __restrict__ cin, float* __restrict__ out,
-                                              uint32_t* __restrict__ czero, int cw, int rs) {
+// rows ROWS*rs .. ROWS*rs+ROWS-1.  All 32 lanes must call it together.  With
+// kUnrolled the row loop of a short strip is unrolled, so the window of 2R+1
+// rows rotates by renaming registers rather than by copies (at the price of
+// registers: kernels that must stay small, like the ensemble's, keep the loop).
+// kDecay is the decay mode (SLIME_DECAY_*) or -1 to read it from p at run time.
+template <int R, bool kGauss, int ROWS, bool kCoherent, int kDecay, bool kUnrolled>
+__device__ __forceinline__ void process_strip_m(const DevParams& p, const float* __restrict__ in,
+                                                const uint32_t* __restrict__ cin, float* __restrict__ out,
+                                                uint32_t* __restrict__ czero, int cw, int rs) {
     const int lane = threadIdx.x & 31;
     const int W = p.W, H = p.H;
     const int y0 = rs * ROWS;
@@ -109,7 +113,10 @@ __device__ __forceinline__ void process_strip(const DevParams& p, const float* _
     RowFetch<R> fa, fb;
     fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R, H), cl, has_halo, hcol0, fa);
     fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R + 1, H), cl, has_halo, hcol0, fb);
-#pragma unroll 1
+    // short strips unroll completely when asked to; long ones stay rolled
+    // (unrolled, their live ranges exceed the register budget and spill)
+    constexpr int kUnroll = (kUnrolled && NR <= 12) ? NR : 1;
+#pragma unroll kUnroll
     for (int r = 0; r < NR; r++) {
         RowFetch<R> cur = fa;
         fa = fb;
@@ -123,7 +130,7 @@ __device__ __forceinline__ void process_strip(const DevParams& p, const float* _
                 for (int j = 0; j < 4; j++) hwin[q][j] = hwin[q + 1][j];
             }
         }
-        build_ext_row<R>(p, cur, left_edge && active, right_edge, win[NWIN - 1]);
+        build_ext_row<R, kDecay>(p, cur, left_edge && active, right_edge, win[NWIN - 1]);
         if (kGauss) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -160,6 +167,20 @@ __device__ __forceinline__ void process_strip(const DevParams& p, const float* _
         *reinterpret_cast<float4*>(out + off) = make_float4(o[0], o[1], o[2], o[3]);
         if (czero) *reinterpret_cast<uint4*>(czero + off) = make_uint4(0u, 0u, 0u, 0u);
     }
+}
+
+template <int R, bool kGauss, int ROWS, bool kCoherent = false, bool kUnrolled = true>
+__device__ __forceinline__ void process_strip(const DevParams& p, const float* __restrict__ in,
+                                              const uint32_t* __restrict__ cin, float* __restrict__ out,
+                                              uint32_t* __restrict__ czero, int cw, int rs) {
+    // the unrolled form also fixes the decay mode per instance; the rolled one
+    // keeps a single copy of the loop (two would cost registers)
+    if (!kUnrolled)
+        process_strip_m<R, kGauss, ROWS, kCoherent, -1, false>(p, in, cin, out, czero, cw, rs);
+    else if (p.decay_mode == SLIME_DECAY_MULTIPLY)
+        process_strip_m<R, kGauss, ROWS, kCoherent, SLIME_DECAY_MULTIPLY, true>(p, in, cin, out, czero, cw, rs);
+    else
+        process_strip_m<R, kGauss, ROWS, kCoherent, SLIME_DECAY_REF_SUBTRACT, true>(p, in, cin, out, czero, cw, rs);
 }
 
 

@@ -103,7 +103,7 @@ class SlimeInfo(C.Structure):
         ("trail_tile", C.c_uint32),
         ("reordered", C.c_uint32),
         ("agent_shape", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("trail_texture", C.c_uint32),
         ("l2_persist_bytes", C.c_uint64),
     ]
 

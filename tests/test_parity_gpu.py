@@ -120,9 +120,14 @@ def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
         assert_bitexact(sim.download_agents(), ca, "agents")
 
 
-@pytest.mark.parametrize("shape", range(1, 13))
-def test_every_agent_shape_is_bitexact(gpu, shape):
-    W, H = 200, 150
+@pytest.mark.parametrize("shape", range(1, 16))
+@pytest.mark.parametrize("W,H", [(256, 150), (201, 150)])
+def test_every_agent_shape_is_bitexact(gpu, shape, W, H):
+    # 256 wide: the trail has gather textures; 201 wide: its rows are not
+    # aligned for one, and the texture shapes (13..15) run their pointer twins
+    sim0 = make_sim(W, H, 1, config0_params(W, H), agents_uniform(1, W, H, 1.0, 2.0, seed=0),
+                    np.zeros((H, W), np.float32))
+    assert sim0.info().trail_texture == (1 if W == 256 else 0)
     for n in (1, 3, 4097, 20001):
         p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, agent_speed_min=30.0,
                            agent_speed_max=50.0, agent_jitter=0.3)
@@ -152,8 +157,9 @@ def test_autotune_keeps_state(gpu):
     assert_bitexact(a.download_trail(), ct, "trail after autotune")
 
 
-@pytest.mark.parametrize("W,H", [(1, 1), (2, 3), (3, 2), (5, 3), (4, 4), (17, 1), (1, 19)])
-def test_tiny_toroidal_grids(gpu, W, H):
+@pytest.mark.parametrize("shape", [0, 14])
+@pytest.mark.parametrize("W,H", [(1, 1), (2, 3), (3, 2), (5, 3), (4, 4), (17, 1), (1, 19), (8, 2), (16, 3)])
+def test_tiny_toroidal_grids(gpu, W, H, shape):
     n = 64
     for blur_mode, radius in ((0, 1.0), (1, 2.0)):
         p = config0_params(W, H, decay_mode=0, blur_mode=blur_mode, blur_radius=radius,
@@ -162,6 +168,7 @@ def test_tiny_toroidal_grids(gpu, W, H):
         agents = agents_uniform(n, W, H, 30.0, 90.0, seed=6)
         trail = np.random.default_rng(7).random((H, W), dtype=np.float32)
         sim = make_sim(W, H, n, p, agents, trail)
+        sim.set_options(agent_shape=shape)
         sim.step(3)
         ca, ct = agents.copy(), trail.copy()
         oracle.run(p, W, H, ca, ct, 3)
@@ -169,7 +176,8 @@ def test_tiny_toroidal_grids(gpu, W, H):
         assert_bitexact(sim.download_trail(), ct, f"trail {W}x{H}")
 
 
-def test_edge_positions_and_sensor_bounds(gpu):
+@pytest.mark.parametrize("shape", [0, 14])
+def test_edge_positions_and_sensor_bounds(gpu, shape):
     """Agents on the last row/column, at x rounding up to W after the wrap,
     sensors off the grid (the sampler returns 0 there, it does not wrap),
     negative and huge angles."""
@@ -190,12 +198,13 @@ def test_edge_positions_and_sensor_bounds(gpu):
     for smin in (0.5, 0.0):
         p = config0_params(W, H, decay_mode=0, blur_mode=0, agent_sensor_distance=20.0, agent_speed_min=smin,
                            agent_speed_max=100.0, agent_jitter=1.0, agent_turn_speed=0.43)
-        _edge_case(W, H, agents, trail, p)
+        _edge_case(W, H, agents, trail, p, shape)
 
 
-def _edge_case(W, H, agents, trail, p):
+def _edge_case(W, H, agents, trail, p, shape=0):
     n = agents.shape[0]
     sim = make_sim(W, H, n, p, agents, trail)
+    sim.set_options(agent_shape=shape)
     for s in range(5):
         sim.step(1)
     ca, ct = agents.copy(), trail.copy()
