@@ -67,6 +67,36 @@ def trail_kernel_name(tile, blur_mode):
     return "trail_gauss_kernel" if blur_mode == 1 else "trail_box3_kernel"
 
 
+# ncu summaries (profiles/) that hold the DRAM traffic of one launch of a
+# kernel on a workload: the "traffic (read + write) per launch" row.
+TRAFFIC_PROFILES = {
+    ("plain-4096", "agents_persistent_kernel"): "agents_kernel_plain-4096.md",
+    ("plain-4096", "trail_stream_kernel"): "trail_stream_kernel_plain-4096.md",
+}
+
+
+def profiled_traffic(workload, kernel):
+    """dram__bytes_read.sum + dram__bytes_write.sum of one launch, in bytes,
+    from the committed ncu summary of that kernel on that workload, if the
+    summary's capture is of the same kernel; else None."""
+    import re
+    name = TRAFFIC_PROFILES.get((workload, kernel))
+    if not name:
+        return None, None
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(path) as f:
+            text = f.read()
+    except OSError:
+        return None, None
+    if not text.startswith("# " + kernel):
+        return None, None
+    m = re.search(r"traffic \(read \+ write\) per launch \| ([0-9.]+) MB", text)
+    if not m:
+        return None, None
+    return float(m.group(1)) * 1e6, "profiles/" + name
+
+
 def make_params(W, H, speed_lo, speed_hi, dist):
     import slime_gb300 as sg
     p = sg.SlimeParams()
@@ -519,14 +549,10 @@ def main():
     k_trail = {"name": trail_kernel_name(tuned.trail_tile, int(params.blur_mode)), "ms": t_trail,
                "bytes": bytes_trail, "gbs": bytes_trail / (t_trail * 1e-3) / 1e9}
     dom = k_agents if t_agents >= t_trail else k_trail
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic_per_launch.json")) as f:
-            traffic = json.load(f).get(args.config, {}).get(dom["name"])
-    except Exception:
-        traffic = None
+    traffic, traffic_src = profiled_traffic(args.config, dom["name"])
     roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": dom["gbs"], "peak": peak, "unit": "GB/s",
-                "frac": dom["gbs"] / peak, "traffic": traffic, "peak_kind": peak_kind,
+                "frac": dom["gbs"] / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
+                "traffic_source": traffic_src, "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": dom["bytes"], "launch_ms": dom["ms"]}
     step_bytes = bytes_agents + bytes_trail
     pct_roofline = step_bytes / (ms_per_step * 1e-3) / 1e9 / peak
