@@ -100,7 +100,7 @@ __device__ __forceinline__ float apply_decay(const DevParams& p, float v) {
 template <int kMode>
 __device__ __forceinline__ float apply_decay_m(const DevParams& p, float v) {
     if (kMode < 0) return apply_decay(p, v);
-    return kMode == SLIME_DECAY_MULTIPLY ? slm_mul(v, p.decay) : slm_max(slm_sub(v, p.decay_k), 0.0f);
+    return kMode == (int)SLIME_DECAY_MULTIPLY ? slm_mul(v, p.decay) : slm_max(slm_sub(v, p.decay_k), 0.0f);
 }
 
 // Wrap g into [0, n) for g in [-n*k, n*(k+1)); the loops run at most once for

@@ -28,6 +28,10 @@ __device__ __forceinline__ uint32_t spread_bits(uint32_t v) {
     return v;
 }
 
+// Agents that are already nearly in order share keys with their warp
+// neighbours (about 2^(2 cell_log2) per key at one agent per cell), so the
+// histogram and the slot claims are aggregated per warp: the lanes holding
+// one key elect a leader that adds the group's size with a single atomic.
 __global__ void key_hist_kernel(const float* __restrict__ x, const float* __restrict__ y, uint64_t n, int W,
                                 int H, int cl, uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,7 +40,8 @@ __global__ void key_hist_kernel(const float* __restrict__ x, const float* __rest
     int cy = min(max(slm_f2i(y[i]), 0), H - 1) >> cl;
     uint32_t k = spread_bits((uint32_t)cx) | (spread_bits((uint32_t)cy) << 1);
     keys[i] = k;
-    atomicAdd(hist + k, 1u);
+    const unsigned group = __match_any_sync(__activemask(), k);
+    if ((int)(threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(hist + k, (uint32_t)__popc(group));
 }
 
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
@@ -121,7 +126,16 @@ __global__ void scatter_kernel(const float* __restrict__ x, const float* __restr
                                float* __restrict__ tth, float* __restrict__ tv, uint32_t* __restrict__ tid) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t pos = atomicAdd(offsets + keys[i], 1u);
+    const uint32_t k = keys[i];
+    const unsigned active = __activemask();
+    const unsigned group = __match_any_sync(active, k);
+    const int lane = (int)(threadIdx.x & 31);
+    const int leader = __ffs(group) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(offsets + k, (uint32_t)__popc(group));
+    base = __shfl_sync(active, base, leader);
+    // slots of one key are claimed in lane order within the warp
+    const uint32_t pos = base + (uint32_t)__popc(group & ((1u << lane) - 1u));
     tx[pos] = x[i];
     ty[pos] = y[i];
     tth[pos] = th[i];

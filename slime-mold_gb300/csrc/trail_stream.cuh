@@ -178,9 +178,9 @@ __device__ __forceinline__ void process_strip(const DevParams& p, const float* _
     if (!kUnrolled)
         process_strip_m<R, kGauss, ROWS, kCoherent, -1, false>(p, in, cin, out, czero, cw, rs);
     else if (p.decay_mode == SLIME_DECAY_MULTIPLY)
-        process_strip_m<R, kGauss, ROWS, kCoherent, SLIME_DECAY_MULTIPLY, true>(p, in, cin, out, czero, cw, rs);
+        process_strip_m<R, kGauss, ROWS, kCoherent, (int)SLIME_DECAY_MULTIPLY, true>(p, in, cin, out, czero, cw, rs);
     else
-        process_strip_m<R, kGauss, ROWS, kCoherent, SLIME_DECAY_REF_SUBTRACT, true>(p, in, cin, out, czero, cw, rs);
+        process_strip_m<R, kGauss, ROWS, kCoherent, (int)SLIME_DECAY_REF_SUBTRACT, true>(p, in, cin, out, czero, cw, rs);
 }
 
 
