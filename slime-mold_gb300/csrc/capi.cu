@@ -254,27 +254,53 @@ void invalidate_graphs(slime_ctx* ctx) {
     ctx->graphs.clear();
 }
 
-// Size the persisting-L2 carve-out for the trail (the context's limit, gone
-// with the context) and remember the largest window the device accepts.
+// The persisting-L2 carve-out is a limit of the device's context, shared by
+// every simulation on that device in the process.  Each context registers the
+// carve-out it wants; the limit is the largest live request, and persisting
+// lines are released once no context wants any.
+std::mutex g_l2_mutex;
+std::map<int, std::map<const slime_ctx*, size_t>> g_l2_grants; // device -> context -> bytes
+
+void apply_l2_limit(int device) {
+    size_t want = 0;
+    for (const auto& kv : g_l2_grants[device]) want = kv.second > want ? kv.second : want;
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) cudaGetLastError();
+    if (want == 0 && cudaCtxResetPersistingL2Cache() != cudaSuccess) cudaGetLastError();
+}
+
+void release_l2(slime_ctx* ctx) {
+    std::lock_guard<std::mutex> lock(g_l2_mutex);
+    cudaSetDevice(ctx->device);
+    g_l2_grants[ctx->device].erase(ctx);
+    apply_l2_limit(ctx->device);
+    ctx->l2_persist_bytes = 0;
+}
+
+// Size the persisting-L2 carve-out for the trail and remember the largest
+// window the device accepts.  The trail persists only when all of it fits
+// the device's maximum carve-out and one window: a trail larger than that
+// (8192^2 binary32 is 256 MiB) would keep a random part resident at the cost
+// of the L2 left to every other access, which measured slower than no
+// carve-out at all.
 void setup_l2(slime_ctx* ctx) {
+    std::lock_guard<std::mutex> lock(g_l2_mutex);
+    cudaSetDevice(ctx->device);
+    auto& grants = g_l2_grants[ctx->device];
+    grants.erase(ctx);
     ctx->l2_persist_bytes = 0;
     ctx->l2_max_window = 0;
-    if (!ctx->opt.l2_persist) return;
     int max_persist = 0, max_window = 0;
-    if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device) != cudaSuccess ||
-        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device) != cudaSuccess ||
-        max_persist <= 0 || max_window <= 0) {
-        cudaGetLastError();
-        return;
+    const size_t want = (size_t)ctx->W * ctx->H * sizeof(float);
+    if (ctx->opt.l2_persist && !ctx->l2_tuned_off &&
+        cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device) == cudaSuccess &&
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device) == cudaSuccess &&
+        max_persist > 0 && max_window > 0 && want <= (size_t)max_persist && want <= (size_t)max_window) {
+        grants[ctx] = want;
+        ctx->l2_persist_bytes = want;
+        ctx->l2_max_window = (size_t)max_window;
     }
-    size_t want = (size_t)ctx->W * ctx->H * sizeof(float);
-    size_t grant = want < (size_t)max_persist ? want : (size_t)max_persist;
-    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, grant) != cudaSuccess) {
-        cudaGetLastError();
-        return;
-    }
-    ctx->l2_persist_bytes = grant;
-    ctx->l2_max_window = (size_t)max_window;
+    cudaGetLastError();
+    apply_l2_limit(ctx->device);
 }
 
 // The access window for a launch that reads (or writes) trail buffer `t`.
@@ -371,6 +397,70 @@ int do_reorder(slime_ctx* ctx) {
     return SLIME_OK;
 }
 
+// Whether the persisting-L2 window over the trail pays off for this context:
+// `steps` full steps (an even number) with and without it, twice each in
+// alternation, from a snapshot of the agents and the trail that is put back
+// before every trial and at the end.  Without a snapshot buffer nothing
+// changes.
+int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
+    const size_t cells = (size_t)ctx->W * ctx->H;
+    const size_t abytes = 4 * ctx->agents.n_pad * sizeof(float);
+    const size_t tbytes = cells * sizeof(float);
+    char* snap = nullptr;
+    if (dev_alloc((void**)&snap, abytes + tbytes) != cudaSuccess) {
+        cudaGetLastError();
+        return SLIME_OK;
+    }
+    const int cur = ctx->cur;
+    auto restore = [&]() -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(ctx->agent_block, snap, abytes, cudaMemcpyDeviceToDevice, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->trail[cur], snap + abytes, tbytes, cudaMemcpyDeviceToDevice, ctx->stream);
+        for (int i = 0; i < 2 && e == cudaSuccess; i++)
+            e = cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream);
+        ctx->cur = cur;
+        return e;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMemcpyAsync(snap, ctx->agent_block, abytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(snap + abytes, ctx->trail[cur], tbytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float total[2] = {0.0f, 0.0f}; // [0] window on, [1] off
+    for (int round = 0; round < 2 && e == cudaSuccess; round++) {
+        for (int off = 0; off < 2 && e == cudaSuccess; off++) {
+            ctx->l2_tuned_off = off != 0;
+            setup_l2(ctx);
+            if (!off && !ctx->l2_persist_bytes) break; // no carve-out to compare with
+            e = restore();
+            for (int w = 0; w < 2 && e == cudaSuccess; w++) e = enqueue_step(ctx);
+            if (e == cudaSuccess) e = restore();
+            if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+            for (uint32_t i = 0; i < steps && e == cudaSuccess; i++) e = enqueue_step(ctx);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            total[off] += ms;
+            ctx->launches += (steps + 2) * kernels_per_step(ctx);
+        }
+    }
+    const bool measured = e == cudaSuccess && total[0] > 0.0f && total[1] > 0.0f;
+    ctx->l2_tuned_off = measured && total[1] < total[0];
+    setup_l2(ctx);
+    cudaError_t re = restore();
+    if (re == cudaSuccess) re = cudaStreamSynchronize(ctx->stream);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    dev_free(snap);
+    invalidate_graphs(ctx);
+    ctx->last_counts_valid = false;
+    if (e != cudaSuccess) return cuda_error(ctx->err, e, "autotuning the L2 window");
+    if (re != cudaSuccess) return cuda_error(ctx->err, re, "autotuning the L2 window");
+    return SLIME_OK;
+}
+
 int run_steps(slime_ctx* ctx, uint32_t n) {
     int rc;
     while (n > 0) {
@@ -460,6 +550,7 @@ void slime_destroy(slime_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    release_l2(ctx);
     invalidate_graphs(ctx);
     free_adjoint(ctx);
     free_agents(ctx);
@@ -515,6 +606,7 @@ int slime_set_options(slime_ctx* ctx, const SlimeOptions* o) {
     ctx->opt = *o;
     if (ctx->opt.graph_chunk == 0) ctx->opt.graph_chunk = 50;
     if (l2_changed) {
+        ctx->l2_tuned_off = false;
         setup_l2(ctx);
         invalidate_graphs(ctx);
     }
@@ -657,6 +749,7 @@ int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height) {
     ctx->params = np;
     ctx->dev = d;
     ctx->tuned_tile = -1;
+    ctx->l2_tuned_off = false;
     setup_l2(ctx);
     CK(cudaStreamSynchronize(ctx->stream), "resizing");
     return SLIME_OK;
@@ -902,6 +995,12 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
         ctx->tile = tile;
         ctx->agent_shape = shape;
         invalidate_graphs(ctx);
+    }
+    // 3. the persisting-L2 window, with the tile and shape just chosen
+    if (ctx->opt.l2_persist && ctx->agents.n > 0) {
+        ctx->l2_tuned_off = false;
+        setup_l2(ctx);
+        if (ctx->l2_persist_bytes) return tune_l2_window(ctx, 2 * (reps < 5 ? 5 : reps));
     }
     return SLIME_OK;
 }

@@ -37,6 +37,7 @@ struct slime_ctx {
     // Persisting-L2 window over the trail being sensed (0 = off).
     size_t l2_persist_bytes = 0; // carve-out granted to this context
     size_t l2_max_window = 0;    // cudaDevAttrMaxAccessPolicyWindowSize
+    bool l2_tuned_off = false;   // the autotuner measured the steps faster without it
 
     std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs; // (steps, start parity) -> graph
 

@@ -393,3 +393,19 @@ def test_memory_cap_reports_out_of_memory(gpu):
     env = dict(os.environ, SLIME_DEVICE_MEMORY_CAP=str(2 * 1024 * 1024))
     out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
     assert "status -2" in out.stdout and "small ok" in out.stdout, out.stdout + out.stderr
+
+
+def test_l2_carveout_only_for_trails_that_fit(gpu):
+    """The trail persists in L2 only when all of it fits the carve-out; a
+    larger trail, or persistence switched off, reserves nothing."""
+    import slime_gb300 as sg
+    small = sg.Simulation(1024, 1024, 1000, config0_params(1024, 1024))
+    assert small.info().l2_persist_bytes == 1024 * 1024 * 4
+    small.set_options(l2_persist=0)
+    assert small.info().l2_persist_bytes == 0
+    small.set_options(l2_persist=1)
+    assert small.info().l2_persist_bytes == 1024 * 1024 * 4
+    big = sg.Simulation(8192, 8192, 1000, config0_params(8192, 8192))
+    assert big.info().l2_persist_bytes == 0  # 256 MiB: more than any carve-out
+    big.close()
+    small.close()
