@@ -11,7 +11,7 @@ nearest binary32 value, so the header carries no number of unknown origin:
   * SLM_S*, SLM_C*: Taylor coefficients (-1)^k / (2k+1)! and (-1)^k / (2k)!.
   * SLM_PH_WIN_INIT: bits 19..146 of the word stream above (bit 0 = the most
     significant bit of the zero word), the only bits of 2/pi the Payne-Hanek
-    window reads for 4096 <= |x| < 2^28.
+    window reads for 4096 <= |x| < 2^44.
 
 Run `python include/gen_slime_math_constants.py` to print the C block; the
 CPU test suite re-runs it and compares against the header.

@@ -22,7 +22,7 @@
  *       * otherwise: Payne-Hanek reduction (M. Payne and R. Hanek, "Radian
  *         reduction for trigonometric functions", SIGNUM Newsletter 18(1),
  *         1983) with a 96-bit window of 2/pi and 32x32->64 integer products;
- *         below 2^28 the window comes from four fixed words of 2/pi by funnel
+ *         below 2^44 the window comes from four fixed words of 2/pi by funnel
  *         shifts instead of table reads (same bits, fewer instructions);
  *       * the reduced argument |r| <= pi/4 is fed to the Taylor polynomials of
  *         sin (to r^9) and cos (to r^10) in Horner form.
@@ -282,11 +282,12 @@ SLM_FN void slm_reduce_pio2_ph(float x, float* r_out, int* q_out) {
     slm_ph_finish(m, w0, w1, w2, ix >> 31, r_out, q_out);
 }
 
-/* The same for 4096 <= |x| < 2^28 (biased exponent 139..154): there the
- * window starts at table position u = e + 30 in [19, 34], inside the fixed
- * 128 bits 19..146 of the table (SLM_PH_WIN_INIT), and each window word is one
- * funnel shift of two of them by u - 19.  Equal to slm_reduce_pio2_ph bit for
- * bit on that range (the oracle's self-test compares all 2^28 inputs). */
+/* The same for 4096 <= |x| < 2^44 (biased exponent 139..170): there the
+ * window starts at table position u = e + 30 in [19, 50], so its 96 bits lie
+ * inside the fixed 128 bits 19..146 of the table (SLM_PH_WIN_INIT), and each
+ * window word is one funnel shift of two of them by u - 19 <= 31.  Equal to
+ * slm_reduce_pio2_ph bit for bit on that range (the oracle's self-test
+ * compares all 2^29 inputs). */
 SLM_FN void slm_reduce_pio2_win(float x, float* r_out, int* q_out) {
     const uint32_t K[4] = SLM_PH_WIN_INIT;
     uint32_t ix = slm_f2u_bits(x);
@@ -323,7 +324,7 @@ SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
         *q_out = 0;
         return;
     }
-    if (E <= 154u)
+    if (E <= 170u)
         slm_reduce_pio2_win(x, r_out, q_out);
     else
         slm_reduce_pio2_ph(x, r_out, q_out);

@@ -138,7 +138,7 @@ def colorize(W, H, trail, lut768, tw, th):
     return out
 
 
-def ph_window_mismatches(e_lo=139, e_hi=154):
+def ph_window_mismatches(e_lo=139, e_hi=170):
     """Inputs with biased exponent e_lo..e_hi on which the fixed-window and the
     table-driven Payne-Hanek reductions disagree (0 expected)."""
     return int(lib().oracle_ph_window_mismatches(e_lo, e_hi))

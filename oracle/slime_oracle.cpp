@@ -546,9 +546,9 @@ void oracle_uniform01(uint64_t seed, uint64_t n, uint32_t field, float* out) {
 }
 /* Number of binary32 inputs with biased exponent in [e_lo, e_hi] (both signs)
  * on which the fixed-window Payne-Hanek reduction differs from the table one
- * in the reduced argument's bits or the quadrant; e_lo >= 139, e_hi <= 154. */
+ * in the reduced argument's bits or the quadrant; e_lo >= 139, e_hi <= 170. */
 uint64_t oracle_ph_window_mismatches(uint32_t e_lo, uint32_t e_hi) {
-    if (e_lo < 139 || e_hi > 154 || e_lo > e_hi) return ~0ull;
+    if (e_lo < 139 || e_hi > 170 || e_lo > e_hi) return ~0ull;
     const int64_t per_sign = (int64_t)(e_hi - e_lo + 1) << 23;
     uint64_t bad = 0;
 #pragma omp parallel for schedule(static) reduction(+ : bad)
