@@ -30,7 +30,6 @@ using namespace slime;
 namespace {
 
 constexpr int kEnsThreads = 256;
-constexpr int kAgentsPerItem = 4 * kEnsThreads; // one float4 group per thread
 
 struct DevColony {
     DevParams p;
@@ -39,6 +38,7 @@ struct DevColony {
     uint64_t trail_off; // first cell of the colony in the trail/count buffers
     int32_t warps_x;    // 128-column strips per row band
     int32_t pad;
+    cudaTextureObject_t tex[2]; // gather textures over the colony's two trails (0 = none)
 };
 
 struct GridBarrier {
@@ -53,6 +53,7 @@ struct Colony {
     uint64_t n, n_pad, agent_off, trail_off;
     SlimeParams params;
     DevParams dev;
+    cudaTextureObject_t tex[2] = {0, 0};
 };
 
 // Bounded grid barrier: every block arrives once; the last one to arrive
@@ -95,12 +96,31 @@ __global__ void barrier_timeout_kernel(GridBarrier* bar, long long limit_cycles,
     if (threadIdx.x == 0) *reached_after = ok ? 1 : 2;
 }
 
+// Four consecutive agents of one colony (the last group may be partial).
+template <class Trail>
+__device__ __forceinline__ void steps4(const DevParams& sp, float4& x, float4& y, float4& th, float4& v, const uint4& id,
+                                       uint64_t base, uint64_t n, const Trail& trail, int& c0, int& c1, int& c2,
+                                       int& c3) {
+    if (base + 4 <= n) { // full group: no per-agent branch
+        c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+        c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
+        c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
+        c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
+    } else {
+        c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+        if (base + 1 < n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
+        if (base + 2 < n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
+        if (base + 3 < n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
+    }
+}
+
 template <int R, bool kGauss, int ROWS>
 __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
     const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
     const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
     float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS, const float* __restrict__ trail_in,
-    uint32_t* counts_in, float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar) {
+    uint32_t* counts_in, float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar,
+    int parity) {
     __shared__ DevParams sp;
     // ---- phase 1: agents
     for (uint32_t item = blockIdx.x; item < n_agent_items; item += gridDim.x) {
@@ -123,19 +143,15 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
         float4* pv = reinterpret_cast<float4*>(V + slot);
         float4 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
         const uint4 id = __ldcs(reinterpret_cast<const uint4*>(IDS + slot)); // colony-local agent ids
-        const float* trail = trail_in + c.trail_off;
         uint32_t* counts = counts_in + c.trail_off;
+        const cudaTextureObject_t tex = c.tex[parity];
         int c0, c1 = -1, c2 = -1, c3 = -1;
-        if (base + 4 <= c.n) { // full group: no per-agent branch
-            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
-            c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
-            c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
-            c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
+        // the colony's trail through its gather texture when it has one,
+        // else through the padded buffer (block-uniform choice)
+        if (tex) {
+            steps4(sp, x, y, th, v, id, base, c.n, TrailTex{tex}, c0, c1, c2, c3);
         } else {
-            c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
-            if (base + 1 < c.n) c1 = agent_step(sp, x.y, y.y, th.y, v.y, (int32_t)id.y, trail);
-            if (base + 2 < c.n) c2 = agent_step(sp, x.z, y.z, th.z, v.z, (int32_t)id.z, trail);
-            if (base + 3 < c.n) c3 = agent_step(sp, x.w, y.w, th.w, v.w, (int32_t)id.w, trail);
+            steps4(sp, x, y, th, v, id, base, c.n, TrailPtr{trail_in + c.trail_off}, c0, c1, c2, c3);
         }
         if (c0 >= 0) atomicAdd(counts + c0, 1u);
         if (c1 >= 0) atomicAdd(counts + c1, 1u);
@@ -162,7 +178,7 @@ __global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
 }
 
 typedef void (*EnsKernel)(const DevColony*, const uint2*, uint32_t, const uint4*, uint32_t, float*, float*, float*,
-                          float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*);
+                          float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*, int);
 
 template <int ROWS>
 EnsKernel pick_rows(int R, bool gauss) {
@@ -243,6 +259,8 @@ int upload_cols(slime_ensemble* e) {
         dc[j].n = c.n;
         dc[j].trail_off = c.trail_off;
         dc[j].warps_x = (int32_t)((c.W + 127) / 128);
+        dc[j].tex[0] = c.tex[0];
+        dc[j].tex[1] = c.tex[1];
     }
     ECK(cudaMemcpyAsync(e->d_cols, dc.data(), dc.size() * sizeof(DevColony), cudaMemcpyHostToDevice, e->stream),
         "uploading colony table");
@@ -296,7 +314,8 @@ cudaError_t enqueue_ens_step(slime_ensemble* e) {
     uint32_t* cz = e->counts[1 - cur];
     GridBarrier* bar = e->d_bar;
     const uint32_t* ids = e->ids;
-    void* args[] = {&cols, &ai, &nai, &si, &nsi, &X, &Y, &TH, &V, &ids, &tin, &cin, &tout, &cz, &bar};
+    int parity = cur;
+    void* args[] = {&cols, &ai, &nai, &si, &nsi, &X, &Y, &TH, &V, &ids, &tin, &cin, &tout, &cz, &bar, &parity};
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3(e->grid);
@@ -459,8 +478,9 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         c.trail_off = cells;
         slots += c.n_pad;
         cells += (uint64_t)c.W * c.H;
-        // keep every colony's first cell 16-byte aligned
-        cells = (cells + 3) & ~3ull;
+        // every colony's first cell 256-byte aligned (float4 rows, and a
+        // base its gather texture accepts)
+        cells = (cells + 63) & ~63ull;
         e->colonies.push_back(c);
     }
     if (e->colonies.size() != k) {
@@ -511,6 +531,10 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         cudaError_t ie = launch_iota(e->ids + c.agent_off, c.n, e->stream);
         if (ie != cudaSuccess) rc = cuda_error(e->err, ie, "initialising agent ids");
     }
+    for (uint32_t j = 0; rc == SLIME_OK && j < k; j++) {
+        Colony& c = e->colonies[j];
+        for (int i = 0; i < 2; i++) c.tex[i] = make_trail_texture(e->trail[i] + c.trail_off, c.W, c.H);
+    }
     if (rc == SLIME_OK) rc = upload_cols(e);
     if (rc == SLIME_OK) rc = build_strip_items(e);
     if (rc == SLIME_OK) rc = size_grid(e);
@@ -528,6 +552,9 @@ void slime_ensemble_destroy(slime_ensemble* e) {
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     ens_invalidate(e);
+    for (Colony& c : e->colonies)
+        for (int i = 0; i < 2; i++)
+            if (c.tex[i]) cudaDestroyTextureObject(c.tex[i]);
     void* ptrs[] = {e->agent_block, e->ids, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->d_cols,
                     e->d_agent_items, e->d_strip_items, e->d_bar, e->staging, e->reorder.buf};
     for (void* p : ptrs)
