@@ -121,7 +121,9 @@ typedef struct SlimeOptions {
     uint32_t l2_persist;        /* 1: persisting-L2 access window over the sensed trail (default 1) */
     uint32_t trail_tile;        /* 0: autotuned/default, otherwise 1 + an index into the tile table */
     uint32_t agent_shape;       /* 0: autotuned/default, otherwise 1 + an index into the agent-shape table */
-    uint32_t reserved;
+    uint32_t exact_counts;      /* 1: always keep per-cell deposit counts (slime_download_deposit_counts); 0
+                                   (default): steps in which every deposit saturates the fold (deposition >= 1
+                                   on a non-negative trail) record only which cells received deposits */
 } SlimeOptions;
 
 typedef struct SlimeInfo {

@@ -228,7 +228,11 @@ int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every) 
             CK(cudaMemcpyAsync(a.ckpt_trail + (size_t)j * cells, ctx->trail[ctx->cur], cells * sizeof(float),
                                cudaMemcpyDeviceToDevice, ctx->stream), "checkpointing trail");
         }
-        CK(enqueue_step(ctx), "recording a step");
+        const bool marks = use_marks(ctx);
+        int prc = prepare_deposits(ctx, marks);
+        if (prc != SLIME_OK) return prc;
+        CK(enqueue_step(ctx, marks), "recording a step");
+        after_steps(ctx, marks, 1);
         ctx->launches += kernels_per_step(ctx);
         ctx->steps_done++;
     }

@@ -8,6 +8,8 @@
 //   counts[2] per-cell deposit counters: counts[cur] collects the next step's
 //            deposits (kept zero between steps), counts[1-cur] holds the
 //            previous step's
+//   marks[2] per-cell deposit marks (bytes), the counts' stand-in for steps
+//            in which every deposit saturates the fold
 // and enqueues everything on its own stream.  Steps are captured in CUDA
 // graphs of `graph_chunk` steps, one per starting parity, and replayed.
 #include <math.h>
@@ -177,6 +179,8 @@ void free_trail(slime_ctx* ctx) {
         ctx->trail_tex[i] = 0;
         if (ctx->trail[i]) dev_free(ctx->trail[i]);
         if (ctx->counts[i]) dev_free(ctx->counts[i]);
+        if (ctx->marks[i]) dev_free(ctx->marks[i]);
+        ctx->marks[i] = nullptr;
         ctx->trail[i] = nullptr;
         ctx->counts[i] = nullptr;
     }
@@ -209,10 +213,16 @@ int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
         CK(dev_alloc((void**)&ctx->counts[i], cells * sizeof(uint32_t)), "allocating deposit counts");
         CK(cudaMemsetAsync(ctx->trail[i], 0, (cells + W + 2) * sizeof(float), ctx->stream), "clearing trail");
         CK(cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream), "clearing counts");
+        CK(dev_alloc((void**)&ctx->marks[i], (cells + 15) & ~(size_t)15), "allocating deposit marks");
+        CK(cudaMemsetAsync(ctx->marks[i], 0, (cells + 15) & ~(size_t)15, ctx->stream), "clearing marks");
+        ctx->counts_dirty[i] = false;
+        ctx->marks_dirty[i] = false;
         ctx->trail_tex[i] = make_trail_texture(ctx->trail[i], W, H);
     }
     ctx->cur = 0;
     ctx->last_counts_valid = false;
+    ctx->trail_clean = true;
+    ctx->last_marks = false;
     return SLIME_OK;
 }
 
@@ -317,29 +327,96 @@ bool trail_window(const slime_ctx* ctx, const float* t, cudaAccessPolicyWindow* 
     return true;
 }
 
-// Enqueue one step on the context's stream (also used under capture).  The
-// agent pass keeps the trail it senses resident; the trail pass marks the
-// trail it writes, which the next agent pass senses.
-cudaError_t enqueue_step(slime_ctx* ctx) {
+// Whether a step keeps a clean trail clean (finite values >= 0, or +inf):
+// the subtractive decay never raises a value, the multiplicative one with a
+// factor in [0, 1] neither; the fold, the blur's non-negative weights and the
+// clamped diffusion rate preserve it.
+bool keeps_trail_clean(const DevParams& d) {
+    if (d.decay_mode == SLIME_DECAY_MULTIPLY) return d.decay >= 0.0f && d.decay <= 1.0f;
+    return d.decay_k >= 0.0f;
+}
+
+// Whether the next steps record deposit marks instead of counts.  With a
+// deposition of at least 1 on a trail value t >= 0, the first deposit folds
+// t to clamp(t + dep, 0, 1) = 1 and every further one leaves it there, so the
+// fold of k deposits depends only on whether k > 0: one byte per cell carries
+// it, written with plain stores instead of 32-bit atomics, and the trail pass
+// reads 1 byte per cell instead of 4 and clears 1 instead of 4.  The result
+// is the same, bit for bit.  The host decides, from the parameters, the tile
+// (the streaming tiles read marks) and what it knows of the trail: clean
+// after creation, clear and resize, checked on upload, kept by steps that
+// keep it (keeps_trail_clean).
+bool use_marks(const slime_ctx* ctx) {
+    if (ctx->opt.exact_counts || ctx->agents.n == 0 || !ctx->trail_clean) return false;
+    if (!(ctx->dev.dep >= 1.0f) || !keeps_trail_clean(ctx->dev)) return false;
+    return trail_tile_streams(ctx->dev, ctx->tile);
+}
+
+// The record the next step writes (counts[cur] or marks[cur]) must start at
+// zero; a record left behind by steps of the other kind is cleared here,
+// outside any captured graph.
+int prepare_deposits(slime_ctx* ctx, bool marks) {
     const int cur = ctx->cur;
-    cudaAccessPolicyWindow wa, wt;
+    const size_t cells = (size_t)ctx->W * ctx->H;
+    if (marks && ctx->marks_dirty[cur]) {
+        CK(cudaMemsetAsync(ctx->marks[cur], 0, cells, ctx->stream), "clearing deposit marks");
+        ctx->marks_dirty[cur] = false;
+    }
+    if (!marks && ctx->counts_dirty[cur]) {
+        CK(cudaMemsetAsync(ctx->counts[cur], 0, cells * sizeof(uint32_t), ctx->stream), "clearing deposit counts");
+        ctx->counts_dirty[cur] = false;
+    }
+    return SLIME_OK;
+}
+
+// Bookkeeping after m steps of one kind (ctx->cur already advanced): the
+// last step's record holds its deposits, the trail pass cleared the other.
+void after_steps(slime_ctx* ctx, bool marks, uint32_t m) {
+    if (m == 0) return;
+    bool* dirty = marks ? ctx->marks_dirty : ctx->counts_dirty;
+    dirty[ctx->cur] = false;
+    dirty[1 - ctx->cur] = true;
+    ctx->trail_clean = ctx->trail_clean && keeps_trail_clean(ctx->dev);
+    ctx->last_marks = marks;
+    ctx->last_counts_valid = true;
+}
+
+// The two passes of one step on the context's stream (also used under
+// capture).  The agent pass keeps the trail it senses resident; the trail
+// pass marks the trail it writes, which the next agent pass senses.
+cudaError_t enqueue_agents_pass(slime_ctx* ctx, bool marks) {
+    const int cur = ctx->cur;
+    cudaAccessPolicyWindow wa;
     bool ha = trail_window(ctx, ctx->trail[cur], &wa);
+    return launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, ctx->agent_shape,
+                         ha ? &wa : nullptr, ctx->trail_tex[cur], marks ? ctx->marks[cur] : nullptr);
+}
+
+cudaError_t enqueue_trail_pass(slime_ctx* ctx, bool marks) {
+    const int cur = ctx->cur;
+    cudaAccessPolicyWindow wt;
     bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt);
-    cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream,
-                                  ctx->agent_shape, ha ? &wa : nullptr, ctx->trail_tex[cur]);
+    if (marks)
+        return launch_trail_marks(ctx->dev, ctx->tile, ctx->trail[cur], ctx->marks[cur], ctx->trail[1 - cur],
+                                  ctx->marks[1 - cur], ctx->stream, ht ? &wt : nullptr);
+    return launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
+                        ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr);
+}
+
+cudaError_t enqueue_step(slime_ctx* ctx, bool marks) {
+    cudaError_t e = enqueue_agents_pass(ctx, marks);
     if (e != cudaSuccess) return e;
-    e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                     ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr);
+    e = enqueue_trail_pass(ctx, marks);
     if (e != cudaSuccess) return e;
-    ctx->cur = 1 - cur;
+    ctx->cur = 1 - ctx->cur;
     return cudaSuccess;
 }
 
 uint64_t kernels_per_step(const slime_ctx* ctx) { return ctx->agents.n ? 2 : 1; }
 
-int run_steps_direct(slime_ctx* ctx, uint32_t m) {
+int run_steps_direct(slime_ctx* ctx, uint32_t m, bool marks) {
     for (uint32_t i = 0; i < m; i++) {
-        CK(enqueue_step(ctx), "launching a step");
+        CK(enqueue_step(ctx, marks), "launching a step");
         ctx->launches += kernels_per_step(ctx);
         ctx->steps_done++;
     }
@@ -347,15 +424,15 @@ int run_steps_direct(slime_ctx* ctx, uint32_t m) {
     return SLIME_OK;
 }
 
-int run_steps_graph(slime_ctx* ctx, uint32_t m) {
-    auto key = std::make_pair(m, ctx->cur);
+int run_steps_graph(slime_ctx* ctx, uint32_t m, bool marks) {
+    auto key = std::make_pair(m, ctx->cur | (marks ? 2 : 0));
     auto it = ctx->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
     if (it == ctx->graphs.end()) {
         const int saved = ctx->cur;
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "beginning graph capture");
         cudaError_t ce = cudaSuccess;
-        for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_step(ctx);
+        for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_step(ctx, marks);
         cudaGraph_t graph = nullptr;
         cudaError_t ee = cudaStreamEndCapture(ctx->stream, &graph);
         ctx->cur = saved;
@@ -416,11 +493,15 @@ int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
         cudaError_t e = cudaMemcpyAsync(ctx->agent_block, snap, abytes, cudaMemcpyDeviceToDevice, ctx->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(ctx->trail[cur], snap + abytes, tbytes, cudaMemcpyDeviceToDevice, ctx->stream);
-        for (int i = 0; i < 2 && e == cudaSuccess; i++)
+        for (int i = 0; i < 2 && e == cudaSuccess; i++) {
             e = cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(ctx->marks[i], 0, cells, ctx->stream);
+            ctx->counts_dirty[i] = ctx->marks_dirty[i] = false;
+        }
         ctx->cur = cur;
         return e;
     };
+    const bool marks = use_marks(ctx);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = cudaMemcpyAsync(snap, ctx->agent_block, abytes, cudaMemcpyDeviceToDevice, ctx->stream);
     if (e == cudaSuccess)
@@ -434,10 +515,10 @@ int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
             setup_l2(ctx);
             if (!off && !ctx->l2_persist_bytes) break; // no carve-out to compare with
             e = restore();
-            for (int w = 0; w < 2 && e == cudaSuccess; w++) e = enqueue_step(ctx);
+            for (int w = 0; w < 2 && e == cudaSuccess; w++) e = enqueue_step(ctx, marks);
             if (e == cudaSuccess) e = restore();
             if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
-            for (uint32_t i = 0; i < steps && e == cudaSuccess; i++) e = enqueue_step(ctx);
+            for (uint32_t i = 0; i < steps && e == cudaSuccess; i++) e = enqueue_step(ctx, marks);
             if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float ms = 0.0f;
@@ -471,13 +552,17 @@ int run_steps(slime_ctx* ctx, uint32_t n) {
             uint64_t to_next = ctx->opt.reorder_every - ctx->steps_done % ctx->opt.reorder_every;
             if (to_next < m) m = (uint32_t)to_next;
         }
+        const bool marks = use_marks(ctx);
+        if ((rc = prepare_deposits(ctx, marks)) != SLIME_OK) return rc;
         if (ctx->opt.use_graphs) {
             uint32_t chunk = ctx->opt.graph_chunk ? ctx->opt.graph_chunk : 50;
             uint32_t take = m < chunk ? m : chunk;
-            if ((rc = run_steps_graph(ctx, take)) != SLIME_OK) return rc;
+            if ((rc = run_steps_graph(ctx, take, marks)) != SLIME_OK) return rc;
+            after_steps(ctx, marks, take);
             n -= take;
         } else {
-            if ((rc = run_steps_direct(ctx, m)) != SLIME_OK) return rc;
+            if ((rc = run_steps_direct(ctx, m, marks)) != SLIME_OK) return rc;
+            after_steps(ctx, marks, m);
             n -= m;
         }
     }
@@ -601,7 +686,6 @@ int slime_set_options(slime_ctx* ctx, const SlimeOptions* o) {
     if (o->agent_shape > (uint32_t)agent_shape_count())
         return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "agent_shape out of range (0..%d)",
                          agent_shape_count());
-    if (o->reserved != 0) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "options.reserved must be 0");
     const bool l2_changed = (o->l2_persist != 0) != (ctx->opt.l2_persist != 0);
     ctx->opt = *o;
     if (ctx->opt.graph_chunk == 0) ctx->opt.graph_chunk = 50;
@@ -701,7 +785,12 @@ int slime_upload_trail(slime_ctx* ctx, const float* trail, uint64_t n_cells) {
                          (unsigned long long)n_cells, (unsigned long long)ctx->W * ctx->H);
     CK(cudaMemcpyAsync(ctx->trail[ctx->cur], trail, n_cells * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
        "uploading trail");
+    // deposit marks need every value finite and >= 0 (or +inf): checked
+    // while the copy runs
+    bool clean = true;
+    for (uint64_t i = 0; i < n_cells; i++) clean = clean && (trail[i] >= 0.0f);
     CK(cudaStreamSynchronize(ctx->stream), "uploading trail");
+    ctx->trail_clean = clean;
     return SLIME_OK;
 }
 
@@ -722,6 +811,7 @@ int slime_clear_trail(slime_ctx* ctx) {
     cudaSetDevice(ctx->device);
     CK(cudaMemsetAsync(ctx->trail[ctx->cur], 0, (size_t)ctx->W * ctx->H * sizeof(float), ctx->stream), "clearing trail");
     CK(cudaStreamSynchronize(ctx->stream), "clearing trail");
+    ctx->trail_clean = true;
     return SLIME_OK;
 }
 
@@ -840,6 +930,10 @@ int slime_download_deposit_counts(slime_ctx* ctx, uint32_t* counts, uint64_t n_c
         memset(counts, 0, n_cells * sizeof(uint32_t));
         return SLIME_OK;
     }
+    if (ctx->last_marks)
+        return set_error(ctx->err, SLIME_ERR_STATE,
+                         "the last step recorded which cells received deposits, not how many (every deposit "
+                         "saturated the fold); set options.exact_counts = 1 to keep counts");
     CK(cudaMemcpyAsync(counts, ctx->counts[1 - ctx->cur], n_cells * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                        ctx->stream),
        "downloading deposit counts");
@@ -868,26 +962,22 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
         if (ctx->opt.reorder_every && ctx->steps_done % ctx->opt.reorder_every == 0 &&
             ctx->last_reorder_step != ctx->steps_done)
             rc = do_reorder(ctx);
+        const bool marks = use_marks(ctx);
+        if (rc == SLIME_OK) rc = prepare_deposits(ctx, marks);
+        if (rc != SLIME_OK) break;
         cudaEventRecord(ev[1], ctx->stream);
-        const int cur = ctx->cur;
-        cudaAccessPolicyWindow wa, wt;
-        bool ha = trail_window(ctx, ctx->trail[cur], &wa);
-        bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt);
-        cudaError_t e = launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream,
-                                      ctx->agent_shape, ha ? &wa : nullptr, ctx->trail_tex[cur]);
+        cudaError_t e = enqueue_agents_pass(ctx, marks);
         cudaEventRecord(ev[2], ctx->stream);
-        if (e == cudaSuccess)
-            e = launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                             ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr);
+        if (e == cudaSuccess) e = enqueue_trail_pass(ctx, marks);
         cudaEventRecord(ev[3], ctx->stream);
         if (e != cudaSuccess) {
             rc = cuda_error(ctx->err, e, "profiling a step");
             break;
         }
-        ctx->cur = 1 - cur;
+        ctx->cur = 1 - ctx->cur;
         ctx->steps_done++;
         ctx->launches += kernels_per_step(ctx);
-        ctx->last_counts_valid = true;
+        after_steps(ctx, marks, 1);
         if ((e = cudaEventSynchronize(ev[3])) != cudaSuccess) {
             rc = cuda_error(ctx->err, e, "profiling a step");
             break;

@@ -25,6 +25,13 @@ struct slime_ctx {
     uint32_t* counts[2] = {nullptr, nullptr};
     int cur = 0;
     bool last_counts_valid = false;
+    // Deposit marks: one byte per cell, used instead of the counts by steps
+    // in which every deposit saturates the fold (see use_marks in capi.cu).
+    uint8_t* marks[2] = {nullptr, nullptr};
+    bool counts_dirty[2] = {false, false}; // buffer may hold non-zero entries
+    bool marks_dirty[2] = {false, false};
+    bool trail_clean = true; // every value of trail[cur] is finite and >= 0 (or +inf)
+    bool last_marks = false; // the last step recorded marks, not counts
 
     SlimeParams params{};
     slime::DevParams dev{};
@@ -86,7 +93,10 @@ namespace slime {
 int set_error(std::string& err, int code, const char* fmt, ...);
 int cuda_error(std::string& err, cudaError_t e, const char* what);
 void invalidate_graphs(slime_ctx* ctx);
-cudaError_t enqueue_step(slime_ctx* ctx);
+bool use_marks(const slime_ctx* ctx);
+int prepare_deposits(slime_ctx* ctx, bool marks);
+cudaError_t enqueue_step(slime_ctx* ctx, bool marks);
+void after_steps(slime_ctx* ctx, bool marks, uint32_t m);
 uint64_t kernels_per_step(const slime_ctx* ctx);
 int run_steps(slime_ctx* ctx, uint32_t n);
 void free_adjoint(slime_ctx* ctx);

@@ -33,10 +33,12 @@ AgentShape agent_shape(int index);
 bool agent_shape_uses_texture(int index);
 // One agent pass (compute.wgsl:57-145): reads trail, adds deposit counts.
 // `tex` is a texture over `trail` (make_trail_texture) for the shapes that
-// sample through it; 0 runs those shapes on the pointer path.
+// sample through it; 0 runs those shapes on the pointer path.  With `marks`
+// the deposits set per-cell byte marks instead of counting (valid only when
+// every deposit saturates the fold: deposition >= 1 on a trail >= 0).
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
                           cudaStream_t s, int shape = 0, const cudaAccessPolicyWindow* win = nullptr,
-                          cudaTextureObject_t tex = 0);
+                          cudaTextureObject_t tex = 0, uint8_t* marks = nullptr);
 cudaTextureObject_t make_trail_texture(const float* trail, uint32_t W, uint32_t H);
 // AoS staging (x, y, angle, speed per agent, id order) <-> SoA slots.
 cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s);
@@ -61,6 +63,13 @@ bool trail_tile_supported(const DevParams& p, int tile);
 // counts_zero (the other step's count buffer, may be null) over the same cells.
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
                          uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr);
+// Whether tile `index` is a streaming tile that runs here (the only ones that
+// read deposit marks).
+bool trail_tile_streams(const DevParams& p, int tile);
+// The same pass folding per-cell byte marks (0/1) instead of counts; zeroes
+// marks_zero.  Streaming tiles only (cudaErrorInvalidValue otherwise).
+cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, const uint8_t* marks_in, float* out,
+                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr);
 
 // ---- adjoint.cu
 // One backward step of the frozen-trajectory chain: from g_in = dL/dT_{s+1}

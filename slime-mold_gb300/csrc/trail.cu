@@ -103,32 +103,31 @@ __global__ void __launch_bounds__(kThreads) trail_gauss_kernel(const __grid_cons
     }
 }
 
-template <int R, bool kGauss, int ROWS>
+template <int R, bool kGauss, int ROWS, class D>
 __global__ void __launch_bounds__(128) trail_stream_kernel(const __grid_constant__ DevParams p,
-                                                           const float* __restrict__ in,
-                                                           const uint32_t* __restrict__ cin,
-                                                           float* __restrict__ out,
-                                                           uint32_t* __restrict__ czero, int warps_x) {
+                                                           const float* __restrict__ in, const D* __restrict__ cin,
+                                                           float* __restrict__ out, D* __restrict__ czero,
+                                                           int warps_x) {
     const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
-    process_strip<R, kGauss, ROWS>(p, in, cin, out, czero, gw % warps_x, gw / warps_x);
+    process_strip<R, kGauss, ROWS, false, true, D>(p, in, cin, out, czero, gw % warps_x, gw / warps_x);
 }
 
-template <int R, bool kGauss, int ROWS>
-cudaError_t launch_stream(const DevParams& p, const float* in, const uint32_t* cin, float* out, uint32_t* cz,
-                          cudaStream_t s, const cudaAccessPolicyWindow* win) {
+template <int R, bool kGauss, int ROWS, class D>
+cudaError_t launch_stream(const DevParams& p, const float* in, const D* cin, float* out, D* cz, cudaStream_t s,
+                          const cudaAccessPolicyWindow* win) {
     int warps_x = (p.W + 127) / 128;
     long long warps = (long long)warps_x * ((p.H + ROWS - 1) / ROWS);
     unsigned blocks = (unsigned)((warps + 3) / 4);
-    return launch_k(trail_stream_kernel<R, kGauss, ROWS>, dim3(blocks), dim3(128), 0, s, win, p, in, cin, out, cz,
-                    warps_x);
+    return launch_k(trail_stream_kernel<R, kGauss, ROWS, D>, dim3(blocks), dim3(128), 0, s, win, p, in, cin, out,
+                    cz, warps_x);
 }
 
-template <int ROWS>
-cudaError_t launch_stream_rows(const DevParams& p, const float* in, const uint32_t* cin, float* out, uint32_t* cz,
-                               cudaStream_t s, const cudaAccessPolicyWindow* win) {
-    if (p.blur_mode != SLIME_BLUR_GAUSS) return launch_stream<1, false, ROWS>(p, in, cin, out, cz, s, win);
-    if (p.R == 1) return launch_stream<1, true, ROWS>(p, in, cin, out, cz, s, win);
-    return launch_stream<2, true, ROWS>(p, in, cin, out, cz, s, win);
+template <int ROWS, class D>
+cudaError_t launch_stream_rows(const DevParams& p, const float* in, const D* cin, float* out, D* cz, cudaStream_t s,
+                               const cudaAccessPolicyWindow* win) {
+    if (p.blur_mode != SLIME_BLUR_GAUSS) return launch_stream<1, false, ROWS, D>(p, in, cin, out, cz, s, win);
+    if (p.R == 1) return launch_stream<1, true, ROWS, D>(p, in, cin, out, cz, s, win);
+    return launch_stream<2, true, ROWS, D>(p, in, cin, out, cz, s, win);
 }
 
 const TrailTile kTiles[] = {{32, 8}, {64, 8}, {32, 16}, {64, 16}, {128, 8}, {128, 16}, {256, 8}};
@@ -196,6 +195,18 @@ bool trail_tile_supported(const DevParams& p, int tile) {
     // wider than a halo
     int R = p.blur_mode == SLIME_BLUR_GAUSS ? p.R : 1;
     return (p.W % 4) == 0 && p.W >= 8 && R >= 1 && R <= 2 && p.H >= 1;
+}
+
+bool trail_tile_streams(const DevParams& p, int tile) { return tile >= kNumTiles && trail_tile_supported(p, tile); }
+
+cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, const uint8_t* marks_in, float* out,
+                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win) {
+    if (!trail_tile_streams(p, tile)) return cudaErrorInvalidValue;
+    switch (tile) {
+    case 7: return launch_stream_rows<8>(p, in, marks_in, out, marks_zero, s, win);
+    case 8: return launch_stream_rows<16>(p, in, marks_in, out, marks_zero, s, win);
+    default: return launch_stream_rows<32>(p, in, marks_in, out, marks_zero, s, win);
+    }
 }
 
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,

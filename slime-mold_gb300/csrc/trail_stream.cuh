@@ -31,6 +31,29 @@ __device__ __forceinline__ uint4 load_count4(const uint4* p) {
     return kCoherent ? __ldcg(p) : __ldg(p);
 }
 
+// The step's deposit record is either per-cell 32-bit counts or, when every
+// deposit saturates the fold, per-cell byte marks (0 or 1).  Both are read as
+// a count k of 32-bit width; a mark of 1 folds exactly as any k >= 1 does then.
+template <bool kCoherent>
+__device__ __forceinline__ uint4 load_dep4(const uint32_t* p) {
+    return load_count4<kCoherent>(reinterpret_cast<const uint4*>(p));
+}
+template <bool kCoherent>
+__device__ __forceinline__ uint4 load_dep4(const uint8_t* p) {
+    const uchar4 m = __ldg(reinterpret_cast<const uchar4*>(p));
+    return make_uint4(m.x, m.y, m.z, m.w);
+}
+template <bool kCoherent>
+__device__ __forceinline__ uint32_t load_dep(const uint32_t* p) {
+    return load_count<kCoherent>(p);
+}
+template <bool kCoherent>
+__device__ __forceinline__ uint32_t load_dep(const uint8_t* p) {
+    return __ldg(p);
+}
+__device__ __forceinline__ void zero_dep4(uint32_t* p) { *reinterpret_cast<uint4*>(p) = make_uint4(0u, 0u, 0u, 0u); }
+__device__ __forceinline__ void zero_dep4(uint8_t* p) { *reinterpret_cast<uchar4*>(p) = make_uchar4(0, 0, 0, 0); }
+
 // One input row as a lane sees it: its four cells and, for the first lane and
 // the last active lane of the warp, the R wrapped halo cells on its open side.
 template <int R>
@@ -41,13 +64,12 @@ struct RowFetch {
     uint32_t hk[R];
 };
 
-template <int R, bool kCoherent>
-__device__ __forceinline__ void fetch_row(const DevParams& p, const float* __restrict__ in,
-                                          const uint32_t* __restrict__ cin, int row, int cl, bool has_halo,
-                                          int hcol0, RowFetch<R>& f) {
+template <int R, bool kCoherent, class D>
+__device__ __forceinline__ void fetch_row(const DevParams& p, const float* __restrict__ in, const D* __restrict__ cin,
+                                          int row, int cl, bool has_halo, int hcol0, RowFetch<R>& f) {
     const size_t base = (size_t)row * p.W;
     f.t = __ldg(reinterpret_cast<const float4*>(in + base + cl));
-    f.k = load_count4<kCoherent>(reinterpret_cast<const uint4*>(cin + base + cl));
+    f.k = load_dep4<kCoherent>(cin + base + cl);
 #pragma unroll
     for (int j = 0; j < R; j++) {
         f.ht[j] = 0.0f;
@@ -55,18 +77,27 @@ __device__ __forceinline__ void fetch_row(const DevParams& p, const float* __res
         if (has_halo) {
             int col = wrap_coord(hcol0 + j, p.W);
             f.ht[j] = __ldg(in + base + col);
-            f.hk[j] = load_count<kCoherent>(cin + base + col);
+            f.hk[j] = load_dep<kCoherent>(cin + base + col);
         }
     }
 }
 
-template <int R, int kDecay>
+// The fold of a cell's deposits.  From marks, which are used only when every
+// deposit saturates (deposition >= 1 on t >= 0), the first deposit's
+// clamp(t + dep, 0, 1) is exactly 1, so a marked cell folds to 1.0f.
+template <bool kMarks>
+__device__ __forceinline__ float fold_dep(float t, uint32_t k, float dep) {
+    if (kMarks) return k ? 1.0f : t;
+    return fold_deposits(t, k, dep);
+}
+
+template <int R, int kDecay, bool kMarks>
 __device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch<R>& f, bool left_edge,
                                               bool right_edge, ExtRow<R>& e) {
-    float d[4] = {apply_decay_m<kDecay>(p, fold_deposits(f.t.x, f.k.x, p.dep)),
-                  apply_decay_m<kDecay>(p, fold_deposits(f.t.y, f.k.y, p.dep)),
-                  apply_decay_m<kDecay>(p, fold_deposits(f.t.z, f.k.z, p.dep)),
-                  apply_decay_m<kDecay>(p, fold_deposits(f.t.w, f.k.w, p.dep))};
+    float d[4] = {apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.x, f.k.x, p.dep)),
+                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.y, f.k.y, p.dep)),
+                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.z, f.k.z, p.dep)),
+                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.w, f.k.w, p.dep))};
 #pragma unroll
     for (int j = 0; j < 4; j++) e.v[R + j] = d[j];
 #pragma unroll
@@ -76,7 +107,7 @@ __device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch
     }
 #pragma unroll
     for (int j = 0; j < R; j++) {
-        float h = apply_decay_m<kDecay>(p, fold_deposits(f.ht[j], f.hk[j], p.dep));
+        float h = apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.ht[j], f.hk[j], p.dep));
         if (left_edge) e.v[j] = h;
         if (right_edge) e.v[R + 4 + j] = h;
     }
@@ -88,10 +119,11 @@ __device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch
 // rows rotates by renaming registers rather than by copies (at the price of
 // registers: kernels that must stay small, like the ensemble's, keep the loop).
 // kDecay is the decay mode (SLIME_DECAY_*) or -1 to read it from p at run time.
-template <int R, bool kGauss, int ROWS, bool kCoherent, int kDecay, bool kUnrolled>
+// D is the deposit record's element type: uint32_t counts or uint8_t marks.
+template <int R, bool kGauss, int ROWS, bool kCoherent, int kDecay, bool kUnrolled, class D>
 __device__ __forceinline__ void process_strip_m(const DevParams& p, const float* __restrict__ in,
-                                                const uint32_t* __restrict__ cin, float* __restrict__ out,
-                                                uint32_t* __restrict__ czero, int cw, int rs) {
+                                                const D* __restrict__ cin, float* __restrict__ out,
+                                                D* __restrict__ czero, int cw, int rs) {
     const int lane = threadIdx.x & 31;
     const int W = p.W, H = p.H;
     const int y0 = rs * ROWS;
@@ -111,8 +143,8 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     const bool has_halo = active && (left_edge || right_edge);
     const int hcol0 = left_edge ? c0 - R : c0 + 4;
     RowFetch<R> fa, fb;
-    fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R, H), cl, has_halo, hcol0, fa);
-    fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R + 1, H), cl, has_halo, hcol0, fb);
+    fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R, H), cl, has_halo, hcol0, fa);
+    fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + 1, H), cl, has_halo, hcol0, fb);
     // short strips unroll completely when asked to; long ones stay rolled
     // (unrolled, their live ranges exceed the register budget and spill)
     constexpr int kUnroll = (kUnrolled && NR <= 12) ? NR : 1;
@@ -120,7 +152,8 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     for (int r = 0; r < NR; r++) {
         RowFetch<R> cur = fa;
         fa = fb;
-        if (r + 2 < NR) fetch_row<R, kCoherent>(p, in, cin, wrap_coord(y0 - R + r + 2, H), cl, has_halo, hcol0, fb);
+        if (r + 2 < NR)
+            fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + r + 2, H), cl, has_halo, hcol0, fb);
         // shift the window and add the new row
 #pragma unroll
         for (int q = 0; q < NWIN - 1; q++) {
@@ -130,7 +163,7 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
                 for (int j = 0; j < 4; j++) hwin[q][j] = hwin[q + 1][j];
             }
         }
-        build_ext_row<R, kDecay>(p, cur, left_edge && active, right_edge, win[NWIN - 1]);
+        build_ext_row<R, kDecay, sizeof(D) == 1>(p, cur, left_edge && active, right_edge, win[NWIN - 1]);
         if (kGauss) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -165,22 +198,24 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
         }
         const size_t off = (size_t)y * W + c0;
         *reinterpret_cast<float4*>(out + off) = make_float4(o[0], o[1], o[2], o[3]);
-        if (czero) *reinterpret_cast<uint4*>(czero + off) = make_uint4(0u, 0u, 0u, 0u);
+        if (czero) zero_dep4(czero + off);
     }
 }
 
-template <int R, bool kGauss, int ROWS, bool kCoherent = false, bool kUnrolled = true>
+template <int R, bool kGauss, int ROWS, bool kCoherent = false, bool kUnrolled = true, class D = uint32_t>
 __device__ __forceinline__ void process_strip(const DevParams& p, const float* __restrict__ in,
-                                              const uint32_t* __restrict__ cin, float* __restrict__ out,
-                                              uint32_t* __restrict__ czero, int cw, int rs) {
+                                              const D* __restrict__ cin, float* __restrict__ out,
+                                              D* __restrict__ czero, int cw, int rs) {
     // the unrolled form also fixes the decay mode per instance; the rolled one
     // keeps a single copy of the loop (two would cost registers)
     if (!kUnrolled)
-        process_strip_m<R, kGauss, ROWS, kCoherent, -1, false>(p, in, cin, out, czero, cw, rs);
+        process_strip_m<R, kGauss, ROWS, kCoherent, -1, false, D>(p, in, cin, out, czero, cw, rs);
     else if (p.decay_mode == SLIME_DECAY_MULTIPLY)
-        process_strip_m<R, kGauss, ROWS, kCoherent, (int)SLIME_DECAY_MULTIPLY, true>(p, in, cin, out, czero, cw, rs);
+        process_strip_m<R, kGauss, ROWS, kCoherent, (int)SLIME_DECAY_MULTIPLY, true, D>(p, in, cin, out, czero, cw,
+                                                                                     rs);
     else
-        process_strip_m<R, kGauss, ROWS, kCoherent, (int)SLIME_DECAY_REF_SUBTRACT, true>(p, in, cin, out, czero, cw, rs);
+        process_strip_m<R, kGauss, ROWS, kCoherent, (int)SLIME_DECAY_REF_SUBTRACT, true, D>(p, in, cin, out, czero,
+                                                                                         cw, rs);
 }
 
 

@@ -89,7 +89,7 @@ class SlimeOptions(C.Structure):
         ("l2_persist", C.c_uint32),
         ("trail_tile", C.c_uint32),
         ("agent_shape", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("exact_counts", C.c_uint32),
     ]
 
 

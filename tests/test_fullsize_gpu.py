@@ -46,7 +46,8 @@ def test_full_size_steps_bitexact(gpu, size):
     agents = agents_uniform(n, W, H, lo, hi, seed=11)
     trail = np.random.default_rng(12).random((H, W), dtype=np.float32)
     sim = make_sim(W, H, n, p, agents, trail)
-    sim.set_options(reorder_every=1)  # Morton order before every step
+    # Morton order before every step; counts kept for the comparison
+    sim.set_options(reorder_every=1, exact_counts=1)
     ca, ct = agents.copy(), trail.copy()
     del agents, trail
     for step in range(2):
@@ -63,7 +64,7 @@ def test_full_size_run_properties(gpu):
     p = bench_params(W, H, lo, hi, dist)
     agents = agents_uniform(n, W, H, lo, hi, seed=13)
     a = make_sim(W, H, n, p, agents)
-    a.set_options(reorder_every=50, graph_chunk=50)
+    a.set_options(reorder_every=50, graph_chunk=50, exact_counts=1)
     a.step(200)
     got = a.download_agents()
     counts = a.download_deposit_counts()
@@ -76,9 +77,10 @@ def test_full_size_run_properties(gpu):
     assert np.isfinite(trail).all() and trail.min() >= 0.0 and trail.max() <= 1.0
     assert (got[:, 2] >= 0).all() and (got[:, 2] < np.float32(2 * np.pi) + np.float32(1e-6)).all()
     assert (got[:, 0] >= 0).all() and (got[:, 0] <= W).all() and (got[:, 1] >= 0).all() and (got[:, 1] <= H).all()
-    # invariance: no reordering, no graphs, a different chunking -> the same bits
+    # invariance: no reordering, no graphs, a different chunking, the
+    # streaming trail kernel with deposit marks -> the same bits
     b = make_sim(W, H, n, p, agents)
-    b.set_options(reorder_every=0, use_graphs=0)
+    b.set_options(reorder_every=0, use_graphs=0, trail_tile=8)
     b.step(73)
     b.set_options(use_graphs=1, graph_chunk=31)
     b.step(127)

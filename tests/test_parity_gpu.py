@@ -48,6 +48,7 @@ def test_one_step_bitexact_random_trail(gpu, decay_mode, blur_mode):
     agents = agents_uniform(n, W, H, 30.0, 50.0, seed=1)
     trail = np.random.default_rng(2).random((H, W), dtype=np.float32)
     sim = make_sim(W, H, n, p, agents, trail)
+    sim.set_options(exact_counts=1)
     sim.step(1)
     ga, gt, gc = sim.download_agents(), sim.download_trail(), sim.download_deposit_counts()
     ca = agents.copy()
@@ -409,3 +410,73 @@ def test_l2_carveout_only_for_trails_that_fit(gpu):
     assert big.info().l2_persist_bytes == 0  # 256 MiB: more than any carve-out
     big.close()
     small.close()
+
+
+STREAM8 = 8  # 1 + the tile-table index of the 8-row streaming trail kernel
+
+
+@pytest.mark.parametrize("decay_mode,decay,dep", [(0, 10.0, 1.0), (1, 0.97, 1.0), (1, 0.9, 2.5), (0, 0.0, 1.0)])
+def test_deposit_marks_match_counts(gpu, decay_mode, decay, dep):
+    """Steps that record deposit marks (deposition >= 1 on a non-negative
+    trail) give the same bits as steps that count, and as the oracle."""
+    W, H, n = 512, 384, 150_000  # ~0.8 agents per cell: many cells with 2+ deposits
+    p = config0_params(W, H, decay_mode=decay_mode, blur_mode=1, decay_factor=decay,
+                       pheromone_deposition_amount=dep)
+    agents = agents_uniform(n, W, H, 1.0, 2.0, seed=31)
+    trail = np.random.default_rng(32).random((H, W), dtype=np.float32)
+    a = make_sim(W, H, n, p, agents, trail)
+    a.set_options(trail_tile=STREAM8, exact_counts=1)
+    b = make_sim(W, H, n, p, agents, trail)
+    b.set_options(trail_tile=STREAM8)
+    for chunk in (1, 7, 12):
+        a.step(chunk)
+        b.step(chunk)
+        assert_bitexact(b.download_trail(), a.download_trail(), f"trail, marks vs counts ({chunk})")
+        assert_bitexact(b.download_agents(), a.download_agents(), f"agents, marks vs counts ({chunk})")
+    a.download_deposit_counts()  # counting steps keep their counts
+    with pytest.raises(RuntimeError):
+        b.download_deposit_counts()  # marking steps have none
+    ca, ct = agents.copy(), trail.copy()
+    oracle.run(p, W, H, ca, ct, 20)
+    assert_bitexact(b.download_trail(), ct, "trail vs oracle")
+    assert_bitexact(b.download_agents(), ca, "agents vs oracle")
+
+
+def test_deposit_marks_only_when_every_deposit_saturates(gpu):
+    """Marks are used only while they cannot change a result: a trail with
+    negative or NaN values, a deposition below 1, or a growing multiplicative
+    decay keep the counts; a cleared trail brings the marks back."""
+    W, H, n = 256, 128, 30_000
+    agents = agents_uniform(n, W, H, 1.0, 2.0, seed=41)
+    rng = np.random.default_rng(42)
+    dirty = rng.random((H, W), dtype=np.float32) - np.float32(0.3)  # some cells negative
+    dirty[5, 7] = np.nan
+    cases = [
+        (config0_params(W, H), dirty, False),
+        (config0_params(W, H, pheromone_deposition_amount=0.5), np.abs(dirty), False),
+        (config0_params(W, H, decay_mode=1, decay_factor=1.5), np.abs(dirty[:, :]).clip(0, 1), False),
+        (config0_params(W, H), np.nan_to_num(np.abs(dirty)), True),
+    ]
+    for p, tr, marks in cases:
+        tr = np.ascontiguousarray(tr, np.float32)
+        sim = make_sim(W, H, n, p, agents, tr)
+        sim.set_options(trail_tile=STREAM8)
+        sim.step(3)
+        if marks:
+            with pytest.raises(RuntimeError):
+                sim.download_deposit_counts()
+        else:
+            sim.download_deposit_counts()
+        ca, ct = agents.copy(), tr.copy()
+        oracle.run(p, W, H, ca, ct, 3)
+        assert_bitexact(sim.download_trail(), ct, f"trail (marks={marks})")
+        assert_bitexact(sim.download_agents(), ca, f"agents (marks={marks})")
+    # clearing a dirty trail makes it clean again
+    sim = make_sim(W, H, n, config0_params(W, H), agents, np.ascontiguousarray(dirty))
+    sim.set_options(trail_tile=STREAM8)
+    sim.step(1)
+    sim.download_deposit_counts()
+    sim.clear_trail()
+    sim.step(1)
+    with pytest.raises(RuntimeError):
+        sim.download_deposit_counts()
