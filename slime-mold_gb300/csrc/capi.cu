@@ -346,11 +346,11 @@ bool keeps_trail_clean(const DevParams& d) {
 // (the streaming tiles read marks) and what it knows of the trail: clean
 // after creation, clear and resize, checked on upload, kept by steps that
 // keep it (keeps_trail_clean).
-bool use_marks(const slime_ctx* ctx) {
+bool marks_allowed(const slime_ctx* ctx) {
     if (ctx->opt.exact_counts || ctx->agents.n == 0 || !ctx->trail_clean) return false;
-    if (!(ctx->dev.dep >= 1.0f) || !keeps_trail_clean(ctx->dev)) return false;
-    return trail_tile_streams(ctx->dev, ctx->tile);
+    return ctx->dev.dep >= 1.0f && keeps_trail_clean(ctx->dev);
 }
+bool use_marks(const slime_ctx* ctx) { return marks_allowed(ctx) && trail_tile_streams(ctx->dev, ctx->tile); }
 
 // The record the next step writes (counts[cur] or marks[cur]) must start at
 // zero; a record left behind by steps of the other kind is cleared here,
@@ -1009,17 +1009,24 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
     // 1. trail tiles.  The trial launches read trail[cur] and the (zero)
     // counts[cur] and write the other buffers, so the state is untouched; the
     // previous step's counts are overwritten with zeros.
+    // Each tile runs with the deposit record the steps would use with it.
     float best = 1e30f;
     int best_tile = ctx->tile;
+    const bool marks_ok = marks_allowed(ctx);
     for (int t = 0; t < trail_tile_count(); t++) {
         if (!trail_tile_supported(ctx->dev, t)) continue;
-        cudaError_t e = launch_trail(ctx->dev, t, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                                     ctx->counts[1 - cur], ctx->stream); // warm-up
+        const bool mk = marks_ok && trail_tile_streams(ctx->dev, t);
+        auto trial = [&]() {
+            return mk ? launch_trail_marks(ctx->dev, t, ctx->trail[cur], ctx->marks[cur], ctx->trail[1 - cur],
+                                           ctx->marks[1 - cur], ctx->stream)
+                      : launch_trail(ctx->dev, t, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
+                                     ctx->counts[1 - cur], ctx->stream);
+        };
+        cudaError_t e = trial(); // warm-up
         if (e != cudaSuccess) continue;
+        (mk ? ctx->marks_dirty : ctx->counts_dirty)[1 - cur] = false; // zeroed by the trial
         cudaEventRecord(e0, ctx->stream);
-        for (uint32_t r = 0; r < reps; r++)
-            launch_trail(ctx->dev, t, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur], ctx->counts[1 - cur],
-                         ctx->stream);
+        for (uint32_t r = 0; r < reps; r++) trial();
         cudaEventRecord(e1, ctx->stream);
         CK(cudaEventSynchronize(e1), "autotuning");
         float ms = 0;

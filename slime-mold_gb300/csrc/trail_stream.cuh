@@ -32,16 +32,29 @@ __device__ __forceinline__ uint4 load_count4(const uint4* p) {
 }
 
 // The step's deposit record is either per-cell 32-bit counts or, when every
-// deposit saturates the fold, per-cell byte marks (0 or 1).  Both are read as
-// a count k of 32-bit width; a mark of 1 folds exactly as any k >= 1 does then.
+// deposit saturates the fold, per-cell byte marks (0 or 1).  A lane's four
+// cells come as a uint4 of counts or as one 32-bit word of four marks (one
+// register per row in flight instead of four); dep_at reads cell j of either
+// as a count k, and a mark of 1 folds exactly as any k >= 1 does then.
+template <class D>
+struct DepVec {
+    typedef uint4 type;
+};
+template <>
+struct DepVec<uint8_t> {
+    typedef uint32_t type;
+};
+__device__ __forceinline__ uint32_t dep_at(const uint4& k, int j) {
+    return j == 0 ? k.x : (j == 1 ? k.y : (j == 2 ? k.z : k.w));
+}
+__device__ __forceinline__ uint32_t dep_at(uint32_t k, int j) { return (k >> (8 * j)) & 0xffu; }
 template <bool kCoherent>
 __device__ __forceinline__ uint4 load_dep4(const uint32_t* p) {
     return load_count4<kCoherent>(reinterpret_cast<const uint4*>(p));
 }
 template <bool kCoherent>
-__device__ __forceinline__ uint4 load_dep4(const uint8_t* p) {
-    const uchar4 m = __ldg(reinterpret_cast<const uchar4*>(p));
-    return make_uint4(m.x, m.y, m.z, m.w);
+__device__ __forceinline__ uint32_t load_dep4(const uint8_t* p) {
+    return __ldg(reinterpret_cast<const unsigned int*>(p));
 }
 template <bool kCoherent>
 __device__ __forceinline__ uint32_t load_dep(const uint32_t* p) {
@@ -56,17 +69,17 @@ __device__ __forceinline__ void zero_dep4(uint8_t* p) { *reinterpret_cast<uchar4
 
 // One input row as a lane sees it: its four cells and, for the first lane and
 // the last active lane of the warp, the R wrapped halo cells on its open side.
-template <int R>
+template <int R, class D>
 struct RowFetch {
     float4 t;
-    uint4 k;
+    typename DepVec<D>::type k;
     float ht[R];
     uint32_t hk[R];
 };
 
 template <int R, bool kCoherent, class D>
 __device__ __forceinline__ void fetch_row(const DevParams& p, const float* __restrict__ in, const D* __restrict__ cin,
-                                          int row, int cl, bool has_halo, int hcol0, RowFetch<R>& f) {
+                                          int row, int cl, bool has_halo, int hcol0, RowFetch<R, D>& f) {
     const size_t base = (size_t)row * p.W;
     f.t = __ldg(reinterpret_cast<const float4*>(in + base + cl));
     f.k = load_dep4<kCoherent>(cin + base + cl);
@@ -91,13 +104,14 @@ __device__ __forceinline__ float fold_dep(float t, uint32_t k, float dep) {
     return fold_deposits(t, k, dep);
 }
 
-template <int R, int kDecay, bool kMarks>
-__device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch<R>& f, bool left_edge,
+template <int R, int kDecay, class D>
+__device__ __forceinline__ void build_ext_row(const DevParams& p, const RowFetch<R, D>& f, bool left_edge,
                                               bool right_edge, ExtRow<R>& e) {
-    float d[4] = {apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.x, f.k.x, p.dep)),
-                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.y, f.k.y, p.dep)),
-                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.z, f.k.z, p.dep)),
-                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.w, f.k.w, p.dep))};
+    constexpr bool kMarks = sizeof(D) == 1;
+    float d[4] = {apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.x, dep_at(f.k, 0), p.dep)),
+                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.y, dep_at(f.k, 1), p.dep)),
+                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.z, dep_at(f.k, 2), p.dep)),
+                  apply_decay_m<kDecay>(p, fold_dep<kMarks>(f.t.w, dep_at(f.k, 3), p.dep))};
 #pragma unroll
     for (int j = 0; j < 4; j++) e.v[R + j] = d[j];
 #pragma unroll
@@ -138,11 +152,13 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     ExtRow<R> win[NWIN];
     float hwin[NWIN][4];
 
-    // rows are fetched two ahead of their use, halo cells with them
+    // rows are fetched two ahead of their use, halo cells with them (three or
+    // four ahead measured slower: the registers cost more warps than the
+    // deeper prefetch hides)
     constexpr int NR = ROWS + 2 * R;
     const bool has_halo = active && (left_edge || right_edge);
     const int hcol0 = left_edge ? c0 - R : c0 + 4;
-    RowFetch<R> fa, fb;
+    RowFetch<R, D> fa, fb;
     fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R, H), cl, has_halo, hcol0, fa);
     fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + 1, H), cl, has_halo, hcol0, fb);
     // short strips unroll completely when asked to; long ones stay rolled
@@ -150,7 +166,7 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     constexpr int kUnroll = (kUnrolled && NR <= 12) ? NR : 1;
 #pragma unroll kUnroll
     for (int r = 0; r < NR; r++) {
-        RowFetch<R> cur = fa;
+        RowFetch<R, D> cur = fa;
         fa = fb;
         if (r + 2 < NR)
             fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + r + 2, H), cl, has_halo, hcol0, fb);
@@ -163,7 +179,7 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
                 for (int j = 0; j < 4; j++) hwin[q][j] = hwin[q + 1][j];
             }
         }
-        build_ext_row<R, kDecay, sizeof(D) == 1>(p, cur, left_edge && active, right_edge, win[NWIN - 1]);
+        build_ext_row<R, kDecay, D>(p, cur, left_edge && active, right_edge, win[NWIN - 1]);
         if (kGauss) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {

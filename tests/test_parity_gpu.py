@@ -415,8 +415,9 @@ def test_l2_carveout_only_for_trails_that_fit(gpu):
 STREAM8 = 8  # 1 + the tile-table index of the 8-row streaming trail kernel
 
 
+@pytest.mark.parametrize("tile", [STREAM8, 9, 10])
 @pytest.mark.parametrize("decay_mode,decay,dep", [(0, 10.0, 1.0), (1, 0.97, 1.0), (1, 0.9, 2.5), (0, 0.0, 1.0)])
-def test_deposit_marks_match_counts(gpu, decay_mode, decay, dep):
+def test_deposit_marks_match_counts(gpu, decay_mode, decay, dep, tile):
     """Steps that record deposit marks (deposition >= 1 on a non-negative
     trail) give the same bits as steps that count, and as the oracle."""
     W, H, n = 512, 384, 150_000  # ~0.8 agents per cell: many cells with 2+ deposits
@@ -425,9 +426,9 @@ def test_deposit_marks_match_counts(gpu, decay_mode, decay, dep):
     agents = agents_uniform(n, W, H, 1.0, 2.0, seed=31)
     trail = np.random.default_rng(32).random((H, W), dtype=np.float32)
     a = make_sim(W, H, n, p, agents, trail)
-    a.set_options(trail_tile=STREAM8, exact_counts=1)
+    a.set_options(trail_tile=tile, exact_counts=1)
     b = make_sim(W, H, n, p, agents, trail)
-    b.set_options(trail_tile=STREAM8)
+    b.set_options(trail_tile=tile)
     for chunk in (1, 7, 12):
         a.step(chunk)
         b.step(chunk)
