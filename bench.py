@@ -72,7 +72,7 @@ def trail_kernel_name(tile, blur_mode):
 TRAFFIC_PROFILES = {
     ("plain-4096", "agents_persistent_kernel"): "agents_kernel_plain-4096.md",
     ("plain-4096", "trail_stream_kernel"): "trail_stream_kernel_plain-4096.md",
-    ("plain-8192", "agents_kernel"): "agents_kernel_plain-8192.md",
+    ("plain-8192", "agents_persistent_kernel"): "agents_kernel_plain-8192.md",
     ("plain-8192", "trail_stream_kernel"): "trail_stream_kernel_plain-8192.md",
 }
 
