@@ -11,6 +11,18 @@ from test_oracle import fd4
 
 pytestmark = pytest.mark.gpu
 
+# Parameter gradients: within 1e-6 relative of the binary64 references (the
+# target for this adjoint; measured up to 5.3e-7).  A reference of exactly 0
+# (a deposition on the clamp kink) must come out 0.
+REL = 1e-6
+
+
+def assert_rel(got, ref, what, tol=REL):
+    if ref == 0.0:
+        assert got == 0.0, (what, got, ref)
+    else:
+        assert abs(got - ref) <= tol * abs(ref), (what, got, ref, abs(got - ref) / abs(ref))
+
 
 def run_case(W, H, n, steps, K, dm, bm, dep, seed=0, radius=1.0, t_lo=0.0):
     import slime_gb300 as sg
@@ -45,8 +57,9 @@ def test_adjoint_matches_binary64_adjoint(gpu, dm, bm, dep):
     p, t0, counts, theta, grads, d0, ref, d0_ref, g = run_case(W, H, 2000, 37, 10, dm, bm, dep)
     got = [grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount]
     for i in range(3):
-        assert abs(got[i] - ref[i]) <= 1e-5 * max(1.0, abs(ref[i])), (i, got[i], ref[i])
-    assert np.abs(d0 - d0_ref).max() <= 1e-5 * max(1.0, np.abs(d0_ref).max())
+        assert_rel(got[i], ref[i], f"parameter {i}")
+    # the initial-trail gradient, relative to its largest entry
+    assert np.abs(d0 - d0_ref).max() <= REL * np.abs(d0_ref).max()
 
 
 def test_adjoint_matches_finite_differences(gpu):
@@ -66,7 +79,7 @@ def test_adjoint_matches_finite_differences(gpu):
 
     for i in range(3):
         fd = fd4(lin_loss, theta, i, h)
-        assert abs(got[i] - fd) <= 1e-5 * max(1.0, abs(fd)), (i, got[i], fd)
+        assert_rel(got[i], fd, f"parameter {i} vs finite differences")
     assert target is None
 
 
@@ -75,7 +88,7 @@ def test_adjoint_radius2_and_ragged_segments(gpu):
     p, t0, counts, theta, grads, d0, ref, d0_ref, g = run_case(W, H, 900, 23, 5, 1, 1, 0.2, seed=5, radius=2.0)
     got = [grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount]
     for i in range(3):
-        assert abs(got[i] - ref[i]) <= 1e-5 * max(1.0, abs(ref[i])), (i, got[i], ref[i])
+        assert_rel(got[i], ref[i], f"parameter {i} (radius 2)")
 
 
 def test_backward_without_record_is_an_error(gpu):
@@ -106,8 +119,10 @@ def test_autograd_function_role(gpu):
         loss.backward()
     counts = oracle.run(p, W, H, agents.copy(), t0.detach().numpy().copy(), steps, record_counts=True)
     theta = [float(np.float32(0.97)), float(np.float32(0.5)), float(np.float32(0.05))]
-    _, ref, d0_ref = oracle.chain_adjoint_f64(p, W, H, *theta, t0.detach().numpy(), counts,
-                                              target=target.numpy().astype(np.float64))
-    for got, want in zip((decay.grad, rate.grad, dep.grad), ref):
-        assert abs(float(got) - want) <= 1e-5 * max(1.0, abs(want))
-    assert np.abs(t0.grad.numpy() - d0_ref).max() <= 1e-5 * max(1.0, np.abs(d0_ref).max())
+    # dL/dT_n of the loss at the binary32 forward the GPU ran (the adjoint's
+    # input), carried back by the binary64 adjoint
+    g_final = (out.detach() - target).numpy().astype(np.float64)
+    _, ref, d0_ref = oracle.chain_adjoint_f64(p, W, H, *theta, t0.detach().numpy(), counts, g_final=g_final)
+    for i, (got, want) in enumerate(zip((decay.grad, rate.grad, dep.grad), ref)):
+        assert_rel(float(got), want, f"parameter {i}")
+    assert np.abs(t0.grad.numpy() - d0_ref).max() <= REL * np.abs(d0_ref).max()
