@@ -114,8 +114,12 @@ __device__ __forceinline__ void steps4(const DevParams& sp, float4& x, float4& y
     }
 }
 
+// Four blocks per SM (64 registers, a few bytes spilled by the strip phase):
+// 3.33 ms per step on 64 colonies against 3.49 with the three blocks that the
+// uncapped register use allows; two agents per thread instead of four were
+// slower again (3.44 ms).
 template <int R, bool kGauss, int ROWS>
-__global__ void __launch_bounds__(kEnsThreads) ensemble_step_kernel(
+__global__ void __launch_bounds__(kEnsThreads, 4) ensemble_step_kernel(
     const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
     const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
     float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS, const float* __restrict__ trail_in,
