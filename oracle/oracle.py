@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg, as the checker or the timed CPU baseline.
-Parity is unpinned: the reference has no tests or golden vectors and cannot
-run on this machine (see slime_oracle.cpp).
+Pinned against a mechanical C++ translation of the reference's own shader
+(oracle/wgsl/, tests/test_reference_pin.py; see slime_oracle.cpp).
 """
 import ctypes as C
 import os
@@ -51,6 +51,10 @@ def lib():
         L.oracle_num_threads.restype = C.c_int
         L.oracle_sincos.argtypes = [f32, C.c_uint64, f32, f32]
         L.oracle_ph_window_mismatches.argtypes = [C.c_uint32, C.c_uint32]
+        L.oracle_sample.argtypes = [f32, C.c_uint32, C.c_uint32, f32, f32, C.c_uint64, f32]
+        L.oracle_sample.restype = None
+        L.oracle_sense.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_uint64, f32, f32, f32]
+        L.oracle_sense.restype = None
         L.oracle_ph_window_mismatches.restype = C.c_uint64
         L.oracle_jitter_hash.argtypes = [C.POINTER(C.c_int32), f32, f32, C.c_uint64, f32]
         L.oracle_uniform01.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, f32]
@@ -135,6 +139,26 @@ def colorize(W, H, trail, lut768, tw, th):
     lut = np.ascontiguousarray(lut768, np.uint8).reshape(-1)
     out = np.empty((th, tw, 4), np.uint8)
     lib().oracle_colorize(W, H, _p(tr, C.c_float), _p(lut, C.c_uint8), tw, th, _p(out, C.c_uint8))
+    return out
+
+
+def sample(trail, px, py):
+    """sample_trail_map (compute.wgsl:7-29) at positions (px, py)."""
+    t = np.ascontiguousarray(trail, np.float32)
+    H, W = t.shape
+    x = np.ascontiguousarray(px, np.float32)
+    y = np.ascontiguousarray(py, np.float32)
+    out = np.empty(x.size, np.float32)
+    lib().oracle_sample(_p(t, C.c_float), W, H, _p(x, C.c_float), _p(y, C.c_float), x.size, _p(out, C.c_float))
+    return out
+
+
+def sense(params, W, H, agents, trail):
+    """The (left, right, centre) sensor samples of each agent (compute.wgsl:74-95)."""
+    a = np.ascontiguousarray(agents, np.float32)
+    t = np.ascontiguousarray(trail, np.float32).reshape(-1)
+    out = np.empty((a.shape[0], 3), np.float32)
+    lib().oracle_sense(C.byref(params), W, H, a.shape[0], _p(a, C.c_float), _p(t, C.c_float), _p(out, C.c_float))
     return out
 
 

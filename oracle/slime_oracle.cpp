@@ -4,12 +4,17 @@
  * this library, always as the checker or as the timed CPU baseline, never as
  * part of the product path.
  *
- * PARITY UNPINNED.  The reference (Velfi/slime-mold) has no tests, golden
- * vectors or fixtures, and it cannot run here (it is a Rust/wgpu GUI binary;
- * this machine has neither a Rust toolchain nor a graphics stack).  This file
- * is a line-by-line binary32 restatement of the reference shader
- * src/compute.wgsl, checked instead against hand-derived known answers and
- * against an independent pure-Python restatement (tests/golden).
+ * PINNED AGAINST THE REFERENCE'S OWN SHADER.  The reference (Velfi/slime-mold)
+ * has no tests, golden vectors or fixtures, and its Rust/wgpu program cannot
+ * run here.  This file is a line-by-line binary32 restatement of
+ * src/compute.wgsl; oracle/wgsl/ translates that shader mechanically to C++
+ * and runs it invocation by invocation, and tests/test_reference_pin.py and
+ * the frames in tests/golden/wgsl/ show this restatement equal to it bit for
+ * bit (sampler, decay, diffuse, agent update, whole frames where the shader
+ * does not race), the one difference being the side sensors' directions
+ * (rotations of the centre direction here, a few ulp from the shader's
+ * cos/sin of the shifted angle).  Also checked against hand-derived known
+ * answers and an independent pure-Python restatement (tests/golden).
  *
  * What it restates:
  *   sample_trail_map       compute.wgsl:7-29
@@ -63,19 +68,11 @@ inline float sample_trail_map(const float* trail, int32_t W, int32_t H, float px
     return slm_mix(v0, v1, dy);
 }
 
-/* The agent invocation "main", compute.wgsl:57-145, for agent `index`.
- * Returns the deposit cell or -1. */
-inline int64_t agent_update(const SlimeParams* p, int32_t W, int32_t H, int32_t index, float* a,
-                            const float* trail) {
-    float x = a[0];
-    float y = a[1];
-    float angle = a[2];
-    float speed = a[3];
-
-    speed = slm_clamp(speed, p->agent_speed_min, p->agent_speed_max); /* :72 */
-
-    /* :75-77 sensor angles angle - a, angle + a, angle; their cos/sin as the
-     * centre direction and its rotations by -a and +a (slm_sensor_dirs) */
+/* The three sensor samples of compute.wgsl:75-95 for an agent at (x, y)
+ * heading `angle`: sensor angles angle - a, angle + a, angle; their cos/sin
+ * as the centre direction and its rotations by -a and +a (slm_sensor_dirs). */
+inline void sense(const SlimeParams* p, int32_t W, int32_t H, float x, float y, float angle, const float* trail,
+                  float* left_value, float* right_value, float* center_value) {
     float dist = p->agent_sensor_distance;
     float sa, ca;
     slm_sincos(p->agent_sensor_angle, &sa, &ca);
@@ -87,10 +84,24 @@ inline int64_t agent_update(const SlimeParams* p, int32_t W, int32_t H, int32_t 
     float rpy = slm_add(y, slm_mul(dist, sr));
     float cpx = slm_add(x, slm_mul(dist, cc)); /* :87-90 */
     float cpy = slm_add(y, slm_mul(dist, sc));
+    *left_value = sample_trail_map(trail, W, H, lpx, lpy);   /* :93 */
+    *right_value = sample_trail_map(trail, W, H, rpx, rpy);  /* :94 */
+    *center_value = sample_trail_map(trail, W, H, cpx, cpy); /* :95 */
+}
 
-    float left_value = sample_trail_map(trail, W, H, lpx, lpy);   /* :93 */
-    float right_value = sample_trail_map(trail, W, H, rpx, rpy);  /* :94 */
-    float center_value = sample_trail_map(trail, W, H, cpx, cpy); /* :95 */
+/* The agent invocation "main", compute.wgsl:57-145, for agent `index`.
+ * Returns the deposit cell or -1. */
+inline int64_t agent_update(const SlimeParams* p, int32_t W, int32_t H, int32_t index, float* a,
+                            const float* trail) {
+    float x = a[0];
+    float y = a[1];
+    float angle = a[2];
+    float speed = a[3];
+
+    speed = slm_clamp(speed, p->agent_speed_min, p->agent_speed_max); /* :72 */
+
+    float left_value, right_value, center_value;
+    sense(p, W, H, x, y, angle, trail, &left_value, &right_value, &center_value);
 
     if (center_value > left_value && center_value > right_value) { /* :98 */
         /* continue straight */
@@ -533,6 +544,21 @@ void oracle_colorize(uint32_t W, uint32_t H, const float* trail, const uint8_t* 
 }
 
 int oracle_num_threads(void) { return resolve_threads(0); }
+
+/* The sensor samples (left, right, centre) of n agents, 3 floats each (the
+ * tests pin them against the reference). */
+void oracle_sense(const SlimeParams* p, uint32_t W, uint32_t H, uint64_t n, const float* agents, const float* trail,
+                  float* out) {
+    for (uint64_t i = 0; i < n; i++)
+        sense(p, (int32_t)W, (int32_t)H, agents[4 * i], agents[4 * i + 1], agents[4 * i + 2], trail, &out[3 * i],
+              &out[3 * i + 1], &out[3 * i + 2]);
+}
+
+/* sample_trail_map at n positions (the tests pin it against the reference). */
+void oracle_sample(const float* trail, uint32_t W, uint32_t H, const float* px, const float* py, uint64_t n,
+                   float* out) {
+    for (uint64_t i = 0; i < n; i++) out[i] = sample_trail_map(trail, (int32_t)W, (int32_t)H, px[i], py[i]);
+}
 
 /* The shared builtins, exported so the tests can check them. */
 void oracle_sincos(const float* x, uint64_t n, float* s, float* c) {

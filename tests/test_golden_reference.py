@@ -1,0 +1,78 @@
+"""Golden frames from the reference's own compute shader (tests/golden/wgsl/,
+made by tests/golden/make_reference_golden.py from a mechanical C++
+translation of src/compute.wgsl run invocation by invocation): the CPU
+oracle (always) and the CUDA path (gpu) must reproduce each saved frame bit
+for bit, agents and trail; in `single_deposit_cells` cases the trail is
+compared on the cells at most one agent landed on, the only cells whose
+value the shader's non-atomic deposit defines."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import ROOT
+
+FIXTURES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "wgsl", "*.npz")))
+KEYS = ["decay_factor", "agent_jitter", "agent_speed_min", "agent_speed_max", "agent_turn_speed",
+        "agent_sensor_angle", "agent_sensor_distance", "diffusion_rate", "pheromone_deposition_amount",
+        "blur_radius", "blur_sigma", "time_step", "decay_mode", "blur_mode"]
+
+
+def load(path):
+    from slime_gb300 import SlimeParams
+    d = dict(np.load(path))
+    p = SlimeParams()
+    p.width, p.height = int(d["W"]), int(d["H"])
+    for k in KEYS:
+        setattr(p, k, d["p_" + k].item())
+    return d, p
+
+
+def check(d, s, agents, trail, counts):
+    assert np.array_equal(agents.view(np.uint32), d[f"agents{s}"].view(np.uint32)), f"agents frame {s}"
+    ref = d[f"trail{s}"]
+    if str(d["compare"]) == "all":
+        assert np.array_equal(trail.view(np.uint32), ref.view(np.uint32)), f"trail frame {s}"
+    else:
+        single = counts <= 1
+        assert np.count_nonzero(single) > single.size // 2
+        assert np.array_equal(trail[single].view(np.uint32), ref[single].view(np.uint32)), f"trail frame {s}"
+
+
+def test_fixtures_present():
+    assert len(FIXTURES) == 3
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p))
+def test_oracle_reproduces_reference_frames(path):
+    d, p = load(path)
+    W, H = int(d["W"]), int(d["H"])
+    a, t = d["agents0"].copy(), d["trail0"].copy()
+    done = 0
+    for s in d["frames"].tolist():
+        while done < s:
+            c = oracle.agents_pass(p, W, H, a, t)
+            t = oracle.trail_pass(p, W, H, t, c)
+            done += 1
+        check(d, s, a, t, c)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p))
+def test_gpu_reproduces_reference_frames(gpu, path):
+    import slime_gb300 as sg
+    d, p = load(path)
+    W, H = int(d["W"]), int(d["H"])
+    with sg.Simulation(W, H, d["agents0"].shape[0], p) as sim:
+        sim.set_options(exact_counts=1)
+        sim.upload_agents(d["agents0"])
+        sim.upload_trail(d["trail0"])
+        done = 0
+        for s in d["frames"].tolist():
+            if s - 1 > done:
+                sim.step(s - 1 - done)
+            sim.step(1)  # the counts of the saved frame's own step
+            done = s
+            check(d, s, sim.download_agents(), sim.download_trail(), sim.download_deposit_counts())
