@@ -64,6 +64,16 @@ extern "C" {
 #define SLIME_BLUR_REF_BOX3 0u /* 3x3 toroidal box, summed in shader order, /9 */
 #define SLIME_BLUR_GAUSS 1u    /* separable Gaussian, radius blur_radius, sigma blur_sigma */
 #define SLIME_MAX_BLUR_RADIUS 8
+/* Which agents the agent pass updates.  The reference dispatches
+ * wx x wy workgroups of 64 invocations, wx = min(ceil(n / 64), 65535),
+ * wy = ceil(ceil(n / 64) / wx) (src/main.rs:1174-1178), and invocation
+ * (gx, gy) updates agent gx + 65535 gy (compute.wgsl:60): for n > 4,194,240
+ * agents the highest ones are never updated and some are updated by several
+ * invocations. */
+#define SLIME_DISPATCH_EACH_AGENT 0u /* every agent once per step (the intended reading) */
+#define SLIME_DISPATCH_REFERENCE 1u  /* the reference's dispatch: an agent visited by m invocations
+                                        moves once (every visit reads the state the pass found)
+                                        and deposits m times; m = 0 leaves it as it is */
 
 /* ------------------------------------------------------------ parameters */
 /* The first 14 fields are SimSizeUniform (src/main.rs:29-46) in the same
@@ -88,7 +98,7 @@ typedef struct SlimeParams {
     float time_step;     /* TIME_STEP, compute.wgsl:55 (0.016) */
     uint32_t decay_mode; /* SLIME_DECAY_* */
     uint32_t blur_mode;  /* SLIME_BLUR_* */
-    uint32_t reserved;   /* must be 0 */
+    uint32_t dispatch_mode; /* SLIME_DISPATCH_* (0, every agent once, is the default) */
 } SlimeParams;
 
 /* Settings (src/settings.rs:30-47), field for field. */

@@ -355,6 +355,24 @@ SLM_FN float slm_sin(float x) { float s, c; slm_sincos(x, &s, &c); return s; }
 SLM_FN float slm_cos(float x) { float s, c; slm_sincos(x, &s, &c); return c; }
 
 /* ---------------------------------------------- composite shader pieces */
+/* How many invocations of the reference's agent dispatch update agent
+ * `index` of `n` (compute.wgsl:60 with src/main.rs:1174-1178): wx x wy
+ * workgroups of 64, wx = min(ceil(n / 64), 65535), wy = ceil(ceil(n / 64) / wx);
+ * invocation (gx, gy), gx < 64 wx, gy < wy, updates agent gx + 65535 gy, so
+ * agent i is visited once for each gy < wy with gy 65535 <= i < gy 65535 + 64 wx.
+ * Every agent once for n <= 4,194,240; for n < 2^31 the shader's u32 index
+ * neither wraps nor turns negative as an i32. */
+SLM_FN uint32_t slm_dispatch_visits(uint64_t n, uint64_t index) {
+    if (index >= n) return 0;
+    const uint64_t groups = (n + 63) / 64;
+    const uint64_t wx = groups < 65535 ? groups : 65535;
+    const uint64_t wy = (groups + wx - 1) / wx;
+    const uint64_t span = 64 * wx;
+    const uint64_t hi = index / 65535 < wy - 1 ? index / 65535 : wy - 1; /* gy 65535 <= index */
+    const uint64_t lo = index >= span ? (index - span) / 65535 + 1 : 0;  /* index < gy 65535 + span */
+    return hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+}
+
 /* Sensor directions of compute.wgsl:79-90: cos/sin of angle - a, angle + a
  * and angle.  The centre direction is slm_sincos(angle); the side directions
  * are that vector rotated by -a and +a with (sin a, cos a) =

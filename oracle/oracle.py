@@ -55,6 +55,8 @@ def lib():
         L.oracle_sample.restype = None
         L.oracle_sense.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_uint64, f32, f32, f32]
         L.oracle_sense.restype = None
+        L.oracle_dispatch_visits.argtypes = [C.c_uint64, C.POINTER(C.c_uint64), C.c_uint64, u32]
+        L.oracle_dispatch_visits.restype = None
         L.oracle_ph_window_mismatches.restype = C.c_uint64
         L.oracle_jitter_hash.argtypes = [C.POINTER(C.c_int32), f32, f32, C.c_uint64, f32]
         L.oracle_uniform01.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, f32]
@@ -159,6 +161,15 @@ def sense(params, W, H, agents, trail):
     t = np.ascontiguousarray(trail, np.float32).reshape(-1)
     out = np.empty((a.shape[0], 3), np.float32)
     lib().oracle_sense(C.byref(params), W, H, a.shape[0], _p(a, C.c_float), _p(t, C.c_float), _p(out, C.c_float))
+    return out
+
+
+def dispatch_visits(n, index):
+    """How many invocations of the reference's agent dispatch update each of
+    `index` among n agents (slm_dispatch_visits)."""
+    idx = np.ascontiguousarray(index, np.uint64).reshape(-1)
+    out = np.empty(idx.size, np.uint32)
+    lib().oracle_dispatch_visits(n, _p(idx, C.c_uint64), idx.size, _p(out, C.c_uint32))
     return out
 
 

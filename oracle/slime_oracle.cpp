@@ -189,17 +189,23 @@ extern "C" {
 
 /* One agent pass over AoS agents (x, y, angle, speed), reading `trail` and
  * adding 1 to counts[cell] for every deposit.  ids[i] (or i when ids is NULL)
- * is the agent_index that seeds the jitter hash. */
+ * is the agent_index that seeds the jitter hash.  With SLIME_DISPATCH_REFERENCE
+ * an agent that the reference's dispatch visits m times (compute.wgsl:60,
+ * src/main.rs:1174-1178; slm_dispatch_visits) is updated once from the state
+ * the pass found and deposits m times; m = 0 leaves it untouched. */
 void oracle_agents_pass(const SlimeParams* p, uint32_t W, uint32_t H, uint64_t n, float* agents,
                         const uint32_t* ids, const float* trail, uint32_t* counts, int threads) {
     int nt = resolve_threads(threads);
+    const bool ref_dispatch = p->dispatch_mode == SLIME_DISPATCH_REFERENCE;
 #pragma omp parallel for schedule(static) num_threads(nt)
     for (int64_t i = 0; i < (int64_t)n; i++) {
         int32_t index = ids ? (int32_t)ids[i] : (int32_t)i;
+        uint32_t visits = ref_dispatch ? slm_dispatch_visits(n, (uint64_t)(uint32_t)index) : 1u;
+        if (visits == 0) continue;
         int64_t cell = agent_update(p, (int32_t)W, (int32_t)H, index, agents + 4 * i, trail);
         if (cell >= 0) {
 #pragma omp atomic
-            counts[cell] += 1u;
+            counts[cell] += visits;
         }
     }
 }
@@ -552,6 +558,11 @@ void oracle_sense(const SlimeParams* p, uint32_t W, uint32_t H, uint64_t n, cons
     for (uint64_t i = 0; i < n; i++)
         sense(p, (int32_t)W, (int32_t)H, agents[4 * i], agents[4 * i + 1], agents[4 * i + 2], trail, &out[3 * i],
               &out[3 * i + 1], &out[3 * i + 2]);
+}
+
+/* slm_dispatch_visits(n, index[i]) for m indices. */
+void oracle_dispatch_visits(uint64_t n, const uint64_t* index, uint64_t m, uint32_t* out) {
+    for (uint64_t i = 0; i < m; i++) out[i] = slm_dispatch_visits(n, index[i]);
 }
 
 /* sample_trail_map at n positions (the tests pin it against the reference). */

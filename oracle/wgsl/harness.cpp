@@ -16,6 +16,11 @@
 //   wref_diffuse  `diffuse_trail` over every cell, Jacobi-style (reads from
 //                 `in`, writes `out`), the race-free reading of the in-place
 //                 pass;
+//   wref_agents_dispatch
+//                 `main` over the reference's own dispatch grid
+//                 (src/main.rs:1174-1178: wx x wy workgroups of 64,
+//                 invocation id (gx, gy, 0)), agents and trail both read
+//                 as the pass found them, writes going to the live arrays;
 //   wref_sense    the three sensor samples `main` takes (compute.wgsl:74-95,
 //                 restated here in the prelude's WGSL operations because
 //                 `main` keeps them in locals), to tell a flipped turn
@@ -87,6 +92,37 @@ void wref_agents(const SlimeParams* p, float* agents, uint64_t n, float* trail, 
     ref::agents.src = nullptr;
     ref::agents.length = (uint32_t)n;
     for (uint64_t i = 0; i < n; i++) ref::wgsl_main(ref::vec3u{(uint32_t)i, 0u, 0u});
+    for (uint64_t i = 0; i < n; i++) {
+        agents[4 * i] = a[i].x.v;
+        agents[4 * i + 1] = a[i].y.v;
+        agents[4 * i + 2] = a[i].z.v;
+        agents[4 * i + 3] = a[i].w.v;
+    }
+    for (size_t i = 0; i < cells; i++) trail[i] = t[i].v;
+}
+
+void wref_agents_dispatch(const SlimeParams* p, float* agents, uint64_t n, float* trail) {
+    bind_uniform(p);
+    const size_t cells = (size_t)p->width * p->height;
+    std::vector<wgsl::f32> t(cells);
+    for (size_t i = 0; i < cells; i++) t[i] = wgsl::f32(trail[i]);
+    const std::vector<wgsl::f32> snap = t;
+    bind_trail(t.data(), snap.data(), cells);
+    std::vector<ref::vec4f> a(n);
+    for (uint64_t i = 0; i < n; i++)
+        a[i] = ref::vec4f{wgsl::f32(agents[4 * i]), wgsl::f32(agents[4 * i + 1]), wgsl::f32(agents[4 * i + 2]),
+                          wgsl::f32(agents[4 * i + 3])};
+    const std::vector<ref::vec4f> a0 = a;
+    ref::agents.data = a.data();
+    ref::agents.src = a0.data();
+    ref::agents.length = (uint32_t)n;
+    /* src/main.rs:1174-1178 */
+    const uint32_t workgroup_size = 64u;
+    const uint32_t total = (uint32_t)((n + workgroup_size - 1) / workgroup_size);
+    const uint32_t wx = total < 65535u ? total : 65535u;
+    const uint32_t wy = wx ? (total + wx - 1) / wx : 0u;
+    for (uint32_t gy = 0; gy < wy; gy++)
+        for (uint32_t gx = 0; gx < wx * workgroup_size; gx++) ref::wgsl_main(ref::vec3u{gx, gy, 0u});
     for (uint64_t i = 0; i < n; i++) {
         agents[4 * i] = a[i].x.v;
         agents[4 * i + 1] = a[i].y.v;

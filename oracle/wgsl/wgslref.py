@@ -43,7 +43,8 @@ def lib():
         L.wref_decay.argtypes = [SP, f32]
         L.wref_diffuse.argtypes = [SP, f32, f32]
         L.wref_sense.argtypes = [SP, f32, C.c_uint64, f32, f32]
-        for f in (L.wref_sample, L.wref_agents, L.wref_decay, L.wref_diffuse, L.wref_sense):
+        L.wref_agents_dispatch.argtypes = [SP, f32, C.c_uint64, f32]
+        for f in (L.wref_sample, L.wref_agents, L.wref_decay, L.wref_diffuse, L.wref_sense, L.wref_agents_dispatch):
             f.restype = None
         _lib = L
     return _lib
@@ -70,6 +71,16 @@ def agents_pass(params, agents, trail):
     a = np.ascontiguousarray(agents, np.float32).copy()
     t = np.ascontiguousarray(trail, np.float32).copy()
     lib().wref_agents(C.byref(params), _p(a), a.shape[0], _p(t), 1)
+    return a, t
+
+
+def agents_pass_dispatch(params, agents, trail):
+    """`main` over the reference's own dispatch grid (wx x wy workgroups of
+    64, src/main.rs:1174-1178), agents and trail read as the pass found them;
+    a deposit writes clamp(that value + dep, 0, 1)."""
+    a = np.ascontiguousarray(agents, np.float32).copy()
+    t = np.ascontiguousarray(trail, np.float32).copy()
+    lib().wref_agents_dispatch(C.byref(params), _p(a), a.shape[0], _p(t))
     return a, t
 
 

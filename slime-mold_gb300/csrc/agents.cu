@@ -239,6 +239,48 @@ __global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
     }
 }
 
+// The reference's own dispatch (SLIME_DISPATCH_REFERENCE): agent `id` is
+// visited by slm_dispatch_visits(n, id) invocations of compute.wgsl:60's
+// indexing.  No visit leaves the agent as it is; m >= 1 visits move it once
+// (each visit reads the state the pass found, so all compute the same update)
+// and deposit m times.  One agent per thread: a compatibility mode, untuned.
+template <bool kIds, class Trail>
+__global__ void __launch_bounds__(256) agents_dispatch_kernel(const __grid_constant__ DevParams p,
+                                                              float* __restrict__ X, float* __restrict__ Y,
+                                                              float* __restrict__ TH, float* __restrict__ V,
+                                                              const uint32_t* __restrict__ ids, const Trail trail,
+                                                              uint32_t* __restrict__ counts,
+                                                              uint8_t* __restrict__ marks, uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = kIds ? ids[i] : (uint32_t)i;
+    const uint32_t m = slm_dispatch_visits(n, id);
+    if (m == 0) return;
+    float x = X[i], y = Y[i], th = TH[i], v = V[i];
+    const int cell = agent_step(p, x, y, th, v, (int32_t)id, trail);
+    if (cell >= 0) {
+        if (marks)
+            atomicOr(reinterpret_cast<unsigned*>(marks + (cell & ~3)), 1u << (8 * (cell & 3)));
+        else
+            atomicAdd(counts + cell, m);
+    }
+    X[i] = x;
+    Y[i] = y;
+    TH[i] = th;
+    V[i] = v;
+}
+
+template <class Trail>
+cudaError_t launch_agents_dispatch(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
+                                   uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win) {
+    const dim3 grid(blocks_for(a.n, 256));
+    if (a.ids)
+        return launch_k(agents_dispatch_kernel<true, Trail>, grid, dim3(256), 0, s, win, p, a.x, a.y, a.th, a.v,
+                        (const uint32_t*)a.ids, trail, counts, marks, a.n);
+    return launch_k(agents_dispatch_kernel<false, Trail>, grid, dim3(256), 0, s, win, p, a.x, a.y, a.th, a.v,
+                    (const uint32_t*)nullptr, trail, counts, marks, a.n);
+}
+
 template <int APT, int BS, int MINB, class Trail>
 cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
                                      uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win) {
@@ -300,6 +342,9 @@ cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* t
                           uint8_t* marks) {
     if (a.n == 0) return cudaSuccess;
     const TrailPtr tp{trail};
+    if (p.dispatch_mode == SLIME_DISPATCH_REFERENCE)
+        return tex ? launch_agents_dispatch(p, a, TrailTex{tex}, counts, marks, s, win)
+                   : launch_agents_dispatch(p, a, tp, counts, marks, s, win);
     if (agent_shape_uses_texture(shape) && tex) {
         const TrailTex tt{tex};
         switch (shape) {

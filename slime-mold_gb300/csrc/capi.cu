@@ -56,8 +56,8 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
         *why = "unknown blur_mode";
         return false;
     }
-    if (p.reserved != 0) {
-        *why = "params.reserved must be 0";
+    if (p.dispatch_mode > SLIME_DISPATCH_REFERENCE) {
+        *why = "unknown dispatch_mode";
         return false;
     }
     DevParams d;
@@ -80,6 +80,7 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
     d.rate = slm_clamp(p.diffusion_rate, 0.0f, 1.0f);     // compute.wgsl:173
     d.decay_mode = p.decay_mode;
     d.blur_mode = p.blur_mode;
+    d.dispatch_mode = p.dispatch_mode;
     d.R = 1;
     if (p.blur_mode == SLIME_BLUR_GAUSS) {
         if (!isfinite(p.blur_radius) || !isfinite(p.blur_sigma)) {

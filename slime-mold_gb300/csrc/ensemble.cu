@@ -462,6 +462,10 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
             e->err = why;
             break;
         }
+        if (params[j].dispatch_mode != SLIME_DISPATCH_EACH_AGENT) {
+            e->err = "the reference dispatch mode is available on single-colony contexts only";
+            break;
+        }
         int R = params[j].blur_mode == SLIME_BLUR_GAUSS ? c.dev.R : 1;
         if (R < 1 || R > 2) {
             e->err = "ensemble blur radius must be 1 or 2";
@@ -577,6 +581,9 @@ int slime_ensemble_set_params(slime_ensemble* e, uint32_t j, const SlimeParams* 
     DevParams d;
     const char* why = nullptr;
     if (!make_dev_params(*params, c.W, c.H, &d, &why)) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, why);
+    if (params->dispatch_mode != SLIME_DISPATCH_EACH_AGENT)
+        return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT,
+                        "the reference dispatch mode is available on single-colony contexts only");
     int R = params->blur_mode == SLIME_BLUR_GAUSS ? d.R : 1;
     if (R != e->R || e->gauss != (params->blur_mode == SLIME_BLUR_GAUSS))
         return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "all colonies must share blur mode and radius");

@@ -129,7 +129,7 @@ void slime_params_from_settings(const SlimeSettings* s, uint32_t width, uint32_t
     out->time_step = 0.016f; // TIME_STEP, compute.wgsl:55
     out->decay_mode = SLIME_DECAY_REF_SUBTRACT;
     out->blur_mode = SLIME_BLUR_REF_BOX3;
-    out->reserved = 0;
+    out->dispatch_mode = SLIME_DISPATCH_EACH_AGENT;
 }
 
 } // extern "C"

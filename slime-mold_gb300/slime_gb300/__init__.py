@@ -12,13 +12,15 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from ._abi import (BLUR_GAUSS, BLUR_REF_BOX3, DECAY_MULTIPLY, DECAY_REF_SUBTRACT, MAX_BLUR_RADIUS, SlimeGrads,
+from ._abi import (BLUR_GAUSS, BLUR_REF_BOX3, DECAY_MULTIPLY, DECAY_REF_SUBTRACT, DISPATCH_EACH_AGENT,
+                   DISPATCH_REFERENCE, MAX_BLUR_RADIUS, SlimeGrads,
                    SlimeInfo, SlimeOptions, SlimeParams, SlimeSettings)
 
 __all__ = [
     "SlimeError", "Settings", "default_settings", "preset_names", "preset", "params_from_settings",
     "Simulation", "Ensemble", "SlimeParams", "SlimeOptions", "SlimeGrads", "lib",
     "DECAY_REF_SUBTRACT", "DECAY_MULTIPLY", "BLUR_REF_BOX3", "BLUR_GAUSS", "MAX_BLUR_RADIUS",
+    "DISPATCH_EACH_AGENT", "DISPATCH_REFERENCE",
 ]
 
 Settings = SlimeSettings

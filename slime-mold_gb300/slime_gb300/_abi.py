@@ -22,6 +22,8 @@ DECAY_MULTIPLY = 1
 BLUR_REF_BOX3 = 0
 BLUR_GAUSS = 1
 MAX_BLUR_RADIUS = 8
+DISPATCH_EACH_AGENT = 0
+DISPATCH_REFERENCE = 1
 
 
 class SlimeParams(C.Structure):
@@ -43,7 +45,7 @@ class SlimeParams(C.Structure):
         ("time_step", C.c_float),
         ("decay_mode", C.c_uint32),
         ("blur_mode", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("dispatch_mode", C.c_uint32),
     ]
 
     def copy(self):
