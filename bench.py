@@ -99,6 +99,16 @@ def profiled_traffic(workload, kernel):
     return float(m.group(1)) * 1e6, "profiles/" + name
 
 
+def reference_dispatch_visited(n):
+    """Agents the reference's dispatch updates: min(ceil(n / 64), 65535) x wy
+    workgroups of 64, invocation (gx, gy) updating agent gx + 65535 gy, reach
+    every index below (wy - 1) 65535 + 64 wx."""
+    groups = -(-n // 64)
+    wx = min(groups, 65535)
+    wy = -(-groups // wx)
+    return min(n, (wy - 1) * 65535 + 64 * wx)
+
+
 def make_params(W, H, speed_lo, speed_hi, dist):
     import slime_gb300 as sg
     p = sg.SlimeParams()
@@ -473,6 +483,8 @@ def main():
                     help="1 + tile-table index of the trail kernel (0: autotuned)")
     ap.add_argument("--agent-shape", type=int, default=0,
                     help="1 + shape-table index of the agent kernel (0: autotuned)")
+    ap.add_argument("--dispatch", default="each", choices=["each", "reference"],
+                    help="agents updated per step: every agent once, or the reference's own dispatch")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -500,6 +512,10 @@ def main():
 
     W, H, n, lo, hi, sdist = CONFIGS[args.config]
     params = make_params(W, H, lo, hi, sdist)
+    n_visited = n
+    if args.dispatch == "reference":
+        params.dispatch_mode = sg.DISPATCH_REFERENCE
+        n_visited = reference_dispatch_visited(n)
     agents = make_agents(n, W, H, lo, hi, seed=rank)
     sim = sg.Simulation(W, H, n, params)
     sim.upload_agents(agents)
@@ -544,9 +560,10 @@ def main():
     t_agents = agents_ms / kern_steps
     t_trail = trail_ms / kern_steps
     peak, peak_kind = load_peaks()
-    bytes_agents = 32.0 * n          # agent state read + write
+    bytes_agents = 32.0 * n_visited  # agent state read + write (agents the dispatch skips are untouched)
     bytes_trail = 8.0 * W * H        # trail read + write
-    k_agents = {"name": agents_kernel_name(tuned.agent_shape), "ms": t_agents,
+    k_agents = {"name": "agents_dispatch_kernel" if args.dispatch == "reference"
+                else agents_kernel_name(tuned.agent_shape), "ms": t_agents,
                 "bytes": bytes_agents, "gbs": bytes_agents / (t_agents * 1e-3) / 1e9}
     k_trail = {"name": trail_kernel_name(tuned.trail_tile, int(params.blur_mode)), "ms": t_trail,
                "bytes": bytes_trail, "gbs": bytes_trail / (t_trail * 1e-3) / 1e9}
@@ -598,7 +615,9 @@ def main():
                        "l2_persist": not args.no_l2_persist,
                        "l2": f"agent state {16 * n / 1e6:.0f} MB streamed per step (> 129 MB L2); "
                              f"trail {4 * W * H / 1e6:.0f} MB kept L2-resident by design",
-                       "parallelism": f"replicas x{ws}"},
+                       "parallelism": f"replicas x{ws}",
+                       "dispatch": "every agent once per step" if args.dispatch == "each" else
+                                   f"the reference's dispatch: {n_visited} of {n} agents updated per step"},
             "cells_per_s": cells, "pct_roofline_step": pct_roofline,
             "tuned": {"trail_tile": tuned.trail_tile, "agent_shape": tuned.agent_shape,
                       "trail_texture": tuned.trail_texture, "l2_persist_bytes": tuned.l2_persist_bytes},
