@@ -6,77 +6,106 @@
 
 namespace slime {
 
-// sample_trail_map, compute.wgsl:7-29 (x1 >= W written as x0 >= W - 1).
-// The trail buffers carry W + 2 zero floats past their last cell, so the four
-// taps at index 0 are always in bounds: an out-of-grid sample loads from cell
-// 0 and is discarded, which keeps the sampler free of branches.
-__device__ __forceinline__ float sample_trail(const float* __restrict__ trail, int W, int H, float px, float py) {
-    float fx = floorf(px), fy = floorf(py);
-    int x0 = slm_f2i(fx);
-    int y0 = slm_f2i(fy);
-    // x0 < 0 || x0 + 1 >= W  (and the same for y) as one unsigned compare each
-    bool ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
-    // in range, f32(x0) == floor(px) exactly
-    float dx = slm_sub(px, fx);
-    float dy = slm_sub(py, fy);
-    const float* r0 = trail + (ok ? y0 * W + x0 : 0);
-    float v00 = __ldg(r0);
-    float v10 = __ldg(r0 + 1);
-    float v01 = __ldg(r0 + W);
-    float v11 = __ldg(r0 + W + 1);
-    float v0 = slm_mix(v00, v10, dx);
-    float v1 = slm_mix(v01, v11, dx);
-    return ok ? slm_mix(v0, v1, dy) : 0.0f;
-}
-
-// The same sampler through the texture unit: one four-texel gather returns
-// the 2x2 footprint (raw texels, no filtering), so the interpolation below is
-// the shader's arithmetic on the same four values.  The texture is the trail
-// buffer itself (pitch-linear binary32, point filtering, clamped, unnormalised
-// coordinates); gathering at (x0 + 1, y0 + 1) selects texels x0..x0+1,
-// y0..y0+1, returned as w = (x0, y0), z = (x0+1, y0), x = (x0, y0+1),
-// y = (x0+1, y0+1).  An out-of-grid sample gathers at (1, 1) (always inside a
-// trail of at least 2x2) and is discarded.
-__device__ __forceinline__ float sample_trail_tex(cudaTextureObject_t tex, int W, int H, float px, float py) {
-    float fx = floorf(px), fy = floorf(py);
-    int x0 = slm_f2i(fx);
-    int y0 = slm_f2i(fy);
-    bool ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
-    float dx = slm_sub(px, fx);
-    float dy = slm_sub(py, fy);
-    float u = (float)(ok ? x0 + 1 : 1);
-    float v = (float)(ok ? y0 + 1 : 1);
-    float4 g = tex2Dgather<float4>(tex, u, v, 0);
-    float v0 = slm_mix(g.w, g.z, dx);
-    float v1 = slm_mix(g.x, g.y, dx);
-    return ok ? slm_mix(v0, v1, dy) : 0.0f;
-}
-
-// Trail readers for agent_step: a padded global buffer or a texture over it.
+// Trail readers for agent_step: sample_trail_map, compute.wgsl:7-29 (x1 >= W
+// written as x0 >= W - 1), on a padded global buffer or on a texture over it.
+// Each sample is split in two: fetch() issues the footprint's loads and
+// returns them unconsumed (a Tap), value() interpolates; operator() is both.
+//
+// TrailPtr: the trail buffers carry W + 2 zero floats past their last cell,
+// so the four taps at index 0 are always in bounds: an out-of-grid sample
+// loads from cell 0 and is discarded, which keeps the sampler free of
+// branches.  In range, f32(x0) == floor(px) exactly.
+//
+// TrailTex: one four-texel gather returns the 2x2 footprint (raw texels, no
+// filtering), so the interpolation is the shader's arithmetic on the same four
+// values.  The texture is the trail buffer itself (pitch-linear binary32,
+// point filtering, clamped, unnormalised coordinates); gathering at
+// (x0 + 1, y0 + 1) selects texels x0..x0+1, y0..y0+1, returned as
+// w = (x0, y0), z = (x0+1, y0), x = (x0, y0+1), y = (x0+1, y0+1).  An
+// out-of-grid sample gathers at (1, 1) (always inside a trail of at least
+// 2x2) and is discarded.
 struct TrailPtr {
     const float* __restrict__ t;
+    struct Tap {
+        float v00, v10, v01, v11, dx, dy;
+        bool ok;
+    };
+    __device__ __forceinline__ Tap fetch(int W, int H, float px, float py) const {
+        Tap k;
+        float fx = floorf(px), fy = floorf(py);
+        int x0 = slm_f2i(fx);
+        int y0 = slm_f2i(fy);
+        // x0 < 0 || x0 + 1 >= W  (and the same for y) as one unsigned compare each
+        k.ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
+        k.dx = slm_sub(px, fx);
+        k.dy = slm_sub(py, fy);
+        const float* r0 = t + (k.ok ? y0 * W + x0 : 0);
+        k.v00 = __ldg(r0);
+        k.v10 = __ldg(r0 + 1);
+        k.v01 = __ldg(r0 + W);
+        k.v11 = __ldg(r0 + W + 1);
+        return k;
+    }
+    __device__ __forceinline__ static float value(const Tap& k) {
+        float v0 = slm_mix(k.v00, k.v10, k.dx);
+        float v1 = slm_mix(k.v01, k.v11, k.dx);
+        return k.ok ? slm_mix(v0, v1, k.dy) : 0.0f;
+    }
     __device__ __forceinline__ float operator()(int W, int H, float px, float py) const {
-        return sample_trail(t, W, H, px, py);
+        return value(fetch(W, H, px, py));
     }
 };
 struct TrailTex {
     cudaTextureObject_t t;
+    struct Tap {
+        float4 g;
+        float dx, dy;
+        bool ok;
+    };
+    __device__ __forceinline__ Tap fetch(int W, int H, float px, float py) const {
+        Tap k;
+        float fx = floorf(px), fy = floorf(py);
+        int x0 = slm_f2i(fx);
+        int y0 = slm_f2i(fy);
+        k.ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
+        k.dx = slm_sub(px, fx);
+        k.dy = slm_sub(py, fy);
+        k.g = tex2Dgather<float4>(t, (float)(k.ok ? x0 + 1 : 1), (float)(k.ok ? y0 + 1 : 1), 0);
+        return k;
+    }
+    __device__ __forceinline__ static float value(const Tap& k) {
+        float v0 = slm_mix(k.g.w, k.g.z, k.dx);
+        float v1 = slm_mix(k.g.x, k.g.y, k.dx);
+        return k.ok ? slm_mix(v0, v1, k.dy) : 0.0f;
+    }
     __device__ __forceinline__ float operator()(int W, int H, float px, float py) const {
-        return sample_trail_tex(t, W, H, px, py);
+        return value(fetch(W, H, px, py));
     }
 };
 
-// One agent, compute.wgsl:65-144.  Returns the deposit cell or -1.
+// The three sensor footprints of an agent (compute.wgsl:75-95), fetched.
 template <class Trail>
-__device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,
-                                          int32_t index, const Trail& trail) {
-    speed = slm_clamp(speed, p.speed_min, p.speed_max);
+struct Senses {
+    typename Trail::Tap left, right, center;
+};
 
+template <class Trail>
+__device__ __forceinline__ Senses<Trail> agent_sense(const DevParams& p, float x, float y, float angle,
+                                                     const Trail& trail) {
     float sl, cl, sr, cr, sc, cc;
     slm_sensor_dirs(angle, p.sensor_sin, p.sensor_cos, &cl, &sl, &cc, &sc, &cr, &sr);
-    float left = trail(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)), slm_add(y, slm_mul(p.sensor_dist, sl)));
-    float right = trail(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)), slm_add(y, slm_mul(p.sensor_dist, sr)));
-    float center = trail(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)), slm_add(y, slm_mul(p.sensor_dist, sc)));
+    Senses<Trail> s;
+    s.left = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)), slm_add(y, slm_mul(p.sensor_dist, sl)));
+    s.right = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)), slm_add(y, slm_mul(p.sensor_dist, sr)));
+    s.center = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)), slm_add(y, slm_mul(p.sensor_dist, sc)));
+    return s;
+}
+
+// The rest of the agent (compute.wgsl:72 and 98-144) once its sensor samples
+// are known.  Returns the deposit cell or -1.
+__device__ __forceinline__ int agent_finish(const DevParams& p, float& x, float& y, float& angle, float& speed,
+                                            int32_t index, float left, float right, float center) {
+    speed = slm_clamp(speed, p.speed_min, p.speed_max);
 
     // compute.wgsl:98-112: keep straight, or turn toward target = angle -/+ TAU
     bool turn_left = !(center > left && center > right) && (left > right);
@@ -102,6 +131,15 @@ __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y
     int dy = slm_f2i(y);
     if ((unsigned)dx < (unsigned)p.W && (unsigned)dy < (unsigned)p.H) return dy * p.W + dx;
     return -1;
+}
+
+// One agent, compute.wgsl:65-144.  Returns the deposit cell or -1.
+template <class Trail>
+__device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,
+                                          int32_t index, const Trail& trail) {
+    const Senses<Trail> s = agent_sense(p, x, y, angle, trail);
+    return agent_finish(p, x, y, angle, speed, index, Trail::value(s.left), Trail::value(s.right),
+                        Trail::value(s.center));
 }
 
 __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,

@@ -125,7 +125,8 @@ def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
 @pytest.mark.parametrize("W,H", [(256, 150), (201, 150)])
 def test_every_agent_shape_is_bitexact(gpu, shape, W, H):
     # 256 wide: the trail has gather textures; 201 wide: its rows are not
-    # aligned for one, and the texture shapes (13..15) run their pointer twins
+    # aligned for one, and the texture shapes (13..15) run their pointer
+    # twins.  The largest case runs Morton-reordered (slot -> id map).
     sim0 = make_sim(W, H, 1, config0_params(W, H), agents_uniform(1, W, H, 1.0, 2.0, seed=0),
                     np.zeros((H, W), np.float32))
     assert sim0.info().trail_texture == (1 if W == 256 else 0)
@@ -135,7 +136,7 @@ def test_every_agent_shape_is_bitexact(gpu, shape, W, H):
         agents = agents_uniform(n, W, H, 30.0, 50.0, seed=n)
         trail = np.random.default_rng(n).random((H, W), dtype=np.float32)
         sim = make_sim(W, H, n, p, agents, trail)
-        sim.set_options(agent_shape=shape)
+        sim.set_options(agent_shape=shape, reorder_every=1 if n == 20001 else 0)
         assert sim.info().agent_shape == shape - 1
         sim.step(3)
         ca, ct = agents.copy(), trail.copy()
