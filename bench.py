@@ -560,10 +560,10 @@ def main():
     t_agents = agents_ms / kern_steps
     t_trail = trail_ms / kern_steps
     peak, peak_kind = load_peaks()
-    bytes_agents = 32.0 * n_visited  # agent state read + write (agents the dispatch skips are untouched)
+    bytes_agents = 32.0 * n_visited  # agent state read + write (agents the dispatch never updates sit in
+                                     # the last slots, untouched)
     bytes_trail = 8.0 * W * H        # trail read + write
-    k_agents = {"name": "agents_dispatch_kernel" if args.dispatch == "reference"
-                else agents_kernel_name(tuned.agent_shape), "ms": t_agents,
+    k_agents = {"name": agents_kernel_name(tuned.agent_shape), "ms": t_agents,
                 "bytes": bytes_agents, "gbs": bytes_agents / (t_agents * 1e-3) / 1e9}
     k_trail = {"name": trail_kernel_name(tuned.trail_tile, int(params.blur_mode)), "ms": t_trail,
                "bytes": bytes_trail, "gbs": bytes_trail / (t_trail * 1e-3) / 1e9}

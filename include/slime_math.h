@@ -362,15 +362,24 @@ SLM_FN float slm_cos(float x) { float s, c; slm_sincos(x, &s, &c); return c; }
  * agent i is visited once for each gy < wy with gy 65535 <= i < gy 65535 + 64 wx.
  * Every agent once for n <= 4,194,240; for n < 2^31 the shader's u32 index
  * neither wraps nor turns negative as an i32. */
-SLM_FN uint32_t slm_dispatch_visits(uint64_t n, uint64_t index) {
-    if (index >= n) return 0;
+/* The dispatch's rows wy and row span 64 wx for n agents, 0 < n < 2^31. */
+SLM_FN void slm_dispatch_geometry(uint64_t n, uint32_t* wy, uint32_t* span) {
     const uint64_t groups = (n + 63) / 64;
     const uint64_t wx = groups < 65535 ? groups : 65535;
-    const uint64_t wy = (groups + wx - 1) / wx;
-    const uint64_t span = 64 * wx;
-    const uint64_t hi = index / 65535 < wy - 1 ? index / 65535 : wy - 1; /* gy 65535 <= index */
-    const uint64_t lo = index >= span ? (index - span) / 65535 + 1 : 0;  /* index < gy 65535 + span */
-    return hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+    *wy = (uint32_t)((groups + wx - 1) / wx);
+    *span = (uint32_t)(64 * wx);
+}
+/* Visits of agent `index` < n from that geometry (32-bit arithmetic). */
+SLM_FN uint32_t slm_dispatch_visits_in(uint32_t index, uint32_t wy, uint32_t span) {
+    const uint32_t hi = index / 65535u < wy - 1u ? index / 65535u : wy - 1u; /* gy 65535 <= index */
+    const uint32_t lo = index >= span ? (index - span) / 65535u + 1u : 0u;  /* index < gy 65535 + span */
+    return hi >= lo ? hi - lo + 1u : 0u;
+}
+SLM_FN uint32_t slm_dispatch_visits(uint64_t n, uint64_t index) {
+    if (index >= n || n >= (1ull << 31)) return 0;
+    uint32_t wy, span;
+    slm_dispatch_geometry(n, &wy, &span);
+    return slm_dispatch_visits_in((uint32_t)index, wy, span);
 }
 
 /* Sensor directions of compute.wgsl:79-90: cos/sin of angle - a, angle + a

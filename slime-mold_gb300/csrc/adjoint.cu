@@ -196,6 +196,8 @@ int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every) 
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->stream), "forward_record");
     free_adjoint(ctx);
+    int orc = ensure_dispatch_order(ctx);
+    if (orc != SLIME_OK) return orc;
     auto& a = ctx->adj;
     const size_t cells = (size_t)ctx->W * ctx->H;
     const uint64_t n_pad = ctx->agents.n_pad;
@@ -233,7 +235,7 @@ int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every) 
         if (prc != SLIME_OK) return prc;
         CK(enqueue_step(ctx, marks), "recording a step");
         after_steps(ctx, marks, 1);
-        ctx->launches += kernels_per_step(ctx);
+        ctx->launches += kernels_per_step(ctx, marks);
         ctx->steps_done++;
     }
     ctx->last_counts_valid = true;

@@ -239,46 +239,23 @@ __global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
     }
 }
 
-// The reference's own dispatch (SLIME_DISPATCH_REFERENCE): agent `id` is
-// visited by slm_dispatch_visits(n, id) invocations of compute.wgsl:60's
-// indexing.  No visit leaves the agent as it is; m >= 1 visits move it once
-// (each visit reads the state the pass found, so all compute the same update)
-// and deposit m times.  One agent per thread: a compatibility mode, untuned.
-template <bool kIds, class Trail>
-__global__ void __launch_bounds__(256) agents_dispatch_kernel(const __grid_constant__ DevParams p,
-                                                              float* __restrict__ X, float* __restrict__ Y,
-                                                              float* __restrict__ TH, float* __restrict__ V,
-                                                              const uint32_t* __restrict__ ids, const Trail trail,
-                                                              uint32_t* __restrict__ counts,
-                                                              uint8_t* __restrict__ marks, uint64_t n) {
-    const uint64_t i = (uint64_t)blockIdx.x * 256 + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t id = kIds ? ids[i] : (uint32_t)i;
-    const uint32_t m = slm_dispatch_visits(n, id);
-    if (m == 0) return;
-    float x = X[i], y = Y[i], th = TH[i], v = V[i];
-    const int cell = agent_step(p, x, y, th, v, (int32_t)id, trail);
-    if (cell >= 0) {
-        if (marks)
-            atomicOr(reinterpret_cast<unsigned*>(marks + (cell & ~3)), 1u << (8 * (cell & 3)));
-        else
-            atomicAdd(counts + cell, m);
-    }
-    X[i] = x;
-    Y[i] = y;
-    TH[i] = th;
-    V[i] = v;
-}
-
-template <class Trail>
-cudaError_t launch_agents_dispatch(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
-                                   uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win) {
-    const dim3 grid(blocks_for(a.n, 256));
-    if (a.ids)
-        return launch_k(agents_dispatch_kernel<true, Trail>, grid, dim3(256), 0, s, win, p, a.x, a.y, a.th, a.v,
-                        (const uint32_t*)a.ids, trail, counts, marks, a.n);
-    return launch_k(agents_dispatch_kernel<false, Trail>, grid, dim3(256), 0, s, win, p, a.x, a.y, a.th, a.v,
-                    (const uint32_t*)nullptr, trail, counts, marks, a.n);
+// The reference's own dispatch (SLIME_DISPATCH_REFERENCE) visits agent `id`
+// slm_dispatch_visits(n, id) times (compute.wgsl:60); the agents it visits
+// at all are ids 0 .. reference_dispatch_updated(n) - 1, kept in the first
+// slots.  An agent visited m > 1 times moves once (each visit reads the state
+// the pass found) and deposits m times: the agent kernel deposits once, this
+// kernel adds the other m - 1 at the cell of the agent's new position
+// (compute.wgsl:136-141), which is the cell the agent kernel used.
+__global__ void extra_deposits_kernel(const float* __restrict__ X, const float* __restrict__ Y,
+                                      const uint32_t* __restrict__ ids, uint64_t n_updated, int W, int H,
+                                      uint32_t wy, uint32_t span, uint32_t* __restrict__ counts) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_updated) return;
+    const uint32_t m = slm_dispatch_visits_in(ids ? ids[i] : (uint32_t)i, wy, span);
+    if (m <= 1) return;
+    const int dx = slm_f2i(X[i]);
+    const int dy = slm_f2i(Y[i]);
+    if ((unsigned)dx < (unsigned)W && (unsigned)dy < (unsigned)H) atomicAdd(counts + (size_t)dy * W + dx, m - 1);
 }
 
 template <int APT, int BS, int MINB, class Trail>
@@ -337,14 +314,40 @@ int agent_shape_count() { return (int)(sizeof(kAgentShapes) / sizeof(kAgentShape
 AgentShape agent_shape(int i) { return kAgentShapes[(i >= 0 && i < agent_shape_count()) ? i : 0]; }
 bool agent_shape_uses_texture(int i) { return i >= 12 && i <= 14; }
 
+uint64_t reference_dispatch_updated(uint64_t n) {
+    if (n == 0) return 0;
+    uint32_t wy = 0, span = 0;
+    slm_dispatch_geometry(n, &wy, &span);
+    const uint64_t reach = (uint64_t)(wy - 1) * 65535u + span; // gx + 65535 gy < reach
+    return reach < n ? reach : n;
+}
+
+int agent_pass_kernels(const DevParams& p, uint64_t n, bool marks) {
+    if (n == 0) return 0;
+    if (p.dispatch_mode != SLIME_DISPATCH_REFERENCE || marks) return 1;
+    uint32_t wy = 0, span = 0;
+    slm_dispatch_geometry(n, &wy, &span);
+    return wy > 1 ? 2 : 1; // some agent is visited twice only with two or more rows
+}
+
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
                           cudaStream_t s, int shape, const cudaAccessPolicyWindow* win, cudaTextureObject_t tex,
                           uint8_t* marks) {
     if (a.n == 0) return cudaSuccess;
+    if (p.dispatch_mode == SLIME_DISPATCH_REFERENCE) {
+        AgentsSoA updated = a;
+        updated.n = reference_dispatch_updated(a.n);
+        DevParams each = p;
+        each.dispatch_mode = SLIME_DISPATCH_EACH_AGENT;
+        cudaError_t e = launch_agents(each, updated, trail, counts, s, shape, win, tex, marks);
+        if (e != cudaSuccess || agent_pass_kernels(p, a.n, marks) == 1) return e;
+        uint32_t wy = 0, span = 0;
+        slm_dispatch_geometry(a.n, &wy, &span);
+        extra_deposits_kernel<<<blocks_for(updated.n, 256), 256, 0, s>>>(a.x, a.y, a.ids, updated.n, p.W, p.H, wy,
+                                                                          span, counts);
+        return cudaGetLastError();
+    }
     const TrailPtr tp{trail};
-    if (p.dispatch_mode == SLIME_DISPATCH_REFERENCE)
-        return tex ? launch_agents_dispatch(p, a, TrailTex{tex}, counts, marks, s, win)
-                   : launch_agents_dispatch(p, a, tp, counts, marks, s, win);
     if (agent_shape_uses_texture(shape) && tex) {
         const TrailTex tt{tex};
         switch (shape) {

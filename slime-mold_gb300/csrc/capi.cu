@@ -413,12 +413,14 @@ cudaError_t enqueue_step(slime_ctx* ctx, bool marks) {
     return cudaSuccess;
 }
 
-uint64_t kernels_per_step(const slime_ctx* ctx) { return ctx->agents.n ? 2 : 1; }
+uint64_t kernels_per_step(const slime_ctx* ctx, bool marks) {
+    return 1 + (uint64_t)agent_pass_kernels(ctx->dev, ctx->agents.n, marks);
+}
 
 int run_steps_direct(slime_ctx* ctx, uint32_t m, bool marks) {
     for (uint32_t i = 0; i < m; i++) {
         CK(enqueue_step(ctx, marks), "launching a step");
-        ctx->launches += kernels_per_step(ctx);
+        ctx->launches += kernels_per_step(ctx, marks);
         ctx->steps_done++;
     }
     ctx->last_counts_valid = true;
@@ -451,7 +453,7 @@ int run_steps_graph(slime_ctx* ctx, uint32_t m, bool marks) {
     }
     CK(cudaGraphLaunch(exec, ctx->stream), "launching step graph");
     ctx->cur = (m & 1) ? 1 - ctx->cur : ctx->cur;
-    ctx->launches += kernels_per_step(ctx) * m;
+    ctx->launches += kernels_per_step(ctx, marks) * m;
     ctx->steps_done += m;
     ctx->last_counts_valid = true;
     return SLIME_OK;
@@ -467,10 +469,13 @@ int do_reorder(slime_ctx* ctx) {
         CK(launch_iota(ctx->agents.ids, ctx->agents.n, ctx->stream), "initialising agent ids");
         invalidate_graphs(ctx); // the agent kernel now reads ids
     }
-    CK(launch_reorder(ctx->agents, ctx->W, ctx->H, (int)ctx->opt.reorder_cell_log2, ctx->reorder, ctx->stream),
+    const bool partition = ctx->dev.dispatch_mode == SLIME_DISPATCH_REFERENCE;
+    CK(launch_reorder(ctx->agents, ctx->W, ctx->H, (int)ctx->opt.reorder_cell_log2, ctx->reorder, ctx->stream,
+                      partition ? reference_dispatch_updated(ctx->agents.n) : ~0ull),
        "reordering agents");
     ctx->launches += 5;
     ctx->reordered = true;
+    ctx->reorder_partitioned = partition;
     ctx->last_reorder_step = ctx->steps_done;
     return SLIME_OK;
 }
@@ -525,7 +530,7 @@ int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
             float ms = 0.0f;
             if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
             total[off] += ms;
-            ctx->launches += (steps + 2) * kernels_per_step(ctx);
+            ctx->launches += (steps + 2) * kernels_per_step(ctx, marks);
         }
     }
     const bool measured = e == cudaSuccess && total[0] > 0.0f && total[1] > 0.0f;
@@ -543,8 +548,15 @@ int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
     return SLIME_OK;
 }
 
+int ensure_dispatch_order(slime_ctx* ctx) {
+    if (ctx->dev.dispatch_mode != SLIME_DISPATCH_REFERENCE || !ctx->reordered || ctx->reorder_partitioned)
+        return SLIME_OK;
+    return do_reorder(ctx);
+}
+
 int run_steps(slime_ctx* ctx, uint32_t n) {
     int rc;
+    if ((rc = ensure_dispatch_order(ctx)) != SLIME_OK) return rc;
     while (n > 0) {
         uint32_t m = n;
         if (ctx->opt.reorder_every) {
@@ -977,7 +989,7 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
         }
         ctx->cur = 1 - ctx->cur;
         ctx->steps_done++;
-        ctx->launches += kernels_per_step(ctx);
+        ctx->launches += kernels_per_step(ctx, marks);
         after_steps(ctx, marks, 1);
         if ((e = cudaEventSynchronize(ev[3])) != cudaSuccess) {
             rc = cuda_error(ctx->err, e, "profiling a step");

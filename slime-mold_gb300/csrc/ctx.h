@@ -17,6 +17,9 @@ struct slime_ctx {
     void* agent_block = nullptr;     // x | y | angle | speed, n_pad floats each
     uint32_t* ids_storage = nullptr; // slot -> agent id, allocated at the first reorder
     bool reordered = false;
+    // the last reorder put the agents the reference's dispatch updates first
+    // (identity ids have them first too)
+    bool reorder_partitioned = false;
     uint64_t last_reorder_step = ~0ull;
     slime::ReorderScratch reorder;
 
@@ -98,7 +101,10 @@ bool use_marks(const slime_ctx* ctx);
 int prepare_deposits(slime_ctx* ctx, bool marks);
 cudaError_t enqueue_step(slime_ctx* ctx, bool marks);
 void after_steps(slime_ctx* ctx, bool marks, uint32_t m);
-uint64_t kernels_per_step(const slime_ctx* ctx);
+uint64_t kernels_per_step(const slime_ctx* ctx, bool marks);
+// Reorder first if the reference's dispatch is on and the slots do not hold
+// the agents it updates first.
+int ensure_dispatch_order(slime_ctx* ctx);
 int run_steps(slime_ctx* ctx, uint32_t n);
 void free_adjoint(slime_ctx* ctx);
 void setup_l2(slime_ctx* ctx);

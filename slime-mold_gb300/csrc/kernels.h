@@ -36,9 +36,17 @@ bool agent_shape_uses_texture(int index);
 // sample through it; 0 runs those shapes on the pointer path.  With `marks`
 // the deposits set per-cell byte marks instead of counting (valid only when
 // every deposit saturates the fold: deposition >= 1 on a trail >= 0).
+// With p.dispatch_mode == SLIME_DISPATCH_REFERENCE the agents the reference's
+// dispatch updates must fill the first reference_dispatch_updated(a.n)
+// slots (identity ids, or a reorder given that count): the pass updates those
+// and, when counting, adds the extra deposits of multiply visited agents.
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
                           cudaStream_t s, int shape = 0, const cudaAccessPolicyWindow* win = nullptr,
                           cudaTextureObject_t tex = 0, uint8_t* marks = nullptr);
+// Kernels one launch_agents call enqueues.
+int agent_pass_kernels(const DevParams& p, uint64_t n, bool marks);
+// How many agents (ids 0 .. this - 1) the reference's dispatch updates.
+uint64_t reference_dispatch_updated(uint64_t n);
 cudaTextureObject_t make_trail_texture(const float* trail, uint32_t W, uint32_t H);
 // AoS staging (x, y, angle, speed per agent, id order) <-> SoA slots.
 cudaError_t launch_aos_to_soa(const float4* aos, const AgentsSoA& a, cudaStream_t s);
@@ -88,8 +96,9 @@ struct ReorderScratch {
     size_t bytes = 0;
 };
 cudaError_t launch_iota(uint32_t* ids, uint64_t n, cudaStream_t s);
+// Morton order; agents with id >= `visited` go to the last slots.
 cudaError_t launch_reorder(AgentsSoA& a, uint32_t W, uint32_t H, int cell_log2, ReorderScratch& scratch,
-                           cudaStream_t s);
+                           cudaStream_t s, uint64_t visited = ~0ull);
 
 // ---- colorize.cu
 cudaError_t launch_colorize(const float* trail, uint32_t W, uint32_t H, const uint8_t* lut, uint32_t tw,

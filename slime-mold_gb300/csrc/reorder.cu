@@ -9,7 +9,10 @@
 //
 // Counting sort on the Morton code of the agent's (cell >> cell_log2):
 // key + histogram, exclusive scan, scatter to scratch, copy back.  The order
-// inside one key is whatever the scatter atomics produce.
+// inside one key is whatever the scatter atomics produce.  Agents whose id is
+// at or above `visited` (those the reference's dispatch never updates) get
+// one key past every Morton code, so they end up in the last slots and the
+// updated agents fill the first ones.
 #include "kernels.h"
 
 namespace slime {
@@ -32,13 +35,15 @@ __device__ __forceinline__ uint32_t spread_bits(uint32_t v) {
 // neighbours (about 2^(2 cell_log2) per key at one agent per cell), so the
 // histogram and the slot claims are aggregated per warp: the lanes holding
 // one key elect a leader that adds the group's size with a single atomic.
-__global__ void key_hist_kernel(const float* __restrict__ x, const float* __restrict__ y, uint64_t n, int W,
-                                int H, int cl, uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+__global__ void key_hist_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                const uint32_t* __restrict__ ids, uint64_t visited, uint32_t frozen_key, uint64_t n,
+                                int W, int H, int cl, uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int cx = min(max(slm_f2i(x[i]), 0), W - 1) >> cl;
     int cy = min(max(slm_f2i(y[i]), 0), H - 1) >> cl;
     uint32_t k = spread_bits((uint32_t)cx) | (spread_bits((uint32_t)cy) << 1);
+    if (visited < n && ids[i] >= visited) k = frozen_key;
     keys[i] = k;
     const unsigned group = __match_any_sync(__activemask(), k);
     if ((int)(threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(hist + k, (uint32_t)__popc(group));
@@ -159,7 +164,7 @@ cudaError_t launch_iota(uint32_t* ids, uint64_t n, cudaStream_t s) {
 }
 
 cudaError_t launch_reorder(AgentsSoA& a, uint32_t W, uint32_t H, int cell_log2, ReorderScratch& scratch,
-                           cudaStream_t s) {
+                           cudaStream_t s, uint64_t visited) {
     if (a.n == 0) return cudaSuccess;
     if (!a.ids) return cudaErrorInvalidValue; // the caller installs identity ids first
     if (cell_log2 < 0) cell_log2 = 0;
@@ -170,7 +175,10 @@ cudaError_t launch_reorder(AgentsSoA& a, uint32_t W, uint32_t H, int cell_log2, 
     int L = 0;
     while ((1u << L) < d) L++;
     if (L > 16) return cudaErrorInvalidValue;
-    uint64_t nb = 1ull << (2 * L);
+    const bool partition = visited < a.n;
+    if (partition && L > 15) return cudaErrorInvalidValue; // no key left past the Morton codes
+    const uint32_t frozen_key = (uint32_t)(1ull << (2 * L));
+    uint64_t nb = (1ull << (2 * L)) + (partition ? 1 : 0);
     uint64_t nblk = (nb + kScanTile - 1) / kScanTile;
     const uint64_t n = a.n;
     size_t need = align256(4 * n) /*keys*/ + align256(4 * nb) /*hist*/ + align256(4 * nblk) /*block sums*/ +
@@ -196,7 +204,8 @@ cudaError_t launch_reorder(AgentsSoA& a, uint32_t W, uint32_t H, int cell_log2, 
     cudaError_t e = cudaMemsetAsync(hist, 0, 4 * nb, s);
     if (e != cudaSuccess) return e;
     unsigned blocks = (unsigned)((n + 255) / 256);
-    key_hist_kernel<<<blocks, 256, 0, s>>>(a.x, a.y, n, (int)W, (int)H, cell_log2, keys, hist);
+    key_hist_kernel<<<blocks, 256, 0, s>>>(a.x, a.y, a.ids, visited, frozen_key, n, (int)W, (int)H, cell_log2, keys,
+                                          hist);
     scan_reduce_kernel<<<(unsigned)nblk, kScanThreads, 0, s>>>(hist, nb, bsum);
     scan_block_sums_kernel<<<1, kScanThreads, 0, s>>>(bsum, (uint32_t)nblk);
     scan_apply_kernel<<<(unsigned)nblk, kScanThreads, 0, s>>>(hist, nb, bsum);

@@ -163,3 +163,31 @@ def test_gpu_rejects_unknown_dispatch_and_ensemble_reference_dispatch(gpu):
         sg.Simulation(64, 64, 10, config0_params(64, 64, dispatch_mode=2))
     with pytest.raises(sg.SlimeError):
         sg.Ensemble([64], [64], [10], [config0_params(64, 64, dispatch_mode=1)])
+
+
+@pytest.mark.gpu
+def test_gpu_reference_dispatch_after_reordered_steps(gpu):
+    """Morton reordering in the every-agent mode scatters the agent ids over
+    the slots; switching to the reference's dispatch (reordering off) must
+    first put the agents it updates back in the leading slots.  Then back to
+    every agent.  Against the oracle at each switch, exact counts."""
+    from test_parity_gpu import assert_bitexact, make_sim
+    W, H, n = 256, 192, 4_264_240
+    p_each = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, pheromone_deposition_amount=0.3,
+                            agent_speed_min=30.0, agent_speed_max=50.0)
+    p_ref = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, pheromone_deposition_amount=0.3,
+                           agent_speed_min=30.0, agent_speed_max=50.0, dispatch_mode=1)
+    agents = agents_uniform(n, W, H, 0.5, 80.0, seed=31)
+    trail = np.random.default_rng(32).random((H, W), dtype=np.float32)
+    sim = make_sim(W, H, n, p_each, agents, trail)
+    sim.set_options(reorder_every=1, exact_counts=1)
+    ca, ct = agents.copy(), trail.copy()
+    for p, steps, reorder in ((p_each, 2, 1), (p_ref, 2, 0), (p_each, 1, 0), (p_ref, 1, 1)):
+        sim.set_params(p)
+        sim.set_options(reorder_every=reorder, exact_counts=1)
+        sim.step(steps)
+        counts = oracle.run(p, W, H, ca, ct, steps, record_counts=True)
+        assert_bitexact(sim.download_deposit_counts(), counts[-1], f"counts mode {p.dispatch_mode}")
+        assert_bitexact(sim.download_agents(), ca, f"agents mode {p.dispatch_mode}")
+        assert_bitexact(sim.download_trail(), ct, f"trail mode {p.dispatch_mode}")
+    sim.close()

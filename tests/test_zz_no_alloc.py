@@ -72,3 +72,33 @@ def test_step_noalloc_rejects_sizes_beyond_its_array(gpu):
     p = config0_params(1, 64)
     rc = L.slime_step_noalloc(C.byref(p), 1, 64, 4, _ptr(x), _ptr(x), _ptr(x), _ptr(x), _ptr(big), _ptr(out), None)
     assert rc == -1
+
+
+def test_step_noalloc_in_the_reference_dispatch(gpu):
+    """4,264,240 agents in the reference's dispatch (4,465 never updated,
+    most of the rest visited twice) at deposition 0.3, so every extra visit's
+    deposit shows in the trail: two calls against the oracle."""
+    import torch
+
+    import oracle
+    import slime_gb300 as sg
+    L = sg.lib()
+    W, H, n = 320, 200, 4_264_240
+    p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, pheromone_deposition_amount=0.3,
+                       agent_speed_min=30.0, agent_speed_max=50.0, dispatch_mode=1)
+    agents = agents_uniform(n, W, H, 0.5, 80.0, seed=7)
+    trail = np.random.default_rng(8).random((H, W), dtype=np.float32)
+    dev = torch.device("cuda", 0)
+    cols = [torch.tensor(np.ascontiguousarray(agents[:, j]), device=dev) for j in range(4)]
+    ta = torch.tensor(trail, device=dev)
+    tb = torch.empty_like(ta)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ca, ct = agents.copy(), trail.copy()
+    for src, dst in ((ta, tb), (tb, ta)):
+        rc = L.slime_step_noalloc(C.byref(p), W, H, n, *[_ptr(c) for c in cols], _ptr(src), _ptr(dst), stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        oracle.run(p, W, H, ca, ct, 1)
+        got = np.stack([c.cpu().numpy() for c in cols], axis=1)
+        assert np.array_equal(got.view(np.uint32), ca.view(np.uint32))
+        assert np.array_equal(dst.cpu().numpy().view(np.uint32), ct.view(np.uint32))
