@@ -25,10 +25,11 @@ def build(force=False):
     return LIB
 
 
-# The reference's compute shader, translated to C++ and built beside the
-# oracle to pin it (tests/test_reference_pin.py).  Built only where the
-# reference's source tree is present; outputs go to oracle/_ref/ only.
+# The reference's compute and display shaders, translated to C++ and built
+# beside the oracle to pin it (tests/test_reference_pin.py).  Built only where
+# the reference's source tree is present; outputs go to oracle/_ref/ only.
 REF_WGSL = os.environ.get("SLIME_REFERENCE_WGSL", "/root/reference/src/compute.wgsl")
+REF_DISPLAY_WGSL = os.path.join(os.path.dirname(REF_WGSL), "display.wgsl")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_DIR, "libwgslref.so")
 
@@ -37,17 +38,17 @@ def build_reference(force=False):
     if not os.path.exists(REF_WGSL):
         return None
     os.makedirs(REF_DIR, exist_ok=True)
-    inc = os.path.join(REF_DIR, "compute_wgsl.inc")
     wgsl_dir = os.path.join(HERE, "wgsl")
-    deps = [REF_WGSL, os.path.join(wgsl_dir, "translate.py"), os.path.join(wgsl_dir, "prelude.h"),
+    deps = [REF_WGSL, REF_DISPLAY_WGSL, os.path.join(wgsl_dir, "translate.py"), os.path.join(wgsl_dir, "prelude.h"),
             os.path.join(wgsl_dir, "harness.cpp"), os.path.join(HERE, "..", "include", "slime_math.h"),
             os.path.abspath(__file__)]
     if not force and os.path.exists(REF_LIB) and os.path.getmtime(REF_LIB) >= max(os.path.getmtime(d) for d in deps):
         return REF_LIB
-    r = subprocess.run([sys.executable, os.path.join(wgsl_dir, "translate.py"), REF_WGSL, inc],
-                       capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"translating {REF_WGSL} failed:\n{r.stdout}\n{r.stderr}")
+    for src, inc in ((REF_WGSL, "compute_wgsl.inc"), (REF_DISPLAY_WGSL, "display_wgsl.inc")):
+        r = subprocess.run([sys.executable, os.path.join(wgsl_dir, "translate.py"), src, os.path.join(REF_DIR, inc)],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"translating {src} failed:\n{r.stdout}\n{r.stderr}")
     tmp = REF_LIB + ".tmp"
     cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fwrapv", "-fPIC", "-shared",
            os.path.join(wgsl_dir, "harness.cpp"), "-o", tmp]

@@ -5,8 +5,10 @@
 // compiled with this file by oracle/build_oracle.py into
 // oracle/_ref/libwgslref.so; none of it is shipped or used by the library.
 //
-// Each entry point binds the shader's buffers and uniform and runs one of
-// its entry points over the whole grid, invocation after invocation:
+// The display shader (src/display.wgsl) is translated the same way into
+// oracle/_ref/display_wgsl.inc.  Each entry point binds the shader's buffers
+// and uniform and runs one of its entry points over the whole grid,
+// invocation after invocation:
 //   wref_sample   sample_trail_map at given positions;
 //   wref_agents   `main` once per agent (invocation id (i, 0, 0), i.e. the
 //                 intended one-invocation-per-agent mapping), sensing the
@@ -21,6 +23,9 @@
 //                 (src/main.rs:1174-1178: wx x wy workgroups of 64,
 //                 invocation id (gx, gy, 0)), agents and trail both read
 //                 as the pass found them, writes going to the live arrays;
+//   wref_colorize display.wgsl's `main` once per pixel of a tex_width x
+//                 tex_height image (the LUT as 768 u32, the reference's
+//                 lut_data);
 //   wref_sense    the three sensor samples `main` takes (compute.wgsl:74-95,
 //                 restated here in the prelude's WGSL operations because
 //                 `main` keeps them in locals), to tell a flipped turn
@@ -37,6 +42,11 @@ namespace ref {
 using namespace wgsl;
 #include "../_ref/compute_wgsl.inc"
 } // namespace ref
+
+namespace ref_display {
+using namespace wgsl;
+#include "../_ref/display_wgsl.inc"
+} // namespace ref_display
 
 namespace {
 
@@ -152,6 +162,28 @@ void wref_diffuse(const SlimeParams* p, const float* in, float* out) {
     for (uint32_t y = 0; y < p->height; y++)
         for (uint32_t x = 0; x < p->width; x++) ref::diffuse_trail(ref::vec3u{x, y, 0u});
     for (size_t i = 0; i < cells; i++) out[i] = dst[i].v;
+}
+
+void wref_colorize(uint32_t W, uint32_t H, const float* trail, const uint8_t* lut768, uint32_t tw, uint32_t th,
+                   uint8_t* rgba) {
+    ref_display::sim_size = ref_display::SimSizeUniform{};
+    ref_display::sim_size.width = W;
+    ref_display::sim_size.height = H;
+    const size_t cells = (size_t)W * H;
+    std::vector<wgsl::f32> t(cells);
+    for (size_t i = 0; i < cells; i++) t[i] = wgsl::f32(trail[i]);
+    ref_display::trail_map.data = t.data();
+    ref_display::trail_map.src = nullptr;
+    ref_display::trail_map.length = (uint32_t)cells;
+    std::vector<uint32_t> lut(lut768, lut768 + 768); /* src/main.rs:329-336: each byte as a u32 */
+    ref_display::lut_data.data = lut.data();
+    ref_display::lut_data.src = nullptr;
+    ref_display::lut_data.length = 768;
+    ref_display::display_tex.data = rgba;
+    ref_display::display_tex.width = tw;
+    ref_display::display_tex.height = th;
+    for (uint32_t y = 0; y < th; y++)
+        for (uint32_t x = 0; x < tw; x++) ref_display::wgsl_main(ref_display::vec3u{x, y, 0u});
 }
 
 void wref_sense(const SlimeParams* p, const float* agents, uint64_t n, const float* trail, float* out) {

@@ -23,7 +23,12 @@
  *     a race-free execution of an in-place pass is defined for comparison.
  *     An index outside the array reads 0 and drops the write, one of the
  *     outcomes WGSL's robust buffer access allows;
- *   - i32 arithmetic wraps as in WGSL (the harness is compiled with -fwrapv).
+ *   - i32 arithmetic wraps as in WGSL (the harness is compiled with -fwrapv);
+ *   - the display's texture_storage_2d<rgba8unorm, write> is StorageTexRGBA8,
+ *     an RGBA8 image the harness binds: textureDimensions gives its size,
+ *     textureStore converts each channel as a unorm8 store does,
+ *     round(clamp(c, 0, 1) * 255) (to nearest; NaN stores 0), and drops
+ *     stores outside the image.
  */
 #ifndef SLIME_WGSL_PRELUDE_H
 #define SLIME_WGSL_PRELUDE_H
@@ -62,6 +67,12 @@ typedef uint32_t u32;
 struct vec2f {
     f32 x, y;
 };
+struct vec2i {
+    int32_t x, y;
+};
+struct vec2u {
+    uint32_t x, y;
+};
 struct vec4f {
     f32 x, y, z, w;
 };
@@ -73,6 +84,13 @@ struct vec3u {
 inline i32 to_i32(f32 e) { return slm_f2i(e.v); }
 inline i32 to_i32(u32 e) { return (i32)e; }
 inline i32 to_i32(i32 e) { return e; }
+inline u32 to_u32(f32 e) { /* truncate, saturate to [0, 2^32 - 1], NaN -> 0 */
+    if (!(e.v > 0.0f)) return 0u;
+    if (e.v >= 4294967296.0f) return 0xffffffffu;
+    return (u32)e.v;
+}
+inline u32 to_u32(i32 e) { return (u32)e; }
+inline u32 to_u32(u32 e) { return e; }
 inline f32 to_f32(i32 e) { return f32(slm_i2f(e)); }
 inline f32 to_f32(u32 e) { return f32((float)e); }
 inline f32 to_f32(f32 e) { return e; }
@@ -121,6 +139,26 @@ template <class T>
 inline u32 arrayLength(const Buffer<T>& b) {
     return b.length;
 }
+/* write-only rgba8unorm storage texture */
+struct StorageTexRGBA8 {
+    uint8_t* data = nullptr; /* width * height RGBA8 texels, row-major */
+    uint32_t width = 0, height = 0;
+};
+inline vec2u textureDimensions(const StorageTexRGBA8& t) { return vec2u{t.width, t.height}; }
+inline uint8_t unorm8(f32 c) {
+    if (!(c.v > 0.0f)) return 0;
+    if (c.v >= 1.0f) return 255;
+    return (uint8_t)(double)((double)c.v * 255.0 + 0.5); /* c * 255 is exact in binary64 */
+}
+inline void textureStore(StorageTexRGBA8& t, vec2i at, vec4f c) {
+    if (at.x < 0 || at.y < 0 || (uint32_t)at.x >= t.width || (uint32_t)at.y >= t.height) return;
+    uint8_t* o = t.data + 4 * ((size_t)at.y * t.width + (uint32_t)at.x);
+    o[0] = unorm8(c.x);
+    o[1] = unorm8(c.y);
+    o[2] = unorm8(c.z);
+    o[3] = unorm8(c.w);
+}
+
 /* `let x = e;` takes e's value (a buffer element is read, not referenced) */
 template <class T>
 inline T value(const T& v) {

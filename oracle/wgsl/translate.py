@@ -1,22 +1,27 @@
-"""Translate the reference's WGSL compute shader into C++ (test infrastructure).
+"""Translate the reference's WGSL compute shaders into C++ (test infrastructure).
 
 The output reads almost token for token like the shader; oracle/wgsl/prelude.h
 gives it WGSL's meaning (binary32 f32 with single roundings, WGSL conversions
-and builtins, storage buffers the harness binds).  Only the WGSL subset that
-src/compute.wgsl uses is handled, and anything else is rejected:
+and builtins, storage buffers and the storage texture the harness binds).
+Only the WGSL subset that src/compute.wgsl and src/display.wgsl use is
+handled, and anything else is rejected:
 
   const NAME: T = EXPR;          -> static const T NAME = EXPR;
   struct S { f: T, ... };        -> struct S { T f; ... };
   @group @binding var<storage, read_write> NAME: array<T>;
                                  -> static Buffer<T> NAME;
   var<uniform> NAME: T;          -> static T NAME;
+  var NAME: texture_storage_2d<rgba8unorm, write>;
+                                 -> static StorageTexRGBA8 NAME;
   @compute ... fn NAME(@builtin(...) p: T) { ... }
   fn NAME(p: T, ...) -> R { ... } -> static R NAME(T p, ...) { ... }
   let NAME = EXPR;               -> const auto NAME = value(EXPR);
   var NAME = EXPR;               -> auto NAME = value(EXPR);
   var NAME: T = EXPR;            -> T NAME = EXPR;
-  vec2<f32>/vec3<u32>/vec4<f32>  -> vec2f / vec3u / vec4f
-  i32(e), f32(e)                 -> to_i32(e), to_f32(e)
+  var NAME: T;                   -> T NAME{};  (WGSL's zero value)
+  vec2<f32|i32|u32>/vec3<u32>/vec4<f32>
+                                 -> vec2f / vec2i / vec2u / vec3u / vec4f
+  i32(e), u32(e), f32(e)         -> to_i32(e), to_u32(e), to_f32(e)
   arrayLength(&b)                -> arrayLength(b)
   float literal                  -> f32(<the literal rounded to binary32>)
 
@@ -121,7 +126,8 @@ def fold_constants(toks):
     return out
 
 
-TYPES = {("vec2", "f32"): "vec2f", ("vec3", "u32"): "vec3u", ("vec4", "f32"): "vec4f"}
+TYPES = {("vec2", "f32"): "vec2f", ("vec2", "i32"): "vec2i", ("vec2", "u32"): "vec2u", ("vec3", "u32"): "vec3u",
+         ("vec4", "f32"): "vec4f"}
 
 
 def parse_type(toks, i):
@@ -138,6 +144,11 @@ def parse_type(toks, i):
         inner, j = parse_type(toks, i + 2)
         assert toks[j] == ("op", ">")
         return f"Buffer<{inner}>", j + 1
+    if v == "texture_storage_2d":
+        fmt = [t[1] for t in toks[i + 1:i + 6]]
+        if fmt != ["<", "rgba8unorm", ",", "write", ">"]:
+            raise SyntaxError(f"unsupported storage texture {fmt}")
+        return "StorageTexRGBA8", i + 6
     if k == "id":
         return v, i + 1
     raise SyntaxError(f"not a type: {toks[i]}")
@@ -188,7 +199,7 @@ def emit_expr(toks):
             out.append(t + "{" + emit_expr(args) + "}")
             i = j + 1
             continue
-        if k == "id" and v in ("i32", "f32") and i + 1 < len(toks) and toks[i + 1] == ("op", "("):
+        if k == "id" and v in ("i32", "u32", "f32") and i + 1 < len(toks) and toks[i + 1] == ("op", "("):
             out.append("to_" + v)
             i += 1
             continue
@@ -229,6 +240,10 @@ def translate_body(toks, i):
             ctype = None
             if toks[j] == ("op", ":"):
                 ctype, j = parse_type(toks, j + 1)
+            if v == "var" and ctype and toks[j] == ("op", ";"):
+                out.append(f"{ctype} {name}{{}};")
+                i = j + 1
+                continue
             assert toks[j] == ("op", "="), toks[i:j + 1]
             e, j = expr_tokens(toks, j + 1)
             qual = "const auto" if v == "let" else "auto"
@@ -310,14 +325,15 @@ def translate(src):
             structs.append(f"struct {name} {{\n" + "\n".join(fields) + "\n};")
             i = j
         elif v == "var":
-            # var<storage, read_write> NAME: array<T>;  |  var<uniform> NAME: T;
-            assert toks[i + 1] == ("op", "<")
-            j = i + 2
-            while toks[j] != ("op", ">"):
+            # var<storage, read_write> NAME: array<T>;  |  var<uniform> NAME: T;  |  var NAME: T;
+            j = i + 1
+            if toks[j] == ("op", "<"):
+                while toks[j] != ("op", ">"):
+                    j += 1
                 j += 1
-            name = toks[j + 1][1]
-            assert toks[j + 2] == ("op", ":")
-            t, j = parse_type(toks, j + 3)
+            name = toks[j][1]
+            assert toks[j + 1] == ("op", ":")
+            t, j = parse_type(toks, j + 2)
             assert toks[j] == ("op", ";")
             decls.append(f"static {t} {name};")
             i = j + 1
@@ -348,7 +364,7 @@ def translate(src):
     return "\n\n".join(structs + decls + ["\n".join(protos)] + funcs) + "\n"
 
 
-HEADER = """// Generated by oracle/wgsl/translate.py from the reference's src/compute.wgsl.
+HEADER = """// Generated by oracle/wgsl/translate.py from the reference's src/{name}.
 // Not part of the repository: rebuilt from the reference's source by
 // oracle/build_oracle.py.  Include inside a namespace that uses wgsl::.
 """
@@ -358,4 +374,4 @@ if __name__ == "__main__":
     with open(src_path) as f:
         code = translate(f.read())
     with open(out_path, "w") as f:
-        f.write(HEADER + code)
+        f.write(HEADER.format(name=src_path.replace("\\", "/").rsplit("/", 1)[-1]) + code)

@@ -44,6 +44,9 @@ def lib():
         L.wref_diffuse.argtypes = [SP, f32, f32]
         L.wref_sense.argtypes = [SP, f32, C.c_uint64, f32, f32]
         L.wref_agents_dispatch.argtypes = [SP, f32, C.c_uint64, f32]
+        u8 = C.POINTER(C.c_uint8)
+        L.wref_colorize.argtypes = [C.c_uint32, C.c_uint32, f32, u8, C.c_uint32, C.c_uint32, u8]
+        L.wref_colorize.restype = None
         for f in (L.wref_sample, L.wref_agents, L.wref_decay, L.wref_diffuse, L.wref_sense, L.wref_agents_dispatch):
             f.restype = None
         _lib = L
@@ -103,6 +106,18 @@ def sense(params, agents, trail):
     t = np.ascontiguousarray(trail, np.float32)
     out = np.empty((a.shape[0], 3), np.float32)
     lib().wref_sense(C.byref(params), _p(a), a.shape[0], _p(t), _p(out))
+    return out
+
+
+def colorize(trail, lut768, tex_width, tex_height):
+    """display.wgsl's `main` over a tex_width x tex_height RGBA8 image."""
+    t = np.ascontiguousarray(trail, np.float32)
+    H, W = t.shape
+    lut = np.ascontiguousarray(lut768, np.uint8).reshape(-1)
+    assert lut.size == 768
+    out = np.zeros((tex_height, tex_width, 4), np.uint8)
+    u8 = C.POINTER(C.c_uint8)
+    lib().wref_colorize(W, H, _p(t), lut.ctypes.data_as(u8), tex_width, tex_height, out.ctypes.data_as(u8))
     return out
 
 

@@ -22,10 +22,14 @@ follows it exactly:
                        0 (the frame is then the agent pass alone); the trail
                        compares on cells at most one agent lands on, where
                        the shader's non-atomic update loses nothing.
+  display_fit          src/display.wgsl's colourise of a 97x61 trail (values
+                       outside [0, 1] and NaN included) through a random LUT
+                       into a wide (160x90) and a tall (90x160) image.
 
-Each file holds W, H, the parameters (p_*), agents0 and trail0, the list of
-saved frames, agents<s> and trail<s> for each, and `compare` ("all" or
-"single_deposit_cells").  Needs the reference's source tree.
+Each frames file holds W, H, the parameters (p_*), agents0 and trail0, the
+list of saved frames, agents<s> and trail<s> for each, and `compare` ("all"
+or "single_deposit_cells"); display_fit holds trail, lut and image<w>x<h>.
+Needs the reference's source tree.
 Run: python tests/golden/make_reference_golden.py
 """
 import os
@@ -112,6 +116,15 @@ def main():
                   decay_factor=0.0, diffusion_rate=0.0)
     write_case("pass_dep03", W, H, p, d, agents(2000, W, H, 30, 50, 25),
                np.random.default_rng(26).random((H, W), dtype=np.float32), [1], "single_deposit_cells")
+    rng = np.random.default_rng(27)
+    trail = rng.uniform(-0.2, 1.2, (61, 97)).astype(np.float32)
+    trail.flat[:6] = [0.0, 1.0, np.nan, -0.0, 0.5 / 255, 254.5 / 255]
+    lut = rng.integers(0, 256, 768, dtype=np.uint8)
+    out = {"trail": trail, "lut": lut}
+    for tw, th in ((160, 90), (90, 160)):
+        out[f"image{tw}x{th}"] = wgslref.colorize(trail, lut, tw, th)
+    np.savez_compressed(os.path.join(OUT, "display_fit.npz"), **out)
+    print("display_fit written")
 
 
 if __name__ == "__main__":

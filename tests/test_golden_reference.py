@@ -1,10 +1,11 @@
-"""Golden frames from the reference's own compute shader (tests/golden/wgsl/,
-made by tests/golden/make_reference_golden.py from a mechanical C++
-translation of src/compute.wgsl run invocation by invocation): the CPU
+"""Golden frames from the reference's own shaders (tests/golden/wgsl/, made by
+tests/golden/make_reference_golden.py from mechanical C++ translations of
+src/compute.wgsl and src/display.wgsl run invocation by invocation): the CPU
 oracle (always) and the CUDA path (gpu) must reproduce each saved frame bit
 for bit, agents and trail; in `single_deposit_cells` cases the trail is
 compared on the cells at most one agent landed on, the only cells whose
-value the shader's non-atomic deposit defines."""
+value the shader's non-atomic deposit defines.  The display images must be
+reproduced byte for byte."""
 import glob
 import os
 
@@ -14,7 +15,9 @@ import pytest
 import oracle
 from conftest import ROOT
 
-FIXTURES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "wgsl", "*.npz")))
+FIXTURES = sorted(p for p in glob.glob(os.path.join(ROOT, "tests", "golden", "wgsl", "*.npz"))
+                  if not os.path.basename(p).startswith("display_"))
+DISPLAY = os.path.join(ROOT, "tests", "golden", "wgsl", "display_fit.npz")
 KEYS = ["decay_factor", "agent_jitter", "agent_speed_min", "agent_speed_max", "agent_turn_speed",
         "agent_sensor_angle", "agent_sensor_distance", "diffusion_rate", "pheromone_deposition_amount",
         "blur_radius", "blur_sigma", "time_step", "decay_mode", "blur_mode"]
@@ -76,3 +79,26 @@ def test_gpu_reproduces_reference_frames(gpu, path):
             sim.step(1)  # the counts of the saved frame's own step
             done = s
             check(d, s, sim.download_agents(), sim.download_trail(), sim.download_deposit_counts())
+
+
+def display_cases():
+    d = dict(np.load(DISPLAY))
+    for key in sorted(k for k in d if k.startswith("image")):
+        tw, th = (int(v) for v in key[5:].split("x"))
+        yield d["trail"], d["lut"], tw, th, d[key]
+
+
+def test_oracle_reproduces_reference_display():
+    for trail, lut, tw, th, image in display_cases():
+        H, W = trail.shape
+        assert np.array_equal(oracle.colorize(W, H, trail, lut, tw, th), image), (tw, th)
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_reference_display(gpu):
+    import slime_gb300 as sg
+    for trail, lut, tw, th, image in display_cases():
+        H, W = trail.shape
+        with sg.Simulation(W, H, 1, None) as sim:
+            sim.upload_trail(trail)
+            assert np.array_equal(sim.colorize(lut, tw, th), image), (tw, th)

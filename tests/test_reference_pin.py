@@ -243,3 +243,18 @@ def test_one_pass_matches_reference_where_deposits_do_not_race():
     single = counts <= 1
     assert same_bits(folded[single], ref_t[single])
     assert np.count_nonzero(counts == 1) > n // 2
+
+
+@pytest.mark.parametrize("W,H,tw,th", [(97, 61, 1600, 900), (97, 61, 900, 1600), (64, 48, 64, 48), (64, 48, 128, 96),
+                                       (300, 100, 301, 199), (5, 7, 33, 17), (1, 1, 3, 2)])
+def test_display_colorize_matches_reference(W, H, tw, th):
+    """display.wgsl's `main` (translated, one invocation per pixel) against
+    the oracle's colourise: aspect fit with black bars, the trail clamped and
+    mapped through the 768-entry LUT, stored as rgba8unorm."""
+    rng = np.random.default_rng(W * 7 + tw)
+    trail = rng.uniform(-0.2, 1.2, (H, W)).astype(np.float32)
+    edge = np.array([0.0, 1.0, np.nextafter(np.float32(1), np.float32(0)), 0.5 / 255, 254.5 / 255, np.nan,
+                     -0.0, 2.0 / 255], np.float32)
+    trail.flat[:min(trail.size, edge.size)] = edge[:trail.size]
+    lut = rng.integers(0, 256, 768, dtype=np.uint8)
+    assert np.array_equal(oracle.colorize(W, H, trail, lut, tw, th), wgslref.colorize(trail, lut, tw, th))
