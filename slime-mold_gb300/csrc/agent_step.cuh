@@ -70,7 +70,10 @@ struct TrailTex {
         k.ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
         k.dx = slm_sub(px, fx);
         k.dy = slm_sub(py, fy);
-        k.g = tex2Dgather<float4>(t, (float)(k.ok ? x0 + 1 : 1), (float)(k.ok ? y0 + 1 : 1), 0);
+        // in range, f32(x0 + 1) == floor(px) + 1 exactly (|x0| < 2^24); a NaN
+        // position passes the test (i32(NaN) = 0) and gathers at a NaN
+        // coordinate, whose texels do not matter: its weights are NaN
+        k.g = tex2Dgather<float4>(t, k.ok ? fx + 1.0f : 1.0f, k.ok ? fy + 1.0f : 1.0f, 0);
         return k;
     }
     __device__ __forceinline__ static float value(const Tap& k) {
