@@ -261,24 +261,29 @@ __global__ void extra_deposits_kernel(const float* __restrict__ X, const float* 
 template <int APT, int BS, int MINB, class Trail>
 cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
                                      uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win) {
-    static int per_sm[2] = {0, 0};
-    static int sms = 0;
-    const int k = a.ids ? 1 : 0;
-    if (!per_sm[k]) {
+    // Resident blocks of each instantiation, found once per process (a
+    // function-local static is initialised exactly once, also when contexts
+    // on several threads launch at the same time).
+    struct Occupancy {
+        int sms = 1, per_sm[2] = {1, 1};
+    };
+    static const Occupancy occ = [] {
+        Occupancy o;
         int dev = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (a.ids)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k],
-                                                          agents_persistent_kernel<APT, BS, MINB, true, Trail>, BS, 0);
-        else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[k],
-                                                          agents_persistent_kernel<APT, BS, MINB, false, Trail>, BS, 0);
-        if (per_sm[k] < 1) per_sm[k] = 1;
-        if (sms < 1) sms = 1;
-    }
+        cudaDeviceGetAttribute(&o.sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o.per_sm[0],
+                                                      agents_persistent_kernel<APT, BS, MINB, false, Trail>, BS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o.per_sm[1],
+                                                      agents_persistent_kernel<APT, BS, MINB, true, Trail>, BS, 0);
+        if (o.sms < 1) o.sms = 1;
+        for (int& b : o.per_sm)
+            if (b < 1) b = 1;
+        return o;
+    }();
+    const int k = a.ids ? 1 : 0;
     uint32_t n_groups = (uint32_t)((a.n + APT - 1) / APT);
-    unsigned want = (unsigned)(per_sm[k] * sms);
+    unsigned want = (unsigned)(occ.per_sm[k] * occ.sms);
     unsigned need = blocks_for(n_groups, BS);
     dim3 grid(want < need ? want : need);
     if (a.ids)
