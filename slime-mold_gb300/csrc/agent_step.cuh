@@ -105,9 +105,10 @@ __device__ __forceinline__ Senses<Trail> agent_sense(const DevParams& p, float x
 }
 
 // The rest of the agent (compute.wgsl:72 and 98-144) once its sensor samples
-// are known.  Returns the deposit cell or -1.
+// and its jitter hash `rv` (slm_jitter_hash of its index and pre-move x, y,
+// :117) are known.  Returns the deposit cell or -1.
 __device__ __forceinline__ int agent_finish(const DevParams& p, float& x, float& y, float& angle, float& speed,
-                                            int32_t index, float left, float right, float center) {
+                                            float rv, float left, float right, float center) {
     speed = slm_clamp(speed, p.speed_min, p.speed_max);
 
     // compute.wgsl:98-112: keep straight, or turn toward target = angle -/+ TAU
@@ -118,7 +119,6 @@ __device__ __forceinline__ int agent_finish(const DevParams& p, float& x, float&
     float turned = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
     angle = (turn_left || turn_right) ? turned : angle;
 
-    float rv = slm_jitter_hash(index, x, y);
     angle = slm_add(angle, slm_mul(slm_sub(slm_mul(rv, 2.0f), 1.0f), p.jitter));
     angle = slm_wrap(angle, SLM_WGSL_TWO_PI);
 
@@ -141,7 +141,9 @@ template <class Trail>
 __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,
                                           int32_t index, const Trail& trail) {
     const Senses<Trail> s = agent_sense(p, x, y, angle, trail);
-    return agent_finish(p, x, y, angle, speed, index, Trail::value(s.left), Trail::value(s.right),
+    // the hash needs no sample: it is worked out while the footprints load
+    const float rv = slm_jitter_hash(index, x, y);
+    return agent_finish(p, x, y, angle, speed, rv, Trail::value(s.left), Trail::value(s.right),
                         Trail::value(s.center));
 }
 
