@@ -972,7 +972,8 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
     int rc = SLIME_OK;
     for (uint32_t i = 0; i < n_steps && rc == SLIME_OK; i++) {
         cudaEventRecord(ev[0], ctx->stream);
-        if (ctx->opt.reorder_every && ctx->steps_done % ctx->opt.reorder_every == 0 &&
+        rc = ensure_dispatch_order(ctx);
+        if (rc == SLIME_OK && ctx->opt.reorder_every && ctx->steps_done % ctx->opt.reorder_every == 0 &&
             ctx->last_reorder_step != ctx->steps_done)
             rc = do_reorder(ctx);
         const bool marks = use_marks(ctx);
