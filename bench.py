@@ -463,7 +463,8 @@ def run_reference(args, cfg_name):
                          "sample": f"{steps} of {args.steps} requested full steps (time-bounded at 90 s) after "
                                    f"{warm} warm-up steps; the reference's wgpu path cannot run here "
                                    "(no Rust toolchain, no graphics stack), so the CPU restatement of its shader "
-                                   "is the reference implementation"},
+                                   "(OpenMP, pinned against a mechanical C++ translation of compute.wgsl) is the "
+                                   "reference implementation"},
         "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
