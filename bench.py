@@ -621,7 +621,8 @@ def main():
                                    f"the reference's dispatch: {n_visited} of {n} agents updated per step"},
             "cells_per_s": cells, "pct_roofline_step": pct_roofline,
             "tuned": {"trail_tile": tuned.trail_tile, "agent_shape": tuned.agent_shape,
-                      "trail_texture": tuned.trail_texture, "l2_persist_bytes": tuned.l2_persist_bytes},
+                      "trail_texture": tuned.trail_texture, "l2_persist_bytes": tuned.l2_persist_bytes,
+                      "l2_window_passes": {0: "none", 1: "agents", 2: "trail", 3: "both"}[tuned.l2_window_passes]},
             "kernels": {"agents": k_agents, "trail": k_trail, "other_ms_per_step": other_ms / kern_steps},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
             "cpu_baseline": cpu,

@@ -147,6 +147,9 @@ typedef struct SlimeInfo {
     uint32_t agent_shape;     /* agent-kernel shape index in use */
     uint32_t trail_texture;   /* 1 if the trail buffers have gather textures (texture agent shapes usable) */
     uint64_t l2_persist_bytes; /* persisting-L2 carve-out granted for the trail (0 = none) */
+    uint32_t l2_window_passes; /* with a carve-out, the passes whose launches carry the window
+                                  (bit 0 the agent pass, bit 1 the trail pass) */
+    uint32_t _pad;
 } SlimeInfo;
 
 const char* slime_version(void);

@@ -315,8 +315,8 @@ void setup_l2(slime_ctx* ctx) {
 }
 
 // The access window for a launch that reads (or writes) trail buffer `t`.
-bool trail_window(const slime_ctx* ctx, const float* t, cudaAccessPolicyWindow* w) {
-    if (!ctx->l2_persist_bytes) return false;
+bool trail_window(const slime_ctx* ctx, const float* t, cudaAccessPolicyWindow* w, unsigned pass) {
+    if (!ctx->l2_persist_bytes || !(ctx->l2_window_passes & pass)) return false;
     size_t bytes = (size_t)ctx->W * ctx->H * sizeof(float);
     if (bytes > ctx->l2_max_window) bytes = ctx->l2_max_window;
     w->base_ptr = (void*)t;
@@ -388,7 +388,7 @@ void after_steps(slime_ctx* ctx, bool marks, uint32_t m) {
 cudaError_t enqueue_agents_pass(slime_ctx* ctx, bool marks) {
     const int cur = ctx->cur;
     cudaAccessPolicyWindow wa;
-    bool ha = trail_window(ctx, ctx->trail[cur], &wa);
+    bool ha = trail_window(ctx, ctx->trail[cur], &wa, kWindowAgents);
     return launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, ctx->agent_shape,
                          ha ? &wa : nullptr, ctx->trail_tex[cur], marks ? ctx->marks[cur] : nullptr);
 }
@@ -396,7 +396,7 @@ cudaError_t enqueue_agents_pass(slime_ctx* ctx, bool marks) {
 cudaError_t enqueue_trail_pass(slime_ctx* ctx, bool marks) {
     const int cur = ctx->cur;
     cudaAccessPolicyWindow wt;
-    bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt);
+    bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt, kWindowTrail);
     if (marks)
         return launch_trail_marks(ctx->dev, ctx->tile, ctx->trail[cur], ctx->marks[cur], ctx->trail[1 - cur],
                                   ctx->marks[1 - cur], ctx->stream, ht ? &wt : nullptr);
@@ -480,11 +480,12 @@ int do_reorder(slime_ctx* ctx) {
     return SLIME_OK;
 }
 
-// Whether the persisting-L2 window over the trail pays off for this context:
-// `steps` full steps (an even number) with and without it, twice each in
-// alternation, from a snapshot of the agents and the trail that is put back
-// before every trial and at the end.  Without a snapshot buffer nothing
-// changes.
+// Whether the persisting-L2 window over the trail pays off for this context,
+// and on which passes: `steps` full steps (an even number) with the window on
+// both passes, on the trail pass only, on the agent pass only and without a
+// carve-out, twice each in alternation, from a snapshot of the agents and the
+// trail that is put back before every trial and at the end.  Without a
+// snapshot buffer nothing changes.
 int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
     const size_t cells = (size_t)ctx->W * ctx->H;
     const size_t abytes = 4 * ctx->agents.n_pad * sizeof(float);
@@ -514,12 +515,16 @@ int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
         e = cudaMemcpyAsync(snap + abytes, ctx->trail[cur], tbytes, cudaMemcpyDeviceToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    float total[2] = {0.0f, 0.0f}; // [0] window on, [1] off
+    // the window on both passes, on the trail pass only, on the agent pass
+    // only, and no carve-out at all
+    const unsigned passes[4] = {kWindowAgents | kWindowTrail, kWindowTrail, kWindowAgents, 0};
+    float total[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int round = 0; round < 2 && e == cudaSuccess; round++) {
-        for (int off = 0; off < 2 && e == cudaSuccess; off++) {
-            ctx->l2_tuned_off = off != 0;
+        for (int c = 0; c < 4 && e == cudaSuccess; c++) {
+            ctx->l2_tuned_off = passes[c] == 0;
+            ctx->l2_window_passes = passes[c] ? passes[c] : 3;
             setup_l2(ctx);
-            if (!off && !ctx->l2_persist_bytes) break; // no carve-out to compare with
+            if (c == 0 && !ctx->l2_persist_bytes) break; // no carve-out to compare with
             e = restore();
             for (int w = 0; w < 2 && e == cudaSuccess; w++) e = enqueue_step(ctx, marks);
             if (e == cudaSuccess) e = restore();
@@ -529,12 +534,17 @@ int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float ms = 0.0f;
             if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            total[off] += ms;
+            total[c] += ms;
             ctx->launches += (steps + 2) * kernels_per_step(ctx, marks);
         }
     }
-    const bool measured = e == cudaSuccess && total[0] > 0.0f && total[1] > 0.0f;
-    ctx->l2_tuned_off = measured && total[1] < total[0];
+    int best = 0;
+    const bool measured = e == cudaSuccess && total[0] > 0.0f && total[3] > 0.0f;
+    if (measured)
+        for (int c = 1; c < 4; c++)
+            if (total[c] > 0.0f && total[c] < total[best]) best = c;
+    ctx->l2_tuned_off = passes[best] == 0;
+    ctx->l2_window_passes = passes[best] ? passes[best] : 3;
     setup_l2(ctx);
     cudaError_t re = restore();
     if (re == cudaSuccess) re = cudaStreamSynchronize(ctx->stream);
@@ -704,6 +714,7 @@ int slime_set_options(slime_ctx* ctx, const SlimeOptions* o) {
     if (ctx->opt.graph_chunk == 0) ctx->opt.graph_chunk = 50;
     if (l2_changed) {
         ctx->l2_tuned_off = false;
+        ctx->l2_window_passes = 3;
         setup_l2(ctx);
         invalidate_graphs(ctx);
     }
@@ -734,6 +745,8 @@ int slime_get_info(const slime_ctx* ctx, SlimeInfo* out) {
     out->agent_shape = (uint32_t)ctx->agent_shape;
     out->trail_texture = ctx->trail_tex[0] && ctx->trail_tex[1] ? 1u : 0u;
     out->l2_persist_bytes = ctx->l2_persist_bytes;
+    out->l2_window_passes = ctx->l2_persist_bytes ? ctx->l2_window_passes : 0u;
+    out->_pad = 0;
     out->reordered = ctx->reordered ? 1u : 0u;
     return SLIME_OK;
 }
@@ -853,6 +866,7 @@ int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height) {
     ctx->dev = d;
     ctx->tuned_tile = -1;
     ctx->l2_tuned_off = false;
+    ctx->l2_window_passes = 3;
     setup_l2(ctx);
     CK(cudaStreamSynchronize(ctx->stream), "resizing");
     return SLIME_OK;
@@ -1116,6 +1130,7 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
     // 3. the persisting-L2 window, with the tile and shape just chosen
     if (ctx->opt.l2_persist && ctx->agents.n > 0) {
         ctx->l2_tuned_off = false;
+        ctx->l2_window_passes = 3;
         setup_l2(ctx);
         if (ctx->l2_persist_bytes) return tune_l2_window(ctx, 2 * (reps < 5 ? 5 : reps));
     }

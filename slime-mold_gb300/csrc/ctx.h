@@ -48,6 +48,9 @@ struct slime_ctx {
     size_t l2_persist_bytes = 0; // carve-out granted to this context
     size_t l2_max_window = 0;    // cudaDevAttrMaxAccessPolicyWindowSize
     bool l2_tuned_off = false;   // the autotuner measured the steps faster without it
+    // which passes carry the window when a carve-out is granted (bit 0 the
+    // agent pass, bit 1 the trail pass; the autotuner may keep only one)
+    unsigned l2_window_passes = 3;
 
     std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs; // (steps, start parity) -> graph
 
@@ -108,6 +111,7 @@ int ensure_dispatch_order(slime_ctx* ctx);
 int run_steps(slime_ctx* ctx, uint32_t n);
 void free_adjoint(slime_ctx* ctx);
 void setup_l2(slime_ctx* ctx);
-bool trail_window(const slime_ctx* ctx, const float* t, cudaAccessPolicyWindow* w);
+constexpr unsigned kWindowAgents = 1, kWindowTrail = 2;
+bool trail_window(const slime_ctx* ctx, const float* t, cudaAccessPolicyWindow* w, unsigned pass);
 
 } // namespace slime

@@ -107,6 +107,8 @@ class SlimeInfo(C.Structure):
         ("agent_shape", C.c_uint32),
         ("trail_texture", C.c_uint32),
         ("l2_persist_bytes", C.c_uint64),
+        ("l2_window_passes", C.c_uint32),
+        ("_pad", C.c_uint32),
     ]
 
 
