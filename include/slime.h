@@ -235,8 +235,11 @@ int slime_reorder_agents(slime_ctx* ctx);
 int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, double* trail_ms,
                         double* other_ms);
 /* Pick the fastest trail tile and agent-kernel shape for this context by
- * timing each candidate (agents and trail are restored afterwards; the
- * previous step's deposit counts are cleared). */
+ * timing each candidate in the deposit mode the steps will use, then (with
+ * l2_persist on) whether and on which passes the persisting-L2 window pays
+ * off, by timing full steps (agents and trail are restored afterwards; the
+ * previous step's deposit counts are cleared).  SlimeInfo reports the
+ * choices. */
 int slime_autotune(slime_ctx* ctx, uint32_t reps);
 
 /* ------------------------------------------------ adjoint (frozen trajectories) */
