@@ -601,6 +601,32 @@ def main():
                                        "slime_download_trail_async of the new trail into pinned host memory "
                                        "(copy overlapped with the next step; all copies waited for)"}
 
+    # -- the reference's own frame loop end to end (src/main.rs:1163-1235):
+    # per step the parameter block, slime_step(1) and the display pass
+    # (display.wgsl) at the reference's default 1600x900 window, the frame
+    # read back into pinned host memory for a host-side presenter
+    tw, th = 1600, 900
+    lut = np.random.default_rng(0).integers(0, 256, 768).astype(np.uint8)  # a LUT's shape; values do not matter
+    frames = [torch.empty((th, tw, 4), dtype=torch.uint8, pin_memory=True).numpy() for _ in range(2)]
+    sim.set_params(params)
+    sim.step(1)
+    sim.colorize_async(lut, frames[0])
+    sim.wait_download()
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        sim.set_params(params)
+        sim.step(1)
+        sim.colorize_async(lut, frames[i % 2])
+    sim.wait_download()
+    dt = time.perf_counter() - t0
+    _, _, e2e_display_value = aggregate_ranks(dt * 1e3, n * e2e_steps)
+    e2e_display = {"value": e2e_display_value, "unit": "agent-steps/s",
+                   "h2d_bytes_per_step": 72, "d2h_bytes_per_step": tw * th * 4, "steps": e2e_steps,
+                   "what": "per step: slime_set_params (72-byte parameter block), slime_step(1), "
+                           "slime_colorize_async of the display pass into a 1600x900 RGBA8 frame in pinned "
+                           "host memory (copy overlapped with the next step; all copies waited for)"}
+
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -624,7 +650,8 @@ def main():
                       "trail_texture": tuned.trail_texture, "l2_persist_bytes": tuned.l2_persist_bytes,
                       "l2_window_passes": {0: "none", 1: "agents", 2: "trail", 3: "both"}[tuned.l2_window_passes]},
             "kernels": {"agents": k_agents, "trail": k_trail, "other_ms_per_step": other_ms / kern_steps},
-            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
+            "roofline": roofline, "e2e": e2e, "e2e_display": e2e_display, "gpu_launches": launches,
+            "clocks": clocks.summary(),
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

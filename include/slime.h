@@ -319,6 +319,15 @@ int slime_step_noalloc(const SlimeParams* params, uint32_t width, uint32_t heigh
  * into an RGBA8 image of tex_width x tex_height with the same aspect fit. */
 int slime_colorize(slime_ctx* ctx, const uint8_t* lut768, uint32_t tex_width, uint32_t tex_height,
                    uint8_t* rgba_out);
+/* The same without stalling the step loop (the per-frame display of
+ * src/main.rs:1199-1212 fed to a host presenter): colourise the current trail
+ * on the context's stream and copy the image to `rgba_out` on the copy stream
+ * slime_download_trail_async uses, overlapping the steps enqueued after it.
+ * Returns at once; `rgba_out` is complete after slime_wait_download (or the
+ * next asynchronous download).  The LUT is uploaded only when its bytes
+ * change.  With page-locked `rgba_out` the copy is asynchronous. */
+int slime_colorize_async(slime_ctx* ctx, const uint8_t* lut768, uint32_t tex_width, uint32_t tex_height,
+                         uint8_t* rgba_out);
 
 #ifdef __cplusplus
 }

@@ -667,6 +667,8 @@ void slime_destroy(slime_ctx* ctx) {
     if (ctx->reorder.buf) dev_free(ctx->reorder.buf);
     if (ctx->aux) dev_free(ctx->aux);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->display_lut) dev_free(ctx->display_lut);
+    if (ctx->display_image) dev_free(ctx->display_image);
     if (ctx->display_snap) dev_free(ctx->display_snap);
     if (ctx->snap_ready) cudaEventDestroy(ctx->snap_ready);
     if (ctx->copy_done) cudaEventDestroy(ctx->copy_done);
@@ -1134,6 +1136,48 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
         setup_l2(ctx);
         if (ctx->l2_persist_bytes) return tune_l2_window(ctx, 2 * (reps < 5 ? 5 : reps));
     }
+    return SLIME_OK;
+}
+
+int slime_colorize_async(slime_ctx* ctx, const uint8_t* lut768, uint32_t tw, uint32_t th, uint8_t* rgba_out) {
+    if (!ctx || !lut768 || !rgba_out || tw == 0 || th == 0) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (!ctx->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "creating copy stream");
+        CK(cudaEventCreateWithFlags(&ctx->snap_ready, cudaEventDisableTiming), "creating event");
+        CK(cudaEventCreateWithFlags(&ctx->copy_done, cudaEventDisableTiming), "creating event");
+    }
+    const size_t bytes = (size_t)tw * th * 4;
+    if (ctx->display_image_bytes != bytes) {
+        if (ctx->copy_pending) CK(cudaEventSynchronize(ctx->copy_done), "waiting for the previous copy");
+        ctx->copy_pending = false;
+        if (ctx->display_image) dev_free(ctx->display_image);
+        ctx->display_image = nullptr;
+        ctx->display_image_bytes = 0;
+        CK(dev_alloc((void**)&ctx->display_image, bytes), "allocating display image");
+        ctx->display_image_bytes = bytes;
+    }
+    if (!ctx->display_lut) CK(dev_alloc((void**)&ctx->display_lut, 768), "allocating display LUT");
+    if (!ctx->display_lut_valid || memcmp(ctx->display_lut_host, lut768, 768) != 0) {
+        // a copy from pageable memory waits for the stream: only when the LUT changes
+        memcpy(ctx->display_lut_host, lut768, 768);
+        CK(cudaMemcpyAsync(ctx->display_lut, ctx->display_lut_host, 768, cudaMemcpyHostToDevice, ctx->stream),
+           "uploading LUT");
+        CK(cudaStreamSynchronize(ctx->stream), "uploading LUT");
+        ctx->display_lut_valid = true;
+    }
+    // the previous host copy may still read the image: finish it before overwriting
+    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_done, 0), "ordering copies");
+    CK(launch_colorize(ctx->trail[ctx->cur], ctx->W, ctx->H, ctx->display_lut, tw, th, ctx->display_image,
+                       ctx->stream),
+       "colourising");
+    ctx->launches += 1;
+    CK(cudaEventRecord(ctx->snap_ready, ctx->stream), "recording image");
+    CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->snap_ready, 0), "ordering copies");
+    CK(cudaMemcpyAsync(rgba_out, ctx->display_image, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream),
+       "copying the image to the host");
+    CK(cudaEventRecord(ctx->copy_done, ctx->copy_stream), "recording copy");
+    ctx->copy_pending = true;
     return SLIME_OK;
 }
 

@@ -61,6 +61,13 @@ struct slime_ctx {
     size_t staging_bytes = 0;
     void* aux = nullptr; // display buffer
     size_t aux_bytes = 0;
+    // slime_colorize_async: the LUT on the device (uploaded when it changes)
+    // and the image the copy stream reads
+    uint8_t* display_lut = nullptr;
+    uint8_t display_lut_host[768] = {};
+    bool display_lut_valid = false;
+    uint8_t* display_image = nullptr;
+    size_t display_image_bytes = 0;
 
     // Asynchronous display feed: device snapshot + copy stream.
     cudaStream_t copy_stream = nullptr;

@@ -259,6 +259,17 @@ class Simulation:
                                            img.ctypes.data_as(_abi.U8P)), "colorize")
         return img
 
+    def colorize_async(self, lut768, out):
+        """Start colourising the current trail into `out` (a C-contiguous
+        (height, width, 4) uint8 image, ideally page-locked); complete after
+        wait_download()."""
+        lut = np.ascontiguousarray(lut768, dtype=np.uint8).reshape(-1)
+        if lut.size != 768:
+            raise ValueError("a LUT has 768 bytes (R[256] G[256] B[256])")
+        assert out.dtype == np.uint8 and out.flags.c_contiguous and out.ndim == 3 and out.shape[2] == 4
+        self._check(self._L.slime_colorize_async(self._h, lut.ctypes.data_as(_abi.U8P), out.shape[1], out.shape[0],
+                                                 out.ctypes.data_as(_abi.U8P)), "colorize_async")
+
 
 class Ensemble:
     """Independent colonies of uneven sizes advanced together."""

@@ -182,6 +182,7 @@ SIGNATURES = {
     "slime_ensemble_launch_count": (C.c_int, [P, C.POINTER(C.c_uint64)]),
     "slime_ensemble_selftest_barrier_timeout": (C.c_int, [P]),
     "slime_colorize": (C.c_int, [P, U8P, C.c_uint32, C.c_uint32, U8P]),
+    "slime_colorize_async": (C.c_int, [P, U8P, C.c_uint32, C.c_uint32, U8P]),
     "slime_step_noalloc": (C.c_int, [C.POINTER(SlimeParams), C.c_uint32, C.c_uint32, C.c_uint64, P, P, P, P, P, P,
                                      P]),
 }

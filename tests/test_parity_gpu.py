@@ -333,6 +333,31 @@ def test_colorize_matches_display_pass(gpu):
         assert np.array_equal(sim.colorize(lut, tw, th), oracle.colorize(W, H, trail, lut, tw, th)), (tw, th)
 
 
+def test_colorize_async_frames(gpu):
+    """slime_colorize_async between steps, as a frame loop calls it: each
+    frame is the oracle's colourise of the trail of its step, across a LUT
+    change, a new image size, and page-locked as well as pageable images."""
+    import torch
+    W, H, n = 300, 170, 20000
+    agents = agents_uniform(n, W, H, 1.0, 2.0, seed=41)
+    sim = make_sim(W, H, n, config0_params(W, H), agents)
+    rng = np.random.default_rng(42)
+    luts = [rng.integers(0, 256, 768, dtype=np.uint8) for _ in range(2)]
+    for frame, (tw, th, lut, pinned) in enumerate([(160, 90, luts[0], True), (160, 90, luts[0], True),
+                                                   (160, 90, luts[1], False), (90, 160, luts[1], True)]):
+        sim.step(3)
+        trail = sim.download_trail()
+        if pinned:
+            out = torch.empty((th, tw, 4), dtype=torch.uint8, pin_memory=True).numpy()
+        else:
+            out = np.empty((th, tw, 4), np.uint8)
+        sim.colorize_async(lut, out)
+        sim.step(2)  # steps enqueued after the frame do not change it
+        sim.wait_download()
+        assert np.array_equal(out, oracle.colorize(W, H, trail, lut, tw, th)), f"frame {frame}"
+    sim.close()
+
+
 def test_async_display_feed_snapshots_the_current_trail(gpu):
     """slime_download_trail_async copies the trail as it was at the call,
     while later steps proceed."""
