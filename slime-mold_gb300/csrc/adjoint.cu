@@ -233,7 +233,7 @@ int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every) 
         const bool marks = use_marks(ctx);
         int prc = prepare_deposits(ctx, marks);
         if (prc != SLIME_OK) return prc;
-        CK(enqueue_step(ctx, marks), "recording a step");
+        CK(enqueue_step(ctx, marks, false), "recording a step");
         after_steps(ctx, marks, 1);
         ctx->launches += kernels_per_step(ctx, marks);
         ctx->steps_done++;

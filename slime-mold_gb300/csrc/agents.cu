@@ -98,6 +98,10 @@ __global__ void __launch_bounds__(BS, MINB) agents_kernel(const __grid_constant_
 #pragma unroll
         for (int j = 0; j < APT; j++) id[j] = (uint32_t)(base + j);
     }
+    // the state is not written by the trail pass this launch may follow; the
+    // trail it senses and the deposit record are
+    pdl_wait();
+    pdl_trigger();
     int cell[APT];
     if (base + APT <= n) {
         // full group: no per-agent branch, so the agents' work can interleave
@@ -192,6 +196,10 @@ __global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
     Lanes<APT>::load(TH + base, th);
     Lanes<APT>::load(V + base, v);
     if (kIds) Lanes<APT>::load_ids(ids + base, id);
+    // the first group's state is not written by the trail pass this launch may
+    // follow; the trail it senses and the deposit record are
+    pdl_wait();
+    pdl_trigger();
     while (true) {
         const uint32_t gn = g + stride;
         const bool more = gn < n_groups;
@@ -260,7 +268,7 @@ __global__ void extra_deposits_kernel(const float* __restrict__ X, const float* 
 
 template <int APT, int BS, int MINB, class Trail>
 cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
-                                     uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win) {
+                                     uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl) {
     // Resident blocks of each instantiation, found once per process (a
     // function-local static is initialised exactly once, also when contexts
     // on several threads launch at the same time).
@@ -287,21 +295,21 @@ cudaError_t launch_agents_persistent(const DevParams& p, const AgentsSoA& a, con
     unsigned need = blocks_for(n_groups, BS);
     dim3 grid(want < need ? want : need);
     if (a.ids)
-        return launch_k(agents_persistent_kernel<APT, BS, MINB, true, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y,
+        return launch_kp(agents_persistent_kernel<APT, BS, MINB, true, Trail>, grid, dim3(BS), 0, s, win, pdl, p, a.x, a.y,
                         a.th, a.v, (const uint32_t*)a.ids, trail, counts, marks, n_groups, a.n);
-    return launch_k(agents_persistent_kernel<APT, BS, MINB, false, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y,
+    return launch_kp(agents_persistent_kernel<APT, BS, MINB, false, Trail>, grid, dim3(BS), 0, s, win, pdl, p, a.x, a.y,
                     a.th, a.v, (const uint32_t*)nullptr, trail, counts, marks, n_groups, a.n);
 }
 
 template <int APT, int BS, int MINB, class Trail>
 cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const Trail& trail, uint32_t* counts,
-                                  uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win) {
+                                  uint8_t* marks, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl) {
     uint32_t n_groups = (uint32_t)((a.n + APT - 1) / APT);
     dim3 grid(blocks_for(n_groups, BS));
     if (a.ids)
-        return launch_k(agents_kernel<APT, BS, MINB, true, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+        return launch_kp(agents_kernel<APT, BS, MINB, true, Trail>, grid, dim3(BS), 0, s, win, pdl, p, a.x, a.y, a.th, a.v,
                         (const uint32_t*)a.ids, trail, counts, marks, n_groups, a.n);
-    return launch_k(agents_kernel<APT, BS, MINB, false, Trail>, grid, dim3(BS), 0, s, win, p, a.x, a.y, a.th, a.v,
+    return launch_kp(agents_kernel<APT, BS, MINB, false, Trail>, grid, dim3(BS), 0, s, win, pdl, p, a.x, a.y, a.th, a.v,
                     (const uint32_t*)nullptr, trail, counts, marks, n_groups, a.n);
 }
 
@@ -337,14 +345,14 @@ int agent_pass_kernels(const DevParams& p, uint64_t n, bool marks) {
 
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
                           cudaStream_t s, int shape, const cudaAccessPolicyWindow* win, cudaTextureObject_t tex,
-                          uint8_t* marks) {
+                          uint8_t* marks, bool pdl) {
     if (a.n == 0) return cudaSuccess;
     if (p.dispatch_mode == SLIME_DISPATCH_REFERENCE) {
         AgentsSoA updated = a;
         updated.n = reference_dispatch_updated(a.n);
         DevParams each = p;
         each.dispatch_mode = SLIME_DISPATCH_EACH_AGENT;
-        cudaError_t e = launch_agents(each, updated, trail, counts, s, shape, win, tex, marks);
+        cudaError_t e = launch_agents(each, updated, trail, counts, s, shape, win, tex, marks, pdl);
         if (e != cudaSuccess || agent_pass_kernels(p, a.n, marks) == 1) return e;
         uint32_t wy = 0, span = 0;
         slm_dispatch_geometry(a.n, &wy, &span);
@@ -356,27 +364,27 @@ cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* t
     if (agent_shape_uses_texture(shape) && tex) {
         const TrailTex tt{tex};
         switch (shape) {
-        case 12: return launch_agents_variant<2, 256, 0>(p, a, tt, counts, marks, s, win);
-        case 13: return launch_agents_persistent<2, 256, 0>(p, a, tt, counts, marks, s, win);
-        default: return launch_agents_persistent<2, 128, 0>(p, a, tt, counts, marks, s, win);
+        case 12: return launch_agents_variant<2, 256, 0>(p, a, tt, counts, marks, s, win, pdl);
+        case 13: return launch_agents_persistent<2, 256, 0>(p, a, tt, counts, marks, s, win, pdl);
+        default: return launch_agents_persistent<2, 128, 0>(p, a, tt, counts, marks, s, win, pdl);
         }
     }
     switch (shape) {
     case 1:
-    case 12: return launch_agents_variant<2, 256, 0>(p, a, tp, counts, marks, s, win);
-    case 2: return launch_agents_variant<1, 256, 0>(p, a, tp, counts, marks, s, win);
-    case 3: return launch_agents_variant<4, 128, 0>(p, a, tp, counts, marks, s, win);
-    case 4: return launch_agents_variant<1, 128, 0>(p, a, tp, counts, marks, s, win);
-    case 5: return launch_agents_variant<2, 256, 5>(p, a, tp, counts, marks, s, win);
-    case 6: return launch_agents_variant<2, 256, 6>(p, a, tp, counts, marks, s, win);
-    case 7: return launch_agents_variant<4, 256, 4>(p, a, tp, counts, marks, s, win);
-    case 8: return launch_agents_variant<1, 256, 8>(p, a, tp, counts, marks, s, win);
+    case 12: return launch_agents_variant<2, 256, 0>(p, a, tp, counts, marks, s, win, pdl);
+    case 2: return launch_agents_variant<1, 256, 0>(p, a, tp, counts, marks, s, win, pdl);
+    case 3: return launch_agents_variant<4, 128, 0>(p, a, tp, counts, marks, s, win, pdl);
+    case 4: return launch_agents_variant<1, 128, 0>(p, a, tp, counts, marks, s, win, pdl);
+    case 5: return launch_agents_variant<2, 256, 5>(p, a, tp, counts, marks, s, win, pdl);
+    case 6: return launch_agents_variant<2, 256, 6>(p, a, tp, counts, marks, s, win, pdl);
+    case 7: return launch_agents_variant<4, 256, 4>(p, a, tp, counts, marks, s, win, pdl);
+    case 8: return launch_agents_variant<1, 256, 8>(p, a, tp, counts, marks, s, win, pdl);
     case 9:
-    case 13: return launch_agents_persistent<2, 256, 0>(p, a, tp, counts, marks, s, win);
-    case 10: return launch_agents_persistent<1, 256, 0>(p, a, tp, counts, marks, s, win);
+    case 13: return launch_agents_persistent<2, 256, 0>(p, a, tp, counts, marks, s, win, pdl);
+    case 10: return launch_agents_persistent<1, 256, 0>(p, a, tp, counts, marks, s, win, pdl);
     case 11:
-    case 14: return launch_agents_persistent<2, 128, 0>(p, a, tp, counts, marks, s, win);
-    default: return launch_agents_variant<4, 256, 0>(p, a, tp, counts, marks, s, win);
+    case 14: return launch_agents_persistent<2, 128, 0>(p, a, tp, counts, marks, s, win, pdl);
+    default: return launch_agents_variant<4, 256, 0>(p, a, tp, counts, marks, s, win, pdl);
     }
 }
 

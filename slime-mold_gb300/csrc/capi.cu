@@ -384,30 +384,36 @@ void after_steps(slime_ctx* ctx, bool marks, uint32_t m) {
 
 // The two passes of one step on the context's stream (also used under
 // capture).  The agent pass keeps the trail it senses resident; the trail
-// pass marks the trail it writes, which the next agent pass senses.
-cudaError_t enqueue_agents_pass(slime_ctx* ctx, bool marks) {
+// pass marks the trail it writes, which the next agent pass senses.  With
+// `pdl` a pass is a programmatic dependent of the kernel just before it in
+// the stream: the other pass of this context.
+cudaError_t enqueue_agents_pass(slime_ctx* ctx, bool marks, bool pdl) {
     const int cur = ctx->cur;
     cudaAccessPolicyWindow wa;
     bool ha = trail_window(ctx, ctx->trail[cur], &wa, kWindowAgents);
     return launch_agents(ctx->dev, ctx->agents, ctx->trail[cur], ctx->counts[cur], ctx->stream, ctx->agent_shape,
-                         ha ? &wa : nullptr, ctx->trail_tex[cur], marks ? ctx->marks[cur] : nullptr);
+                         ha ? &wa : nullptr, ctx->trail_tex[cur], marks ? ctx->marks[cur] : nullptr, pdl);
 }
 
-cudaError_t enqueue_trail_pass(slime_ctx* ctx, bool marks) {
+cudaError_t enqueue_trail_pass(slime_ctx* ctx, bool marks, bool pdl) {
     const int cur = ctx->cur;
     cudaAccessPolicyWindow wt;
     bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt, kWindowTrail);
     if (marks)
         return launch_trail_marks(ctx->dev, ctx->tile, ctx->trail[cur], ctx->marks[cur], ctx->trail[1 - cur],
-                                  ctx->marks[1 - cur], ctx->stream, ht ? &wt : nullptr);
+                                  ctx->marks[1 - cur], ctx->stream, ht ? &wt : nullptr, pdl);
     return launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                        ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr);
+                        ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr, pdl);
 }
 
-cudaError_t enqueue_step(slime_ctx* ctx, bool marks) {
-    cudaError_t e = enqueue_agents_pass(ctx, marks);
+// `chained`: the operation before this step on the stream is the previous
+// step's trail pass, so the agent pass may start while it finishes; the trail
+// pass always follows the agent pass's kernel when there are agents.
+cudaError_t enqueue_step(slime_ctx* ctx, bool marks, bool chained) {
+    const bool agents = ctx->agents.n > 0;
+    cudaError_t e = enqueue_agents_pass(ctx, marks, chained && agents);
     if (e != cudaSuccess) return e;
-    e = enqueue_trail_pass(ctx, marks);
+    e = enqueue_trail_pass(ctx, marks, agents);
     if (e != cudaSuccess) return e;
     ctx->cur = 1 - ctx->cur;
     return cudaSuccess;
@@ -419,7 +425,7 @@ uint64_t kernels_per_step(const slime_ctx* ctx, bool marks) {
 
 int run_steps_direct(slime_ctx* ctx, uint32_t m, bool marks) {
     for (uint32_t i = 0; i < m; i++) {
-        CK(enqueue_step(ctx, marks), "launching a step");
+        CK(enqueue_step(ctx, marks, i > 0), "launching a step");
         ctx->launches += kernels_per_step(ctx, marks);
         ctx->steps_done++;
     }
@@ -435,7 +441,7 @@ int run_steps_graph(slime_ctx* ctx, uint32_t m, bool marks) {
         const int saved = ctx->cur;
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "beginning graph capture");
         cudaError_t ce = cudaSuccess;
-        for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_step(ctx, marks);
+        for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_step(ctx, marks, i > 0);
         cudaGraph_t graph = nullptr;
         cudaError_t ee = cudaStreamEndCapture(ctx->stream, &graph);
         ctx->cur = saved;
@@ -526,10 +532,10 @@ int tune_l2_window(slime_ctx* ctx, uint32_t steps) {
             setup_l2(ctx);
             if (c == 0 && !ctx->l2_persist_bytes) break; // no carve-out to compare with
             e = restore();
-            for (int w = 0; w < 2 && e == cudaSuccess; w++) e = enqueue_step(ctx, marks);
+            for (int w = 0; w < 2 && e == cudaSuccess; w++) e = enqueue_step(ctx, marks, w > 0);
             if (e == cudaSuccess) e = restore();
             if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
-            for (uint32_t i = 0; i < steps && e == cudaSuccess; i++) e = enqueue_step(ctx, marks);
+            for (uint32_t i = 0; i < steps && e == cudaSuccess; i++) e = enqueue_step(ctx, marks, i > 0);
             if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float ms = 0.0f;
@@ -996,9 +1002,9 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
         if (rc == SLIME_OK) rc = prepare_deposits(ctx, marks);
         if (rc != SLIME_OK) break;
         cudaEventRecord(ev[1], ctx->stream);
-        cudaError_t e = enqueue_agents_pass(ctx, marks);
+        cudaError_t e = enqueue_agents_pass(ctx, marks, false);
         cudaEventRecord(ev[2], ctx->stream);
-        if (e == cudaSuccess) e = enqueue_trail_pass(ctx, marks);
+        if (e == cudaSuccess) e = enqueue_trail_pass(ctx, marks, false);
         cudaEventRecord(ev[3], ctx->stream);
         if (e != cudaSuccess) {
             rc = cuda_error(ctx->err, e, "profiling a step");

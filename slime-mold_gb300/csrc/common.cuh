@@ -39,24 +39,46 @@ struct DevParams {
     float w2sum_m1; // (sum of w)^2 - 1 in binary64, rounded: B(u) - u = sum w w (u_n - u_c) + this * u_c
 };
 
+// Programmatic dependent launch: a kernel launched with `pdl` set (below)
+// may start while the kernel before it in the stream finishes.  It runs what
+// does not depend on that kernel, then pdl_wait() returns once that kernel has
+// completed and its writes are visible (at once for a launch without such a
+// predecessor).  pdl_trigger() lets the next such kernel start launching once
+// every block of this grid has triggered or exited.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Launch `k` with an optional persisting-L2 access window attached to this
-// launch (captured into graphs as a kernel-node attribute).
+// launch and, with `pdl`, as a programmatic dependent of the kernel before it
+// in the stream (both captured into graphs as kernel-node attributes).
 template <typename... KArgs, typename... Args>
-cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                     const cudaAccessPolicyWindow* win, Args&&... args) {
+cudaError_t launch_kp(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                      const cudaAccessPolicyWindow* win, bool pdl, Args&&... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
+    unsigned n = 0;
     if (win) {
-        attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
-        attr[0].val.accessPolicyWindow = *win;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
+        attr[n].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[n].val.accessPolicyWindow = *win;
+        n++;
     }
+    if (pdl) {
+        attr[n].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[n].val.programmaticStreamSerializationAllowed = 1;
+        n++;
+    }
+    cfg.attrs = n ? attr : nullptr;
+    cfg.numAttrs = n;
     return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+template <typename... KArgs, typename... Args>
+cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                     const cudaAccessPolicyWindow* win, Args&&... args) {
+    return launch_kp(k, grid, block, smem, s, win, false, std::forward<Args>(args)...);
 }
 
 // Device allocations of the library go through these two functions.  When

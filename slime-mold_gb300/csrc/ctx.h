@@ -109,7 +109,7 @@ void invalidate_graphs(slime_ctx* ctx);
 bool marks_allowed(const slime_ctx* ctx);
 bool use_marks(const slime_ctx* ctx);
 int prepare_deposits(slime_ctx* ctx, bool marks);
-cudaError_t enqueue_step(slime_ctx* ctx, bool marks);
+cudaError_t enqueue_step(slime_ctx* ctx, bool marks, bool chained);
 void after_steps(slime_ctx* ctx, bool marks, uint32_t m);
 uint64_t kernels_per_step(const slime_ctx* ctx, bool marks);
 // Reorder first if the reference's dispatch is on and the slots do not hold

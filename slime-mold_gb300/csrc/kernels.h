@@ -40,9 +40,11 @@ bool agent_shape_uses_texture(int index);
 // dispatch updates must fill the first reference_dispatch_updated(a.n)
 // slots (identity ids, or a reorder given that count): the pass updates those
 // and, when counting, adds the extra deposits of multiply visited agents.
+// With `pdl` the launch is a programmatic dependent of the kernel before it
+// in the stream, which must be the trail pass (or no kernel of this library).
 cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* trail, uint32_t* counts,
                           cudaStream_t s, int shape = 0, const cudaAccessPolicyWindow* win = nullptr,
-                          cudaTextureObject_t tex = 0, uint8_t* marks = nullptr);
+                          cudaTextureObject_t tex = 0, uint8_t* marks = nullptr, bool pdl = false);
 // Kernels one launch_agents call enqueues.
 int agent_pass_kernels(const DevParams& p, uint64_t n, bool marks);
 // How many agents (ids 0 .. this - 1) the reference's dispatch updates.
@@ -69,15 +71,20 @@ int trail_tile_default();
 bool trail_tile_supported(const DevParams& p, int tile);
 // Fused trail pass: out = Diffuse(Decay(Fold(in, counts_in))); zeroes
 // counts_zero (the other step's count buffer, may be null) over the same cells.
+// With `pdl` a streaming tile launches as a programmatic dependent of the
+// kernel before it in the stream (the agent pass); the shared-memory tiles
+// always launch in order.
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
-                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr);
+                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr,
+                         bool pdl = false);
 // Whether tile `index` is a streaming tile that runs here (the only ones that
 // read deposit marks).
 bool trail_tile_streams(const DevParams& p, int tile);
 // The same pass folding per-cell byte marks (0/1) instead of counts; zeroes
 // marks_zero.  Streaming tiles only (cudaErrorInvalidValue otherwise).
 cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, const uint8_t* marks_in, float* out,
-                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr);
+                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr,
+                               bool pdl = false);
 
 // ---- adjoint.cu
 // One backward step of the frozen-trajectory chain: from g_in = dL/dT_{s+1}

@@ -109,25 +109,28 @@ __global__ void __launch_bounds__(128) trail_stream_kernel(const __grid_constant
                                                            float* __restrict__ out, D* __restrict__ czero,
                                                            int warps_x) {
     const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
+    // the deposit record this reads is the agent pass's output
+    pdl_wait();
+    pdl_trigger();
     process_strip<R, kGauss, ROWS, false, true, D>(p, in, cin, out, czero, gw % warps_x, gw / warps_x);
 }
 
 template <int R, bool kGauss, int ROWS, class D>
 cudaError_t launch_stream(const DevParams& p, const float* in, const D* cin, float* out, D* cz, cudaStream_t s,
-                          const cudaAccessPolicyWindow* win) {
+                          const cudaAccessPolicyWindow* win, bool pdl) {
     int warps_x = (p.W + 127) / 128;
     long long warps = (long long)warps_x * ((p.H + ROWS - 1) / ROWS);
     unsigned blocks = (unsigned)((warps + 3) / 4);
-    return launch_k(trail_stream_kernel<R, kGauss, ROWS, D>, dim3(blocks), dim3(128), 0, s, win, p, in, cin, out,
-                    cz, warps_x);
+    return launch_kp(trail_stream_kernel<R, kGauss, ROWS, D>, dim3(blocks), dim3(128), 0, s, win, pdl, p, in, cin,
+                     out, cz, warps_x);
 }
 
 template <int ROWS, class D>
 cudaError_t launch_stream_rows(const DevParams& p, const float* in, const D* cin, float* out, D* cz, cudaStream_t s,
-                               const cudaAccessPolicyWindow* win) {
-    if (p.blur_mode != SLIME_BLUR_GAUSS) return launch_stream<1, false, ROWS, D>(p, in, cin, out, cz, s, win);
-    if (p.R == 1) return launch_stream<1, true, ROWS, D>(p, in, cin, out, cz, s, win);
-    return launch_stream<2, true, ROWS, D>(p, in, cin, out, cz, s, win);
+                               const cudaAccessPolicyWindow* win, bool pdl) {
+    if (p.blur_mode != SLIME_BLUR_GAUSS) return launch_stream<1, false, ROWS, D>(p, in, cin, out, cz, s, win, pdl);
+    if (p.R == 1) return launch_stream<1, true, ROWS, D>(p, in, cin, out, cz, s, win, pdl);
+    return launch_stream<2, true, ROWS, D>(p, in, cin, out, cz, s, win, pdl);
 }
 
 const TrailTile kTiles[] = {{32, 8}, {64, 8}, {32, 16}, {64, 16}, {128, 8}, {128, 16}, {256, 8}};
@@ -200,17 +203,17 @@ bool trail_tile_supported(const DevParams& p, int tile) {
 bool trail_tile_streams(const DevParams& p, int tile) { return tile >= kNumTiles && trail_tile_supported(p, tile); }
 
 cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, const uint8_t* marks_in, float* out,
-                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win) {
+                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl) {
     if (!trail_tile_streams(p, tile)) return cudaErrorInvalidValue;
     switch (tile) {
-    case 7: return launch_stream_rows<8>(p, in, marks_in, out, marks_zero, s, win);
-    case 8: return launch_stream_rows<16>(p, in, marks_in, out, marks_zero, s, win);
-    default: return launch_stream_rows<32>(p, in, marks_in, out, marks_zero, s, win);
+    case 7: return launch_stream_rows<8>(p, in, marks_in, out, marks_zero, s, win, pdl);
+    case 8: return launch_stream_rows<16>(p, in, marks_in, out, marks_zero, s, win, pdl);
+    default: return launch_stream_rows<32>(p, in, marks_in, out, marks_zero, s, win, pdl);
     }
 }
 
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
-                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win) {
+                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl) {
     if (!trail_tile_supported(p, tile)) tile = trail_tile_default();
     switch (tile) {
     case 0: return launch_tile<32, 8>(p, in, counts_in, out, counts_zero, s, win);
@@ -220,9 +223,9 @@ cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const ui
     case 4: return launch_tile<128, 8>(p, in, counts_in, out, counts_zero, s, win);
     case 5: return launch_tile<128, 16>(p, in, counts_in, out, counts_zero, s, win);
     case 6: return launch_tile<256, 8>(p, in, counts_in, out, counts_zero, s, win);
-    case 7: return launch_stream_rows<8>(p, in, counts_in, out, counts_zero, s, win);
-    case 8: return launch_stream_rows<16>(p, in, counts_in, out, counts_zero, s, win);
-    case 9: return launch_stream_rows<32>(p, in, counts_in, out, counts_zero, s, win);
+    case 7: return launch_stream_rows<8>(p, in, counts_in, out, counts_zero, s, win, pdl);
+    case 8: return launch_stream_rows<16>(p, in, counts_in, out, counts_zero, s, win, pdl);
+    case 9: return launch_stream_rows<32>(p, in, counts_in, out, counts_zero, s, win, pdl);
     default: return cudaErrorInvalidValue;
     }
 }
