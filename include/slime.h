@@ -216,8 +216,10 @@ int slime_sync(slime_ctx* ctx);
 /* The cudaStream_t the context enqueues on. */
 int slime_get_stream(slime_ctx* ctx, void** stream);
 /* Display feed without stalling the step loop: snapshot the current trail on
- * the device and copy it to `trail` (width*height floats) on a separate copy
- * stream, so the copy overlaps the steps enqueued after it.  Returns at once;
+ * the device (two snapshot buffers used in turn, so a snapshot waits only for
+ * the copy two calls back) and copy it to `trail` (width*height floats) on a
+ * separate copy stream, so the copy overlaps the steps enqueued after it.
+ * Returns at once;
  * `trail` is complete after slime_wait_download (or the next
  * slime_download_trail_async, which first waits for the previous copy).  With
  * page-locked `trail` the copy is asynchronous; with pageable memory the CUDA

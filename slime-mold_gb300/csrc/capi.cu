@@ -675,7 +675,10 @@ void slime_destroy(slime_ctx* ctx) {
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     if (ctx->display_lut) dev_free(ctx->display_lut);
     if (ctx->display_image) dev_free(ctx->display_image);
-    if (ctx->display_snap) dev_free(ctx->display_snap);
+    for (int b = 0; b < 2; b++) {
+        if (ctx->display_snap[b]) dev_free(ctx->display_snap[b]);
+        if (ctx->snap_copied[b]) cudaEventDestroy(ctx->snap_copied[b]);
+    }
     if (ctx->snap_ready) cudaEventDestroy(ctx->snap_ready);
     if (ctx->copy_done) cudaEventDestroy(ctx->copy_done);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -913,6 +916,19 @@ int slime_get_stream(slime_ctx* ctx, void** stream) {
     return SLIME_OK;
 }
 
+namespace {
+// The copy stream and its events, made at the first asynchronous download.
+int ensure_copy_stream(slime_ctx* ctx) {
+    if (ctx->copy_stream) return SLIME_OK;
+    CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "creating copy stream");
+    CK(cudaEventCreateWithFlags(&ctx->snap_ready, cudaEventDisableTiming), "creating event");
+    CK(cudaEventCreateWithFlags(&ctx->copy_done, cudaEventDisableTiming), "creating event");
+    for (int b = 0; b < 2; b++)
+        CK(cudaEventCreateWithFlags(&ctx->snap_copied[b], cudaEventDisableTiming), "creating event");
+    return SLIME_OK;
+}
+} // namespace
+
 int slime_download_trail_async(slime_ctx* ctx, float* trail, uint64_t n_cells) {
     if (!ctx || !trail) return SLIME_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
@@ -920,28 +936,34 @@ int slime_download_trail_async(slime_ctx* ctx, float* trail, uint64_t n_cells) {
     if (n_cells != cells)
         return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "trail has %llu cells, context has %llu",
                          (unsigned long long)n_cells, (unsigned long long)cells);
-    if (!ctx->copy_stream) {
-        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "creating copy stream");
-        CK(cudaEventCreateWithFlags(&ctx->snap_ready, cudaEventDisableTiming), "creating event");
-        CK(cudaEventCreateWithFlags(&ctx->copy_done, cudaEventDisableTiming), "creating event");
-    }
+    int rc = ensure_copy_stream(ctx);
+    if (rc != SLIME_OK) return rc;
     if (ctx->display_cells != cells) {
         if (ctx->copy_pending) CK(cudaEventSynchronize(ctx->copy_done), "waiting for the previous copy");
         ctx->copy_pending = false;
-        if (ctx->display_snap) dev_free(ctx->display_snap);
-        ctx->display_snap = nullptr;
         ctx->display_cells = 0;
-        CK(dev_alloc((void**)&ctx->display_snap, cells * sizeof(float)), "allocating display snapshot");
+        for (int b = 0; b < 2; b++) {
+            if (ctx->display_snap[b]) dev_free(ctx->display_snap[b]);
+            ctx->display_snap[b] = nullptr;
+            ctx->snap_copy_pending[b] = false;
+        }
+        for (int b = 0; b < 2; b++)
+            CK(dev_alloc((void**)&ctx->display_snap[b], cells * sizeof(float)), "allocating display snapshots");
         ctx->display_cells = cells;
+        ctx->display_next = 0;
     }
-    // the previous host copy reads the snapshot: finish it before overwriting
-    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_done, 0), "ordering copies");
-    CK(cudaMemcpyAsync(ctx->display_snap, ctx->trail[ctx->cur], cells * sizeof(float), cudaMemcpyDeviceToDevice,
+    const int b = ctx->display_next;
+    ctx->display_next = 1 - b;
+    // the host copy that last read this snapshot (two calls back) must be done
+    if (ctx->snap_copy_pending[b]) CK(cudaStreamWaitEvent(ctx->stream, ctx->snap_copied[b], 0), "ordering copies");
+    CK(cudaMemcpyAsync(ctx->display_snap[b], ctx->trail[ctx->cur], cells * sizeof(float), cudaMemcpyDeviceToDevice,
                        ctx->stream), "snapshotting trail");
     CK(cudaEventRecord(ctx->snap_ready, ctx->stream), "recording snapshot");
     CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->snap_ready, 0), "ordering copies");
-    CK(cudaMemcpyAsync(trail, ctx->display_snap, cells * sizeof(float), cudaMemcpyDeviceToHost, ctx->copy_stream),
+    CK(cudaMemcpyAsync(trail, ctx->display_snap[b], cells * sizeof(float), cudaMemcpyDeviceToHost, ctx->copy_stream),
        "copying trail to the host");
+    CK(cudaEventRecord(ctx->snap_copied[b], ctx->copy_stream), "recording copy");
+    ctx->snap_copy_pending[b] = true;
     CK(cudaEventRecord(ctx->copy_done, ctx->copy_stream), "recording copy");
     ctx->copy_pending = true;
     return SLIME_OK;
@@ -1148,11 +1170,8 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
 int slime_colorize_async(slime_ctx* ctx, const uint8_t* lut768, uint32_t tw, uint32_t th, uint8_t* rgba_out) {
     if (!ctx || !lut768 || !rgba_out || tw == 0 || th == 0) return SLIME_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
-    if (!ctx->copy_stream) {
-        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "creating copy stream");
-        CK(cudaEventCreateWithFlags(&ctx->snap_ready, cudaEventDisableTiming), "creating event");
-        CK(cudaEventCreateWithFlags(&ctx->copy_done, cudaEventDisableTiming), "creating event");
-    }
+    int rc = ensure_copy_stream(ctx);
+    if (rc != SLIME_OK) return rc;
     const size_t bytes = (size_t)tw * th * 4;
     if (ctx->display_image_bytes != bytes) {
         if (ctx->copy_pending) CK(cudaEventSynchronize(ctx->copy_done), "waiting for the previous copy");

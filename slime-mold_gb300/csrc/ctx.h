@@ -71,10 +71,15 @@ struct slime_ctx {
 
     // Asynchronous display feed: device snapshot + copy stream.
     cudaStream_t copy_stream = nullptr;
-    float* display_snap = nullptr;
+    // two trail snapshots used in turn, so a snapshot never waits for the
+    // host copy of the one before it, only for the copy two calls back
+    float* display_snap[2] = {nullptr, nullptr};
+    int display_next = 0;
+    cudaEvent_t snap_copied[2] = {nullptr, nullptr}; // last host copy out of display_snap[b] finished
+    bool snap_copy_pending[2] = {false, false};
     size_t display_cells = 0;
     cudaEvent_t snap_ready = nullptr;  // snapshot written (main stream)
-    cudaEvent_t copy_done = nullptr;   // host copy finished (copy stream)
+    cudaEvent_t copy_done = nullptr;   // latest host copy finished (copy stream)
     bool copy_pending = false;
 
     // Adjoint recording (adjoint.cu).

@@ -383,6 +383,28 @@ def test_async_display_feed_snapshots_the_current_trail(gpu):
     assert_bitexact(host, later, "second pinned copy")
 
 
+def test_async_display_feed_back_to_back(gpu):
+    """Downloads issued one after another with steps in between and no wait,
+    as a frame loop does: the two device snapshots are used in turn, and each
+    host buffer receives the trail of its own step."""
+    import torch
+    W, H, n = 256, 128, 20000
+    p = config0_params(W, H)
+    agents = agents_uniform(n, W, H, 1.0, 2.0, seed=33)
+    trail = np.random.default_rng(34).random((H, W), dtype=np.float32)
+    sim = make_sim(W, H, n, p, agents, trail)
+    hosts = [torch.empty((H, W), dtype=torch.float32, pin_memory=True).numpy() for _ in range(5)]
+    for h in hosts:
+        sim.step(2)
+        sim.download_trail_async(h)
+    sim.wait_download()
+    ca, ct = agents.copy(), trail.copy()
+    for k, h in enumerate(hosts):
+        oracle.run(p, W, H, ca, ct, 2)
+        assert_bitexact(h, ct, f"frame {k}")
+    sim.close()
+
+
 def test_checkpoint_resume_continues_bit_identically(gpu, tmp_path):
     import slime_gb300 as sg
     W, H, n = 200, 120, 15000
