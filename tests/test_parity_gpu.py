@@ -402,6 +402,26 @@ def test_async_display_feed_back_to_back(gpu):
     for k, h in enumerate(hosts):
         oracle.run(p, W, H, ca, ct, 2)
         assert_bitexact(h, ct, f"frame {k}")
+    # a resize while a copy is in flight, then downloads at the new size (new snapshots)
+    pending = torch.empty((H, W), dtype=torch.float32, pin_memory=True).numpy()
+    sim.step(1)
+    oracle.run(p, W, H, ca, ct, 1)
+    sim.download_trail_async(pending)
+    W2 = W + 64
+    sim.resize(W2, H)
+    sim.wait_download()
+    assert_bitexact(pending, ct, "copy in flight across a resize")
+    ca[:, 0] = ca[:, 0] * (np.float32(W2) / np.float32(W))  # src/main.rs:987-993
+    ct = np.zeros((H, W2), np.float32)
+    p2 = config0_params(W2, H)
+    hosts2 = [torch.empty((H, W2), dtype=torch.float32, pin_memory=True).numpy() for _ in range(3)]
+    for h in hosts2:
+        sim.step(1)
+        sim.download_trail_async(h)
+    sim.wait_download()
+    for k, h in enumerate(hosts2):
+        oracle.run(p2, W2, H, ca, ct, 1)
+        assert_bitexact(h, ct, f"frame {k} after the resize")
     sim.close()
 
 
