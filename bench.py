@@ -640,8 +640,10 @@ def main():
                        "decay": "multiply 0.97", "blur": "gauss r=1 sigma=1 rate 0.5",
                        "reorder_every": args.reorder_every, "graph_chunk": 50,
                        "l2_persist": not args.no_l2_persist,
-                       "l2": f"agent state {16 * n / 1e6:.0f} MB streamed per step (> 129 MB L2); "
-                             f"trail {4 * W * H / 1e6:.0f} MB kept L2-resident by design",
+                       "l2": f"agent state {16 * n / 1e6:.0f} MB streamed per step (> 129 MB L2, inputs larger "
+                             f"than L2 between timed steps); trail {4 * W * H / 1e6:.0f} MB"
+                             + (" (fits the 129 MB L2; a persisting window over it is the autotuner's choice, "
+                                "see tuned.l2_window_passes)" if 4 * W * H < 129e6 else " (exceeds L2)"),
                        "parallelism": f"replicas x{ws}",
                        "dispatch": "every agent once per step" if args.dispatch == "each" else
                                    f"the reference's dispatch: {n_visited} of {n} agents updated per step"},
