@@ -77,6 +77,16 @@ struct RowFetch {
     uint32_t hk[R];
 };
 
+// L2 prefetch of a row's trail cells and deposit record (a hint: no registers
+// held, no result), so a later fetch_row of it is served from L2.
+template <class D>
+__device__ __forceinline__ void prefetch_row(const DevParams& p, const float* __restrict__ in,
+                                             const D* __restrict__ cin, int row, int cl) {
+    const size_t base = (size_t)row * p.W + cl;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(in + base));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(cin + base));
+}
+
 template <int R, bool kCoherent, class D>
 __device__ __forceinline__ void fetch_row(const DevParams& p, const float* __restrict__ in, const D* __restrict__ cin,
                                           int row, int cl, bool has_halo, int hcol0, RowFetch<R, D>& f) {
@@ -159,6 +169,12 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     const bool has_halo = active && (left_edge || right_edge);
     const int hcol0 = left_edge ? c0 - R : c0 + 4;
     RowFetch<R, D> fa, fb;
+    // rows further ahead are prefetched into L2 (kPrefetchL2 rows beyond the
+    // two held in registers) by the streaming kernel
+    constexpr int kPrefetchL2 = kUnrolled ? 2 : 0;
+#pragma unroll
+    for (int q = 0; q < kPrefetchL2; q++)
+        if (2 + q < NR) prefetch_row<D>(p, in, cin, wrap_coord(y0 - R + 2 + q, H), cl);
     fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R, H), cl, has_halo, hcol0, fa);
     fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + 1, H), cl, has_halo, hcol0, fb);
     // short strips unroll completely when asked to; long ones stay rolled
@@ -170,6 +186,8 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
         fa = fb;
         if (r + 2 < NR)
             fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + r + 2, H), cl, has_halo, hcol0, fb);
+        if (kPrefetchL2 && r + 2 + kPrefetchL2 < NR)
+            prefetch_row<D>(p, in, cin, wrap_coord(y0 - R + r + 2 + kPrefetchL2, H), cl);
         // shift the window and add the new row
 #pragma unroll
         for (int q = 0; q < NWIN - 1; q++) {
