@@ -187,14 +187,23 @@ void free_trail(slime_ctx* ctx) {
     }
 }
 
+// The agent block for `n` agents replaces the context's only once it is
+// allocated and cleared: on failure the context keeps its agents.  The
+// caller has synchronised the stream when the old block may still be read.
 int alloc_agents(slime_ctx* ctx, uint64_t n) {
-    free_agents(ctx);
     uint64_t n_pad = (n + kAgentPad - 1) / kAgentPad * kAgentPad;
     if (n_pad == 0) n_pad = kAgentPad;
     size_t bytes = 4 * n_pad * sizeof(float);
-    CK(dev_alloc((void**)&ctx->agent_block, bytes), "allocating agents");
-    CK(cudaMemsetAsync(ctx->agent_block, 0, bytes, ctx->stream), "clearing agents");
-    float* b = (float*)ctx->agent_block;
+    void* block = nullptr;
+    CK(dev_alloc(&block, bytes), "allocating agents");
+    cudaError_t e = cudaMemsetAsync(block, 0, bytes, ctx->stream);
+    if (e != cudaSuccess) {
+        dev_free(block);
+        return cuda_error(ctx->err, e, "clearing agents");
+    }
+    free_agents(ctx);
+    ctx->agent_block = block;
+    float* b = (float*)block;
     ctx->agents.x = b;
     ctx->agents.y = b + n_pad;
     ctx->agents.th = b + 2 * n_pad;
@@ -205,20 +214,68 @@ int alloc_agents(slime_ctx* ctx, uint64_t n) {
     return SLIME_OK;
 }
 
+// Two trails with their deposit counts, marks and gather textures.
+struct TrailSet {
+    float* trail[2] = {nullptr, nullptr};
+    uint32_t* counts[2] = {nullptr, nullptr};
+    uint8_t* marks[2] = {nullptr, nullptr};
+    cudaTextureObject_t tex[2] = {0, 0};
+
+    void release() {
+        for (int i = 0; i < 2; i++) {
+            if (tex[i]) cudaDestroyTextureObject(tex[i]);
+            dev_free(trail[i]);
+            dev_free(counts[i]);
+            dev_free(marks[i]);
+            tex[i] = 0;
+            trail[i] = nullptr;
+            counts[i] = nullptr;
+            marks[i] = nullptr;
+        }
+    }
+};
+
+cudaError_t make_trail_set(uint32_t W, uint32_t H, cudaStream_t s, TrailSet* t, const char** what) {
+    const size_t cells = (size_t)W * H;
+    // W + 2 zero floats past the last cell: the sampler's discarded taps
+    const size_t trail_bytes = (cells + W + 2) * sizeof(float);
+    const size_t mark_bytes = (cells + 15) & ~(size_t)15;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        *what = "allocating trail";
+        if ((e = dev_alloc((void**)&t->trail[i], trail_bytes)) != cudaSuccess) break;
+        *what = "allocating deposit counts";
+        if ((e = dev_alloc((void**)&t->counts[i], cells * sizeof(uint32_t))) != cudaSuccess) break;
+        *what = "allocating deposit marks";
+        if ((e = dev_alloc((void**)&t->marks[i], mark_bytes)) != cudaSuccess) break;
+        *what = "clearing trail";
+        e = cudaMemsetAsync(t->trail[i], 0, trail_bytes, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(t->counts[i], 0, cells * sizeof(uint32_t), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(t->marks[i], 0, mark_bytes, s);
+        if (e == cudaSuccess) t->tex[i] = make_trail_texture(t->trail[i], W, H);
+    }
+    return e;
+}
+
+// The trails for a W x H grid replace the context's only once all of them
+// are allocated: on failure the context keeps its trail.  The caller has
+// synchronised the stream when the old trails may still be read.
 int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
+    TrailSet t;
+    const char* what = "allocating trail";
+    cudaError_t e = make_trail_set(W, H, ctx->stream, &t, &what);
+    if (e != cudaSuccess) {
+        t.release();
+        return cuda_error(ctx->err, e, what);
+    }
     free_trail(ctx);
-    size_t cells = (size_t)W * H;
     for (int i = 0; i < 2; i++) {
-        // W + 2 zero floats past the last cell: the sampler's discarded taps
-        CK(dev_alloc((void**)&ctx->trail[i], (cells + W + 2) * sizeof(float)), "allocating trail");
-        CK(dev_alloc((void**)&ctx->counts[i], cells * sizeof(uint32_t)), "allocating deposit counts");
-        CK(cudaMemsetAsync(ctx->trail[i], 0, (cells + W + 2) * sizeof(float), ctx->stream), "clearing trail");
-        CK(cudaMemsetAsync(ctx->counts[i], 0, cells * sizeof(uint32_t), ctx->stream), "clearing counts");
-        CK(dev_alloc((void**)&ctx->marks[i], (cells + 15) & ~(size_t)15), "allocating deposit marks");
-        CK(cudaMemsetAsync(ctx->marks[i], 0, (cells + 15) & ~(size_t)15, ctx->stream), "clearing marks");
+        ctx->trail[i] = t.trail[i];
+        ctx->counts[i] = t.counts[i];
+        ctx->marks[i] = t.marks[i];
+        ctx->trail_tex[i] = t.tex[i];
         ctx->counts_dirty[i] = false;
         ctx->marks_dirty[i] = false;
-        ctx->trail_tex[i] = make_trail_texture(ctx->trail[i], W, H);
     }
     ctx->cur = 0;
     ctx->last_counts_valid = false;
@@ -863,14 +920,16 @@ int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height) {
     DevParams d;
     const char* why = nullptr;
     if (!make_dev_params(np, width, height, &d, &why)) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "%s", why);
-    // src/main.rs:987-993: scale = new / old as f32 division.
-    float sx = slm_div((float)width, (float)ctx->W);
-    float sy = slm_div((float)height, (float)ctx->H);
-    CK(launch_scale_positions(ctx->agents, sx, sy, ctx->stream), "scaling agent positions");
     CK(cudaStreamSynchronize(ctx->stream), "resizing");
+    // the graphs and the adjoint recording belong to the old size; the new
+    // trails replace the old only once allocated, so a resize that runs out
+    // of memory leaves the agents and the trail as they were
     invalidate_graphs(ctx);
     free_adjoint(ctx);
     if ((rc = alloc_trail(ctx, width, height)) != SLIME_OK) return rc;
+    // src/main.rs:987-993: scale = new / old as f32 division.
+    float sx = slm_div((float)width, (float)ctx->W);
+    float sy = slm_div((float)height, (float)ctx->H);
     ctx->W = width;
     ctx->H = height;
     ctx->params = np;
@@ -879,6 +938,7 @@ int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height) {
     ctx->l2_tuned_off = false;
     ctx->l2_window_passes = 3;
     setup_l2(ctx);
+    CK(launch_scale_positions(ctx->agents, sx, sy, ctx->stream), "scaling agent positions");
     CK(cudaStreamSynchronize(ctx->stream), "resizing");
     return SLIME_OK;
 }
@@ -888,7 +948,9 @@ int slime_set_agent_count(slime_ctx* ctx, uint64_t n, uint64_t seed) {
     cudaSetDevice(ctx->device);
     int rc;
     if ((rc = valid_size(ctx->err, ctx->W, ctx->H, n)) != SLIME_OK) return rc;
-    cudaStreamSynchronize(ctx->stream);
+    CK(cudaStreamSynchronize(ctx->stream), "changing the agent count");
+    // the new block replaces the agents only once allocated: out of memory,
+    // the context keeps its agents
     invalidate_graphs(ctx);
     free_adjoint(ctx);
     if ((rc = alloc_agents(ctx, n)) != SLIME_OK) return rc;

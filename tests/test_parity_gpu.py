@@ -445,23 +445,44 @@ def test_checkpoint_resume_continues_bit_identically(gpu, tmp_path):
 def test_memory_cap_reports_out_of_memory(gpu):
     """Out-of-memory paths through a capped allocator (SLIME_DEVICE_MEMORY_CAP):
     the failing call returns SLIME_ERR_OUT_OF_MEMORY and nothing leaks into
-    later calls."""
+    later calls.  A resize or an agent-count change that runs out of memory
+    leaves the context as it was: same size, same agents, same trail, and
+    its next steps match a context that never tried."""
     import os
     import subprocess
     import sys
     from conftest import ROOT
     code = (
-        "import sys; sys.path.insert(0, %r); import slime_gb300 as sg\n"
+        "import sys; sys.path.insert(0, %r); import numpy as np; import slime_gb300 as sg\n"
         "try:\n"
         "    sg.Simulation(1024, 1024, 1000)\n"
         "    print('created')\n"
         "except sg.SlimeError as e:\n"
         "    print('status', e.status)\n"
         "s = sg.Simulation(64, 64, 100)\n"
-        "s.step(2); print('small ok')\n" % os.path.join(ROOT, "slime-mold_gb300"))
+        "s.step(2); print('small ok')\n"
+        "s.seed_agents(5); s.step(3)\n"
+        "a0, t0 = s.download_agents(), s.download_trail()\n"
+        "for call in (lambda: s.resize(1024, 1024), lambda: s.set_agent_count(1_000_000)):\n"
+        "    try:\n"
+        "        call(); print('grew')\n"
+        "    except sg.SlimeError as e:\n"
+        "        print('status', e.status)\n"
+        "i = s.info()\n"
+        "same = (i.width, i.height, i.n_agents) == (64, 64, 100)\n"
+        "same = same and np.array_equal(s.download_agents().view(np.uint32), a0.view(np.uint32))\n"
+        "same = same and np.array_equal(s.download_trail().view(np.uint32), t0.view(np.uint32))\n"
+        "print('unchanged', same)\n"
+        "r = sg.Simulation(64, 64, 100, s.params())\n"
+        "r.upload_agents(a0); r.upload_trail(t0); r.step(4); s.step(4)\n"
+        "same = np.array_equal(s.download_agents().view(np.uint32), r.download_agents().view(np.uint32))\n"
+        "same = same and np.array_equal(s.download_trail().view(np.uint32), r.download_trail().view(np.uint32))\n"
+        "print('steps after failure', same)\n" % os.path.join(ROOT, "slime-mold_gb300"))
     env = dict(os.environ, SLIME_DEVICE_MEMORY_CAP=str(2 * 1024 * 1024))
     out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
-    assert "status -2" in out.stdout and "small ok" in out.stdout, out.stdout + out.stderr
+    text = out.stdout + out.stderr
+    assert out.stdout.count("status -2") == 3 and "small ok" in out.stdout, text
+    assert "unchanged True" in out.stdout and "steps after failure True" in out.stdout, text
 
 
 def test_l2_carveout_only_for_trails_that_fit(gpu):
