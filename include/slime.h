@@ -202,10 +202,12 @@ int slime_download_trail(slime_ctx* ctx, float* trail, uint64_t n_cells);
 /* Trail clear on key C (src/main.rs:909-913). */
 int slime_clear_trail(slime_ctx* ctx);
 /* Window resize (src/main.rs:954-1015): agent x,y are scaled by new/old size,
- * the trail is reallocated zeroed. */
+ * the trail is reallocated zeroed.  Out of device memory it returns
+ * SLIME_ERR_OUT_OF_MEMORY with the context unchanged (size, agents, trail). */
 int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height);
 /* Agent-count change (src/main.rs:682-791): reallocates the agent buffer and
- * seeds every agent anew (seeded; the reference uses rand::random). */
+ * seeds every agent anew (seeded; the reference uses rand::random).  Out of
+ * device memory it returns SLIME_ERR_OUT_OF_MEMORY with the agents unchanged. */
 int slime_set_agent_count(slime_ctx* ctx, uint64_t n_agents, uint64_t seed);
 
 /* Advance n_steps steps: the agent dispatch, the decay dispatch and the
