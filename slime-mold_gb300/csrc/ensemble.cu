@@ -636,6 +636,8 @@ int slime_ensemble_download_agents(slime_ensemble* e, uint32_t j, float* aos, ui
 int slime_ensemble_seed_agents(slime_ensemble* e, uint32_t j, uint64_t seed, float hmin, float hmax) {
     int rc = check_colony(e, j);
     if (rc != SLIME_OK) return rc;
+    if (!isfinite(hmin) || !isfinite(hmax))
+        return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "heading bounds must be finite");
     Colony& c = e->colonies[j];
     AgentsSoA a = colony_soa(e, c);
     ECK(launch_seed_agents(a, seed, (float)c.W, (float)c.H, hmin, hmax, c.params.agent_speed_min,

@@ -87,6 +87,13 @@ def test_ensemble_rejects_mixed_blur_and_bad_widths(gpu):
         sg.Ensemble([64, 64], [64, 64], [10, 10], [p1, p2])
     with pytest.raises(sg.SlimeError):
         sg.Ensemble([66], [64], [10], [config0_params(66, 64)])
+    ens = sg.Ensemble([64], [64], [10], [config0_params(64, 64)])
+    with pytest.raises(sg.SlimeError) as e:
+        ens.seed_agents(0, 1, float("nan"), 1.0)
+    assert e.value.status == -1
+    with pytest.raises(sg.SlimeError):
+        ens.seed_agents(1, 1)  # colony index out of range
+    ens.close()
 
 
 def test_bounded_barrier_times_out_and_recovers(gpu):

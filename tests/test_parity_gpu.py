@@ -322,6 +322,9 @@ def test_nan_parameters_rejected(gpu):
     p = config0_params(32, 16)
     with pytest.raises(sg.SlimeError):
         sim.set_params(p)
+    with pytest.raises(sg.SlimeError) as e:
+        sim.seed_agents(1, 0.0, float("inf"))
+    assert e.value.status == -1
 
 
 def test_colorize_matches_display_pass(gpu):
