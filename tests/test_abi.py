@@ -101,3 +101,10 @@ def test_invalid_sizes_rejected_before_touching_the_device(built_lib):
     assert not L.slime_create(65536, 65536, 4, C.byref(st)) and st.value == -1
     assert not L.slime_create(16, 16, 1 << 31, C.byref(st)) and st.value == -1
     assert L.slime_status_string(-5) == b"device-side wait timed out"
+
+
+def test_package_refuses_to_run_without_its_library(tmp_path):
+    """No CPU fallback: a package whose library is absent raises on first use."""
+    import slime_gb300._abi as abi
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        abi.load(str(tmp_path / "libslime_gb300.so"))
