@@ -316,6 +316,13 @@ int slime_ensemble_selftest_barrier_timeout(slime_ensemble* ens);
 int slime_step_noalloc(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents, float* d_x,
                        float* d_y, float* d_angle, float* d_speed, const float* d_trail_in, float* d_trail_out,
                        void* stream);
+/* The same step with the deposit counts in the caller's device memory:
+ * d_counts holds width*height uint32 words (cleared by the call).  No limit
+ * on the trail size beyond width*height < 2^31, and calls with separate count
+ * arrays may overlap on the GPU. */
+int slime_step_noalloc_scratch(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents,
+                               float* d_x, float* d_y, float* d_angle, float* d_speed, const float* d_trail_in,
+                               float* d_trail_out, uint32_t* d_counts, void* stream);
 
 /* ------------------------------------------------ display feed */
 /* Headless equivalent of src/display.wgsl:44-86: colourise the current trail

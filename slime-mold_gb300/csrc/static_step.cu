@@ -16,6 +16,9 @@
 // process exits.  Every call uses the same array: it is cleared at the start
 // of each call, and calls whose work overlaps on the GPU (different streams,
 // or different host threads on one device) race on it and give wrong counts.
+// slime_step_noalloc_scratch takes the counts array from the caller instead
+// (width * height 32-bit words of its own device memory): no size limit
+// beyond the context's, and calls with separate arrays may overlap.
 #include <mutex>
 
 #include "kernels.h"
@@ -51,31 +54,17 @@ int counts_address(int device, uint32_t** out) {
     return SLIME_OK;
 }
 
-} // namespace
 
-extern "C" int slime_step_noalloc(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents,
-                                  float* d_x, float* d_y, float* d_angle, float* d_speed, const float* d_trail_in,
-                                  float* d_trail_out, void* stream) {
+// One step with the deposit counts in `counts` (room for `max_cells` cells).
+int step_with_counts(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents, float* d_x,
+                     float* d_y, float* d_angle, float* d_speed, const float* d_trail_in, float* d_trail_out,
+                     uint32_t* counts, uint64_t max_cells, cudaStream_t s) {
     using namespace slime;
-    if (!params || !d_trail_in || !d_trail_out || d_trail_in == d_trail_out) return SLIME_ERR_INVALID_ARGUMENT;
-    if (n_agents && (!d_x || !d_y || !d_angle || !d_speed)) return SLIME_ERR_INVALID_ARGUMENT;
-    // The sampler reads up to width + 1 cells past a discarded tap's cell 0,
-    // which stays inside the trail only for width, height >= 2.
-    if (width < 2 || height < 2 || (uint64_t)width * height > kNoAllocMaxCells || n_agents >= (1ull << 31))
-        return SLIME_ERR_INVALID_ARGUMENT;
+    const size_t cells = (size_t)width * height;
+    if (cells > max_cells) return SLIME_ERR_INVALID_ARGUMENT;
     DevParams d;
     const char* why = nullptr;
     if (!make_dev_params(*params, width, height, &d, &why)) return SLIME_ERR_INVALID_ARGUMENT;
-    int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess) {
-        cudaGetLastError();
-        return SLIME_ERR_NO_DEVICE;
-    }
-    uint32_t* counts = nullptr;
-    int rc = counts_address(device, &counts);
-    if (rc != SLIME_OK) return rc;
-    cudaStream_t s = (cudaStream_t)stream;
-    const size_t cells = (size_t)width * height;
     if (cudaMemsetAsync(counts, 0, cells * sizeof(uint32_t), s) != cudaSuccess) {
         cudaGetLastError();
         return SLIME_ERR_CUDA;
@@ -98,4 +87,46 @@ extern "C" int slime_step_noalloc(const SlimeParams* params, uint32_t width, uin
         return SLIME_ERR_CUDA;
     }
     return SLIME_OK;
+}
+
+// Argument checks shared by both entry points.
+bool valid_step_args(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents, const float* d_x,
+                     const float* d_y, const float* d_angle, const float* d_speed, const float* d_trail_in,
+                     const float* d_trail_out) {
+    if (!params || !d_trail_in || !d_trail_out || d_trail_in == d_trail_out) return false;
+    if (n_agents && (!d_x || !d_y || !d_angle || !d_speed)) return false;
+    // The sampler reads up to width + 1 cells past a discarded tap's cell 0,
+    // which stays inside the trail only for width, height >= 2.
+    return width >= 2 && height >= 2 && (uint64_t)width * height < (1ull << 31) && n_agents < (1ull << 31);
+}
+
+} // namespace
+
+extern "C" int slime_step_noalloc(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents,
+                                  float* d_x, float* d_y, float* d_angle, float* d_speed, const float* d_trail_in,
+                                  float* d_trail_out, void* stream) {
+    if (!valid_step_args(params, width, height, n_agents, d_x, d_y, d_angle, d_speed, d_trail_in, d_trail_out) ||
+        (uint64_t)width * height > kNoAllocMaxCells)
+        return SLIME_ERR_INVALID_ARGUMENT;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        return SLIME_ERR_NO_DEVICE;
+    }
+    uint32_t* counts = nullptr;
+    int rc = counts_address(device, &counts);
+    if (rc != SLIME_OK) return rc;
+    return step_with_counts(params, width, height, n_agents, d_x, d_y, d_angle, d_speed, d_trail_in, d_trail_out,
+                            counts, kNoAllocMaxCells, (cudaStream_t)stream);
+}
+
+extern "C" int slime_step_noalloc_scratch(const SlimeParams* params, uint32_t width, uint32_t height,
+                                          uint64_t n_agents, float* d_x, float* d_y, float* d_angle, float* d_speed,
+                                          const float* d_trail_in, float* d_trail_out, uint32_t* d_counts,
+                                          void* stream) {
+    if (!valid_step_args(params, width, height, n_agents, d_x, d_y, d_angle, d_speed, d_trail_in, d_trail_out) ||
+        !d_counts)
+        return SLIME_ERR_INVALID_ARGUMENT;
+    return step_with_counts(params, width, height, n_agents, d_x, d_y, d_angle, d_speed, d_trail_in, d_trail_out,
+                            d_counts, (uint64_t)width * height, (cudaStream_t)stream);
 }

@@ -185,6 +185,8 @@ SIGNATURES = {
     "slime_colorize_async": (C.c_int, [P, U8P, C.c_uint32, C.c_uint32, U8P]),
     "slime_step_noalloc": (C.c_int, [C.POINTER(SlimeParams), C.c_uint32, C.c_uint32, C.c_uint64, P, P, P, P, P, P,
                                      P]),
+    "slime_step_noalloc_scratch": (C.c_int, [C.POINTER(SlimeParams), C.c_uint32, C.c_uint32, C.c_uint64, P, P, P,
+                                             P, P, P, P, P]),
 }
 
 _lib = None

@@ -56,6 +56,49 @@ def test_step_noalloc_matches_slime_step_twice(gpu):
             assert np.array_equal(dst.cpu().numpy().view(np.uint32), tw.view(np.uint32))
 
 
+def test_step_noalloc_scratch_beyond_the_array_and_overlapping(gpu):
+    """The caller-owned count array: a 2048x1024 trail (twice the fixed
+    array) matches slime_step bit for bit, and two colonies stepped on two
+    streams at once, each with its own count array, match their sequential
+    runs."""
+    import torch
+
+    import slime_gb300 as sg
+    L = sg.lib()
+    W, H, n = 2048, 1024, 200_000
+    p = config0_params(W, H, agent_speed_min=30.0, agent_speed_max=50.0, agent_jitter=0.3)
+    dev = torch.device("cuda", 0)
+    runs = []
+    for seed in (11, 12):
+        agents = agents_uniform(n, W, H, 30.0, 50.0, seed=seed)
+        trail = np.random.default_rng(seed).random((H, W), dtype=np.float32)
+        with sg.Simulation(W, H, n, p) as sim:
+            sim.upload_agents(agents)
+            sim.upload_trail(trail)
+            sim.step(2)
+            want = sim.download_agents(), sim.download_trail()
+        cols = [torch.tensor(np.ascontiguousarray(agents[:, j]), device=dev) for j in range(4)]
+        ta = torch.tensor(trail, device=dev)
+        tb = torch.empty_like(ta)
+        counts = torch.full((H * W,), 7, dtype=torch.int32, device=dev)  # cleared by each call
+        runs.append((cols, ta, tb, counts, torch.cuda.Stream(), want))
+    torch.cuda.synchronize()
+    for src_dst in ((1, 2), (2, 1)):
+        for cols, ta, tb, counts, st, _ in runs:  # both colonies in flight at once
+            src, dst = (ta, tb) if src_dst == (1, 2) else (tb, ta)
+            rc = L.slime_step_noalloc_scratch(C.byref(p), W, H, n, *[_ptr(c) for c in cols], _ptr(src), _ptr(dst),
+                                              _ptr(counts), C.c_void_p(st.cuda_stream))
+            assert rc == 0
+    torch.cuda.synchronize()
+    for cols, ta, tb, counts, st, (wa, wt) in runs:
+        got = np.stack([c.cpu().numpy() for c in cols], axis=1)
+        assert np.array_equal(got.view(np.uint32), wa.view(np.uint32))
+        assert np.array_equal(ta.cpu().numpy().view(np.uint32), wt.view(np.uint32))
+    cols, ta, tb, counts, st, _ = runs[0]
+    rc = L.slime_step_noalloc_scratch(C.byref(p), W, H, n, *[_ptr(c) for c in cols], _ptr(ta), _ptr(tb), None, None)
+    assert rc == -1
+
+
 def test_step_noalloc_rejects_sizes_beyond_its_array(gpu):
     import torch
 
