@@ -40,6 +40,17 @@ def _f32p(a):
     return a.ctypes.data_as(_abi.F32P)
 
 
+def _host_out(out, dtype, size, what):
+    """`out` as a destination the library may fill with `size` elements of
+    `dtype`: the C functions write exactly that many, so anything smaller,
+    strided or of another type is refused before the call."""
+    if not isinstance(out, np.ndarray) or out.dtype != dtype or not out.flags.c_contiguous \
+            or not out.flags.writeable or out.size != size:
+        raise ValueError(f"{what}: expected a writeable C-contiguous {np.dtype(dtype).name} array of "
+                         f"{size} elements")
+    return out
+
+
 def default_settings():
     """Settings::default() (src/settings.rs:49-70)."""
     s = SlimeSettings()
@@ -80,6 +91,7 @@ class Simulation:
     """One colony on one GPU: the agent buffer, the trail and the step."""
 
     def __init__(self, width, height, n_agents, params=None):
+        self._inflight = {}  # host buffers the asynchronous copies still fill
         self._L = lib()
         st = C.c_int(0)
         self._h = self._L.slime_create(width, height, n_agents, C.byref(st))
@@ -93,8 +105,9 @@ class Simulation:
     # -- lifecycle
     def close(self):
         if getattr(self, "_h", None):
-            self._L.slime_destroy(self._h)
+            self._L.slime_destroy(self._h)  # waits for the copies in flight
             self._h = None
+        self._inflight = {}
 
     def __del__(self):
         try:
@@ -148,7 +161,8 @@ class Simulation:
         self._check(self._L.slime_upload_agents(self._h, _f32p(a), a.shape[0]), "upload_agents")
 
     def download_agents(self, out=None):
-        a = out if out is not None else np.empty((self.n_agents, 4), np.float32)
+        a = _host_out(out, np.float32, 4 * self.n_agents, "download_agents") if out is not None \
+            else np.empty((self.n_agents, 4), np.float32)
         self._check(self._L.slime_download_agents(self._h, _f32p(a), self.n_agents), "download_agents")
         return a
 
@@ -163,18 +177,22 @@ class Simulation:
         self._check(self._L.slime_upload_trail(self._h, _f32p(t), t.size), "upload_trail")
 
     def download_trail(self, out=None):
-        t = out if out is not None else np.empty((self.height, self.width), np.float32)
+        t = _host_out(out, np.float32, self.width * self.height, "download_trail") if out is not None \
+            else np.empty((self.height, self.width), np.float32)
         self._check(self._L.slime_download_trail(self._h, _f32p(t), self.width * self.height), "download_trail")
         return t
 
     def download_trail_async(self, out):
         """Start copying the current trail into `out` (a C-contiguous float32
-        array, ideally page-locked); complete after wait_download()."""
-        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == self.width * self.height
+        array, ideally page-locked); complete after wait_download(), until
+        which this object keeps a reference to `out`."""
+        _host_out(out, np.float32, self.width * self.height, "download_trail_async")
         self._check(self._L.slime_download_trail_async(self._h, _f32p(out), out.size), "download_trail_async")
+        self._inflight[id(out)] = out
 
     def wait_download(self):
         self._check(self._L.slime_wait_download(self._h), "wait_download")
+        self._inflight = {}
 
     def download_deposit_counts(self):
         c = np.empty((self.height, self.width), np.uint32)
@@ -243,6 +261,8 @@ class Simulation:
 
     def backward(self, dl_dtrail_final, want_trail_grad=True):
         g = np.ascontiguousarray(dl_dtrail_final, dtype=np.float32).reshape(-1)
+        if g.size != self.width * self.height:
+            raise ValueError(f"backward: dL/dT has {g.size} cells, the trail {self.width * self.height}")
         out = SlimeGrads()
         d0 = np.empty((self.height, self.width), np.float32) if want_trail_grad else None
         self._check(self._L.slime_backward(self._h, _f32p(g), C.byref(out),
@@ -266,9 +286,12 @@ class Simulation:
         lut = np.ascontiguousarray(lut768, dtype=np.uint8).reshape(-1)
         if lut.size != 768:
             raise ValueError("a LUT has 768 bytes (R[256] G[256] B[256])")
-        assert out.dtype == np.uint8 and out.flags.c_contiguous and out.ndim == 3 and out.shape[2] == 4
+        if not isinstance(out, np.ndarray) or out.ndim != 3 or out.shape[2] != 4:
+            raise ValueError("colorize_async: expected a (height, width, 4) uint8 image")
+        _host_out(out, np.uint8, out.size, "colorize_async")
         self._check(self._L.slime_colorize_async(self._h, lut.ctypes.data_as(_abi.U8P), out.shape[1], out.shape[0],
                                                  out.ctypes.data_as(_abi.U8P)), "colorize_async")
+        self._inflight[id(out)] = out
 
 
 class Ensemble:
@@ -277,7 +300,8 @@ class Ensemble:
     def __init__(self, widths, heights, n_agents, params):
         self._L = lib()
         k = len(widths)
-        assert len(heights) == k and len(n_agents) == k and len(params) == k
+        if not (len(heights) == k and len(n_agents) == k and len(params) == k):
+            raise ValueError("widths, heights, n_agents and params need one entry per colony")
         W = (C.c_uint32 * k)(*widths)
         H = (C.c_uint32 * k)(*heights)
         N = (C.c_uint64 * k)(*n_agents)

@@ -108,3 +108,37 @@ def test_package_refuses_to_run_without_its_library(tmp_path):
     import slime_gb300._abi as abi
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         abi.load(str(tmp_path / "libslime_gb300.so"))
+
+
+def test_host_destinations_are_checked_before_the_library_writes():
+    """The C calls write a fixed number of elements into the caller's
+    buffer; the Python mirror refuses a destination of the wrong size, type
+    or layout, and a gradient of the wrong size, before any call."""
+    import numpy as np
+
+    import slime_gb300 as sg
+    sim = object.__new__(sg.Simulation)  # no device needed: nothing reaches the library
+    sim._L, sim._h, sim._inflight = None, None, {}
+    sim.width, sim.height, sim.n_agents = 8, 4, 3
+    bad_trails = [np.empty((4, 7), np.float32), np.empty((4, 8), np.float64),
+                  np.empty((8, 8), np.float32)[:, ::2], np.empty(32, np.int32)]
+    for out in bad_trails:
+        with pytest.raises(ValueError):
+            sim.download_trail(out)
+        with pytest.raises(ValueError):
+            sim.download_trail_async(out)
+    for out in (np.empty((2, 4), np.float32), np.empty((3, 4), np.float16), np.empty((3, 4), np.float32).T):
+        with pytest.raises(ValueError):
+            sim.download_agents(out)
+    ro = np.empty((4, 8), np.float32)
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        sim.download_trail(ro)
+    with pytest.raises(ValueError):
+        sim.backward(np.zeros(31, np.float32))
+    lut = np.zeros(768, np.uint8)
+    for out in (np.empty((4, 8, 3), np.uint8), np.empty((4, 8, 4), np.float32), np.empty((4, 8), np.uint8)):
+        with pytest.raises(ValueError):
+            sim.colorize_async(lut, out)
+    with pytest.raises(ValueError):
+        sg.Ensemble([64, 64], [64], [10, 10], [None, None])
