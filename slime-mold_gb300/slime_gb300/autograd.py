@@ -27,16 +27,18 @@ class TrailChain(torch.autograd.Function):
         sim.forward_record(int(n_steps), int(ckpt_every))
         out = torch.from_numpy(sim.download_trail().copy())
         ctx.sim = sim
+        # a gradient goes back only to the parameters given as tensors, in
+        # their own dtype (autograd refuses one for a plain number)
+        ctx.param_dtypes = [x.dtype if torch.is_tensor(x) else None for x in (decay, rate, deposition)]
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
         g = grad_out.detach().to(torch.float32).cpu().contiguous().numpy()
-        grads, d0 = ctx.sim.backward(g)
-        f64 = torch.float64
-        return (torch.from_numpy(d0), torch.tensor(grads.d_decay_factor, dtype=f64),
-                torch.tensor(grads.d_diffusion_rate, dtype=f64), torch.tensor(grads.d_deposition_amount, dtype=f64),
-                None, None, None, None)
+        grads, d0 = ctx.sim.backward(g, want_trail_grad=ctx.needs_input_grad[0])
+        values = (grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount)
+        dparams = [torch.tensor(v, dtype=dt) if dt is not None else None for v, dt in zip(values, ctx.param_dtypes)]
+        return (torch.from_numpy(d0) if d0 is not None else None, *dparams, None, None, None, None)
 
 
 def trail_chain(trail0, decay, rate, deposition, sim, n_steps, ckpt_every, agents):
