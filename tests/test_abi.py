@@ -142,3 +142,19 @@ def test_host_destinations_are_checked_before_the_library_writes():
             sim.colorize_async(lut, out)
     with pytest.raises(ValueError):
         sg.Ensemble([64, 64], [64], [10, 10], [None, None])
+
+
+def test_rust_binding_in_the_integration_notes_matches_the_header():
+    """Every `fn slime_*` of the Rust extern block shown in INTEGRATION.md is
+    declared in include/slime.h with the same number of arguments."""
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "slime.h")).read(), flags=re.S)
+    arity = {}
+    for m in re.finditer(r"\b(slime_\w+)\s*\(([^;{]*?)\)\s*;", src):
+        args = [a for a in m.group(2).split(",") if a.strip() and a.strip() != "void"]
+        arity[m.group(1)] = len(args)
+    notes = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    bound = re.findall(r"fn (slime_\w+)\(([^)]*)\)", notes)
+    assert len(bound) >= 15
+    for name, args in bound:
+        assert name in arity, name
+        assert len([a for a in args.split(",") if a.strip()]) == arity[name], name
