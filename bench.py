@@ -162,9 +162,22 @@ class ClockSampler:
         self.proc = None
         self.lines = []
 
+    @staticmethod
+    def smi_id(index):
+        """nvidia-smi's name for CUDA device `index` of this process: the
+        index-th entry of CUDA_VISIBLE_DEVICES (an index or a UUID) when that
+        is set, since nvidia-smi sees every GPU of the machine."""
+        vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+        return vis[index] if 0 <= index < len(vis) else str(index)
+
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+            ident = self.smi_id(self.index)
+            if ident != str(self.index):  # keep the plain index if nvidia-smi does not know that name
+                probe = subprocess.run(["nvidia-smi", f"--id={ident}", "--query-gpu=index", "--format=csv,noheader"],
+                                       capture_output=True, timeout=20)
+                ident = ident if probe.returncode == 0 else str(self.index)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={ident}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)

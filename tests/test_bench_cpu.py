@@ -66,3 +66,22 @@ def test_synthetic_agents_are_seeded_and_in_range():
     assert (a[:, 1] >= 0).all() and (a[:, 1] < H).all()
     assert (a[:, 2] >= 0).all() and (a[:, 2] <= np.float32(2 * np.pi)).all()
     assert (a[:, 3] >= 1.0).all() and (a[:, 3] <= 2.0).all()
+
+
+def test_clock_sampler_names_the_process_gpu(monkeypatch):
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES", raising=False)
+    assert bench.ClockSampler.smi_id(0) == "0"
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "5,GPU-1234")
+    assert bench.ClockSampler.smi_id(0) == "5"
+    assert bench.ClockSampler.smi_id(1) == "GPU-1234"
+    assert bench.ClockSampler.smi_id(2) == "2"
+
+
+def test_clock_summary_reads_reasons():
+    s = bench.ClockSampler(0)
+    s.lines = ["0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+               "0, 2040, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active",
+               "garbage"]
+    out = s.summary()
+    assert out["sm_mhz"] == 2055.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["sw_power_cap"] and out["samples"] == 2
