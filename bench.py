@@ -26,6 +26,7 @@ neither of which exists on the box).  Under torchrun every rank runs an
 independent replica (a single colony does not shard), value = the sum.
 """
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -412,6 +413,71 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def workload_config(args, ws=1, cfg_name=None):
+    """The `config` object of a plain-workload line, the same for both arms."""
+    cfg_name = cfg_name or args.config
+    W, H, n = CONFIGS[cfg_name][:3]
+    n_visited = reference_dispatch_visited(n) if args.dispatch == "reference" else n
+    return {"workload": cfg_name, "width": W, "height": H, "n_agents": n,
+            "sensor_angle": 0.4, "sensor_distance": CONFIGS[cfg_name][5], "turn": 0.3, "jitter": 0.05,
+            "speed": list(CONFIGS[cfg_name][3:5]), "deposition": 1.0,
+            "decay": "multiply 0.97", "blur": "gauss r=1 sigma=1 rate 0.5",
+            "sensor_mode": "shader: cos/sin(angle -/+ a) as compute.wgsl:75-86",
+            "reorder_every": args.reorder_every, "graph_chunk": 50,
+            "l2_persist": not args.no_l2_persist,
+            "l2": f"agent state {16 * n / 1e6:.0f} MB streamed per step (> 129 MB L2, inputs larger "
+                  f"than L2 between timed steps); trail {4 * W * H / 1e6:.0f} MB"
+                  + (" (fits the 129 MB L2; a persisting window over it is the autotuner's choice, "
+                     "see tuned.l2_window_passes)" if 4 * W * H < 129e6 else " (exceeds L2)"),
+            "parallelism": f"replicas x{ws}",
+            "dispatch": "every agent once per step" if args.dispatch == "each" else
+                        f"the reference's dispatch: {n_visited} of {n} agents updated per step"}
+
+
+def measure_plain(sim, stream, params, agents, args, barrier, local, torch):
+    """One parameter set on the plain workload: the seeded initial state,
+    autotuning, W untimed warm-up steps, then K steps replayed from CUDA
+    graphs, timed with CUDA events on the simulation's stream while the
+    clocks are sampled.  The Morton reorders inside the window are counted
+    and the reorder's own time is measured, so that the returned `ms` charges
+    every step its share (one reorder per reorder_every steps) whatever the
+    window's length.  Then per-kernel times over direct launches."""
+    sim.upload_agents(agents)
+    sim.clear_trail()
+    sim.set_params(params)
+    if not (args.trail_tile and args.agent_shape):
+        sim.autotune(5)
+    tuned = sim.info()
+    sim.step(args.warmup)
+    sim.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    info0 = sim.info()
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        e0.record(stream)
+        sim.step(args.steps)
+        e1.record(stream)
+        sim.sync()
+        torch.cuda.synchronize()
+    barrier()
+    window_ms = e0.elapsed_time(e1)
+    info1 = sim.info()
+    reorders_in = int(info1.reorders_done - info0.reorders_done)
+    reorder_ms = sim.profile_reorder(5) / 5 if args.reorder_every else 0.0
+    ms = window_ms
+    if args.reorder_every:
+        ms = window_ms - reorders_in * reorder_ms + args.steps * reorder_ms / args.reorder_every
+    kern_steps = min(args.steps, 100)
+    agents_ms, trail_ms, other_ms = sim.profile_steps(kern_steps)
+    return {"tuned": tuned, "clocks": clocks.summary(), "launches": int(info1.kernel_launches -
+                                                                      info0.kernel_launches),
+            "window_ms": window_ms, "ms": ms, "reorders_in": reorders_in, "reorder_ms": reorder_ms,
+            "kern_steps": kern_steps, "t_agents": agents_ms / kern_steps, "t_trail": trail_ms / kern_steps,
+            "other_ms": other_ms}
+
+
 def aggregate_ranks(ms, units_per_rank, seconds=None):
     """Whole-job figures over replicas: the slowest rank's time and the sum of
     the units every rank processed (a single colony does not shard, so each
@@ -470,7 +536,7 @@ def run_reference(args, cfg_name):
         "impl": "reference", "metric": metric_name(cfg_name), "value": value, "unit": "agent-steps/s",
         "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1000 * dt / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg_name, "width": W, "height": H, "n_agents": n},
+        "config": workload_config(args, 1, cfg_name),
         "cells_per_s": W * H * steps / dt,
         "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": threads, "kind": "port",
                          "sample": f"{steps} of {args.steps} requested full steps (time-bounded at 90 s) after "
@@ -532,47 +598,25 @@ def main():
         n_visited = reference_dispatch_visited(n)
     agents = make_agents(n, W, H, lo, hi, seed=rank)
     sim = sg.Simulation(W, H, n, params)
-    sim.upload_agents(agents)
     sim.set_options(reorder_every=args.reorder_every, reorder_cell_log2=2, graph_chunk=50,
                     l2_persist=0 if args.no_l2_persist else 1,
                     trail_tile=args.trail_tile, agent_shape=args.agent_shape)
-    if not (args.trail_tile and args.agent_shape):
-        sim.autotune(5)
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
-    tuned = sim.info()
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
 
-    # warm-up (untimed)
-    sim.step(args.warmup)
-    sim.sync()
-
-    # -- timed region: K steps from CUDA graphs, state resident in HBM
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    info0 = sim.info()
-    barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        e0.record(stream)
-        sim.step(args.steps)
-        e1.record(stream)
-        sim.sync()
-        torch.cuda.synchronize()
-    barrier()
-    ms = e0.elapsed_time(e1)
-    launches = sim.info().kernel_launches - info0.kernel_launches
-    ms, _, value = aggregate_ranks(ms, n * args.steps)
+    # headline: the shader's sensor evaluation (the reference's result); the
+    # opt-in rotated form is timed after the end-to-end loops, on the same
+    # workload from the same start
+    head = measure_plain(sim, stream, params, agents, args, barrier, local, torch)
+    tuned, clocks, launches = head["tuned"], head["clocks"], head["launches"]
+    ms, _, value = aggregate_ranks(head["ms"], n * args.steps)
     ms_per_step = ms / args.steps
     cells = ws * W * H * args.steps / (ms / 1e3)
-
-    # -- per-kernel CUDA-event times over K steps (direct launches)
-    kern_steps = min(args.steps, 100)
-    agents_ms, trail_ms, other_ms = sim.profile_steps(kern_steps)
-    t_agents = agents_ms / kern_steps
-    t_trail = trail_ms / kern_steps
+    t_agents, t_trail, kern_steps = head["t_agents"], head["t_trail"], head["kern_steps"]
+    other_ms = head["other_ms"]
     peak, peak_kind = load_peaks()
     bytes_agents = 32.0 * n_visited  # agent state read + write (agents the dispatch never updates sit in
                                      # the last slots, untouched)
@@ -595,6 +639,7 @@ def main():
     # step s overlaps step s+1 (double-buffered host trails)
     host = [torch.empty((H, W), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
     e2e_steps = max(3, min(args.steps, 50))
+    param_bytes = ctypes.sizeof(sg.SlimeParams)
     sim.set_params(params)
     sim.step(1)
     sim.download_trail_async(host[0])
@@ -609,10 +654,11 @@ def main():
     dt = time.perf_counter() - t0
     _, _, e2e_value = aggregate_ranks(dt * 1e3, n * e2e_steps)
     e2e = {"value": e2e_value, "unit": "agent-steps/s",
-           "h2d_bytes_per_step": 72, "d2h_bytes_per_step": 4 * W * H,
-           "steps": e2e_steps, "what": "per step: slime_set_params (72-byte parameter block), slime_step(1), "
-                                       "slime_download_trail_async of the new trail into pinned host memory "
-                                       "(copy overlapped with the next step; all copies waited for)"}
+           "h2d_bytes_per_step": param_bytes, "d2h_bytes_per_step": 4 * W * H,
+           "steps": e2e_steps, "what": f"per step: slime_set_params ({param_bytes}-byte parameter block), "
+                                       "slime_step(1), slime_download_trail_async of the new trail into pinned "
+                                       "host memory (copy overlapped with the next step; all copies waited for); "
+                                       "Morton reorders fall where the step schedule puts them"}
 
     # -- the reference's own frame loop end to end (src/main.rs:1163-1235):
     # per step the parameter block, slime_step(1) and the display pass
@@ -635,10 +681,21 @@ def main():
     dt = time.perf_counter() - t0
     _, _, e2e_display_value = aggregate_ranks(dt * 1e3, n * e2e_steps)
     e2e_display = {"value": e2e_display_value, "unit": "agent-steps/s",
-                   "h2d_bytes_per_step": 72, "d2h_bytes_per_step": tw * th * 4, "steps": e2e_steps,
-                   "what": "per step: slime_set_params (72-byte parameter block), slime_step(1), "
+                   "h2d_bytes_per_step": param_bytes, "d2h_bytes_per_step": tw * th * 4, "steps": e2e_steps,
+                   "what": f"per step: slime_set_params ({param_bytes}-byte parameter block), slime_step(1), "
                            "slime_colorize_async of the display pass into a 1600x900 RGBA8 frame in pinned "
                            "host memory (copy overlapped with the next step; all copies waited for)"}
+
+    rotated_params = params.copy()
+    rotated_params.sensor_mode = sg.SENSOR_ROTATED
+    rot = measure_plain(sim, stream, rotated_params, agents, args, barrier, local, torch)
+    rot_ms, _, rot_value = aggregate_ranks(rot["ms"], n * args.steps)
+
+    def mode_summary(m, total_ms, val):
+        return {"value": val, "ms_per_step": total_ms / args.steps,
+                "window_ms_per_step": m["window_ms"] / args.steps, "agents_ms": m["t_agents"],
+                "trail_ms": m["t_trail"], "agent_shape": m["tuned"].agent_shape,
+                "trail_tile": m["tuned"].trail_tile, "clocks": m["clocks"]}
 
     if rank == 0:
         cpu = None
@@ -649,22 +706,19 @@ def main():
             "value": value, "unit": "agent-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": args.config, "width": W, "height": H, "n_agents": n,
-                       "decay": "multiply 0.97", "blur": "gauss r=1 sigma=1 rate 0.5",
-                       "reorder_every": args.reorder_every, "graph_chunk": 50,
-                       "l2_persist": not args.no_l2_persist,
-                       "l2": f"agent state {16 * n / 1e6:.0f} MB streamed per step (> 129 MB L2, inputs larger "
-                             f"than L2 between timed steps); trail {4 * W * H / 1e6:.0f} MB"
-                             + (" (fits the 129 MB L2; a persisting window over it is the autotuner's choice, "
-                                "see tuned.l2_window_passes)" if 4 * W * H < 129e6 else " (exceeds L2)"),
-                       "parallelism": f"replicas x{ws}",
-                       "dispatch": "every agent once per step" if args.dispatch == "each" else
-                                   f"the reference's dispatch: {n_visited} of {n} agents updated per step"},
+            "config": workload_config(args, ws),
             "cells_per_s": cells, "pct_roofline_step": pct_roofline,
+            "sensor_modes": {"shader": mode_summary(head, ms, value),
+                             "rotated": mode_summary(rot, rot_ms, rot_value)},
             "tuned": {"trail_tile": tuned.trail_tile, "agent_shape": tuned.agent_shape,
                       "trail_texture": tuned.trail_texture, "l2_persist_bytes": tuned.l2_persist_bytes,
                       "l2_window_passes": {0: "none", 1: "agents", 2: "trail", 3: "both"}[tuned.l2_window_passes]},
-            "kernels": {"agents": k_agents, "trail": k_trail, "other_ms_per_step": other_ms / kern_steps},
+            "kernels": {"agents": k_agents, "trail": k_trail, "other_ms_per_step": other_ms / kern_steps,
+                        "reorder": {"ms": head["reorder_ms"], "every": args.reorder_every,
+                                    "ms_per_step": head["reorder_ms"] / args.reorder_every if args.reorder_every
+                                    else 0.0, "in_timed_window": head["reorders_in"],
+                                    "what": "ms_per_step = timed window - reorders inside it + K x (one "
+                                            "reorder's time / reorder_every): every step pays its share"}},
             "roofline": roofline, "e2e": e2e, "e2e_display": e2e_display, "gpu_launches": launches,
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,

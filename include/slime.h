@@ -74,6 +74,15 @@ extern "C" {
 #define SLIME_DISPATCH_REFERENCE 1u  /* the reference's dispatch: an agent visited by m invocations
                                         moves once (every visit reads the state the pass found)
                                         and deposits m times; m = 0 leaves it as it is */
+/* How the side sensors' directions are evaluated (compute.wgsl:75-86 takes
+ * cos and sin of the binary32 angles angle - sensor_angle and
+ * angle + sensor_angle). */
+#define SLIME_SENSOR_SHADER 0u  /* as the shader writes it: sin/cos of the rounded angle -/+ a (three
+                                   sin/cos evaluations per agent; the default) */
+#define SLIME_SENSOR_ROTATED 1u /* the centre direction rotated by -/+ a (one sin/cos evaluation per
+                                   agent): a few ulp from the shader's directions, enough to flip the turn
+                                   decision of about 5 agents in 100,000 per step at sensor angles of
+                                   0.3-2.5 rad; an opt-in fast mode, not the reference's result */
 
 /* ------------------------------------------------------------ parameters */
 /* The first 14 fields are SimSizeUniform (src/main.rs:29-46) in the same
@@ -99,6 +108,8 @@ typedef struct SlimeParams {
     uint32_t decay_mode; /* SLIME_DECAY_* */
     uint32_t blur_mode;  /* SLIME_BLUR_* */
     uint32_t dispatch_mode; /* SLIME_DISPATCH_* (0, every agent once, is the default) */
+    uint32_t sensor_mode;   /* SLIME_SENSOR_* (0, the shader's evaluation, is the default) */
+    uint32_t _pad2;
 } SlimeParams;
 
 /* Settings (src/settings.rs:30-47), field for field. */
@@ -150,6 +161,8 @@ typedef struct SlimeInfo {
     uint32_t l2_window_passes; /* with a carve-out, the passes whose launches carry the window
                                   (bit 0 the agent pass, bit 1 the trail pass) */
     uint32_t _pad;
+    uint64_t reorders_done; /* Morton reorders run so far (by the step schedule, slime_reorder_agents or the
+                               autotuner) */
 } SlimeInfo;
 
 const char* slime_version(void);
@@ -238,6 +251,10 @@ int slime_reorder_agents(slime_ctx* ctx);
  * the context's stream; totals in milliseconds (NULL outputs are skipped). */
 int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, double* trail_ms,
                         double* other_ms);
+/* Run `reps` Morton reorders back to back on the context's stream, timed with
+ * CUDA events; total milliseconds in *ms.  The agents' results do not change
+ * (every agent keeps its id). */
+int slime_profile_reorder(slime_ctx* ctx, uint32_t reps, double* ms);
 /* Pick the fastest trail tile and agent-kernel shape for this context by
  * timing each candidate in the deposit mode the steps will use, then (with
  * l2_persist on) whether and on which passes the persisting-L2 window pays
@@ -310,9 +327,12 @@ int slime_ensemble_selftest_barrier_timeout(slime_ensemble* ens);
  * d_angle, d_speed: n_agents floats each (agent i has id i), updated in place;
  * d_trail_in / d_trail_out: width*height floats.  Work is enqueued on
  * `stream` (a cudaStream_t, NULL = legacy default stream) and not waited for.
- * The first call on a device looks up the array's device address (make it
- * before any stream capture).  All calls share the array and clear it at
- * their start, so calls that overlap on the GPU race. */
+ * Every call looks up the array's device address on the current device (a
+ * lookup that allocates nothing, so a device reset cannot leave a stale
+ * address behind); the first call on a device also loads the library's
+ * device code there, so make it before any stream capture.  All calls share
+ * the array and clear it at their start, so calls that overlap on the GPU
+ * race. */
 int slime_step_noalloc(const SlimeParams* params, uint32_t width, uint32_t height, uint64_t n_agents, float* d_x,
                        float* d_y, float* d_angle, float* d_speed, const float* d_trail_in, float* d_trail_out,
                        void* stream);

@@ -382,13 +382,22 @@ SLM_FN uint32_t slm_dispatch_visits(uint64_t n, uint64_t index) {
     return slm_dispatch_visits_in((uint32_t)index, wy, span);
 }
 
-/* Sensor directions of compute.wgsl:79-90: cos/sin of angle - a, angle + a
- * and angle.  The centre direction is slm_sincos(angle); the side directions
- * are that vector rotated by -a and +a with (sin a, cos a) =
- * slm_sincos(sensor_angle), a fixed sequence of binary32 products and fused
- * multiply-adds.  WGSL bounds cos and sin only to an absolute error of 2^-11;
- * the rotation is within a few 1e-8 of cos/sin of the rounded sum, i.e. it is
- * one conforming evaluation of cos(angle -/+ a), shared by host and device. */
+/* Sensor directions of compute.wgsl:75-90 as the shader writes them: the
+ * sensor angles angle - a and angle + a are binary32 differences and sums
+ * (:75-76), and each of the three directions is slm_sincos of its own angle. */
+SLM_FN void slm_sensor_dirs_shader(float angle, float a, float* cl, float* sl, float* cc, float* sc, float* cr,
+                                   float* sr) {
+    slm_sincos(slm_sub(angle, a), sl, cl);
+    slm_sincos(slm_add(angle, a), sr, cr);
+    slm_sincos(angle, sc, cc);
+}
+
+/* The rotated form (SLIME_SENSOR_ROTATED): the centre direction is
+ * slm_sincos(angle); the side directions are that vector rotated by -a and +a
+ * with (sin a, cos a) = slm_sincos(sensor_angle), a fixed sequence of
+ * binary32 products and fused multiply-adds.  Within a few 1e-8 of cos/sin of
+ * the rounded angle -/+ a, but not equal to it: near-ties of the turn
+ * decision can go the other way than the shader's. */
 SLM_FN void slm_sensor_dirs(float angle, float sa, float ca, float* cl, float* sl, float* cc, float* sc, float* cr,
                             float* sr) {
     float s, c;

@@ -10,11 +10,12 @@
  * src/compute.wgsl; oracle/wgsl/ translates that shader mechanically to C++
  * and runs it invocation by invocation, and tests/test_reference_pin.py and
  * the frames in tests/golden/wgsl/ show this restatement equal to it bit for
- * bit (sampler, decay, diffuse, agent update, whole frames where the shader
- * does not race), the one difference being the side sensors' directions
- * (rotations of the centre direction here, a few ulp from the shader's
- * cos/sin of the shifted angle).  Also checked against hand-derived known
- * answers and an independent pure-Python restatement (tests/golden).
+ * bit (sampler, decay, diffuse, agent update at any sensor angle, whole
+ * frames where the shader does not race).  The opt-in SLIME_SENSOR_ROTATED
+ * mode is the one deliberate difference: its side sensors' directions are
+ * rotations of the centre direction, a few ulp from the shader's cos/sin of
+ * the shifted angle.  Also checked against hand-derived known answers and an
+ * independent pure-Python restatement (tests/golden).
  *
  * What it restates:
  *   sample_trail_map       compute.wgsl:7-29
@@ -69,15 +70,21 @@ inline float sample_trail_map(const float* trail, int32_t W, int32_t H, float px
 }
 
 /* The three sensor samples of compute.wgsl:75-95 for an agent at (x, y)
- * heading `angle`: sensor angles angle - a, angle + a, angle; their cos/sin
- * as the centre direction and its rotations by -a and +a (slm_sensor_dirs). */
+ * heading `angle`: sensor angles angle - a, angle + a, angle (:75-77) and
+ * their cos/sin (:79-90), each evaluated as written (slm_sensor_dirs_shader);
+ * with SLIME_SENSOR_ROTATED the side directions are the centre direction's
+ * rotations by -a and +a instead (slm_sensor_dirs). */
 inline void sense(const SlimeParams* p, int32_t W, int32_t H, float x, float y, float angle, const float* trail,
                   float* left_value, float* right_value, float* center_value) {
     float dist = p->agent_sensor_distance;
-    float sa, ca;
-    slm_sincos(p->agent_sensor_angle, &sa, &ca);
     float sl, cl, sr, cr, sc, cc;
-    slm_sensor_dirs(angle, sa, ca, &cl, &sl, &cc, &sc, &cr, &sr);
+    if (p->sensor_mode == SLIME_SENSOR_ROTATED) {
+        float sa, ca;
+        slm_sincos(p->agent_sensor_angle, &sa, &ca);
+        slm_sensor_dirs(angle, sa, ca, &cl, &sl, &cc, &sc, &cr, &sr);
+    } else {
+        slm_sensor_dirs_shader(angle, p->agent_sensor_angle, &cl, &sl, &cc, &sc, &cr, &sr);
+    }
     float lpx = slm_add(x, slm_mul(dist, cl)); /* :79-82 */
     float lpy = slm_add(y, slm_mul(dist, sl));
     float rpx = slm_add(x, slm_mul(dist, cr)); /* :83-86 */

@@ -92,11 +92,17 @@ struct Senses {
     typename Trail::Tap left, right, center;
 };
 
+// The sensor directions: by default cos/sin of angle -/+ a and of angle, as
+// the shader evaluates them (compute.wgsl:75-90); with SLIME_SENSOR_ROTATED
+// the centre direction rotated by -/+ a.  The mode is uniform over a launch.
 template <class Trail>
 __device__ __forceinline__ Senses<Trail> agent_sense(const DevParams& p, float x, float y, float angle,
                                                      const Trail& trail) {
     float sl, cl, sr, cr, sc, cc;
-    slm_sensor_dirs(angle, p.sensor_sin, p.sensor_cos, &cl, &sl, &cc, &sc, &cr, &sr);
+    if (p.sensor_mode == SLIME_SENSOR_ROTATED)
+        slm_sensor_dirs(angle, p.sensor_sin, p.sensor_cos, &cl, &sl, &cc, &sc, &cr, &sr);
+    else
+        slm_sensor_dirs_shader(angle, p.sensor_angle, &cl, &sl, &cc, &sc, &cr, &sr);
     Senses<Trail> s;
     s.left = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)), slm_add(y, slm_mul(p.sensor_dist, sl)));
     s.right = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)), slm_add(y, slm_mul(p.sensor_dist, sr)));

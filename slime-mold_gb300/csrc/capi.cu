@@ -60,6 +60,10 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
         *why = "unknown dispatch_mode";
         return false;
     }
+    if (p.sensor_mode > SLIME_SENSOR_ROTATED) {
+        *why = "unknown sensor_mode";
+        return false;
+    }
     DevParams d;
     memset(&d, 0, sizeof(d));
     d.W = (int32_t)W;
@@ -81,6 +85,7 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
     d.decay_mode = p.decay_mode;
     d.blur_mode = p.blur_mode;
     d.dispatch_mode = p.dispatch_mode;
+    d.sensor_mode = p.sensor_mode;
     d.R = 1;
     if (p.blur_mode == SLIME_BLUR_GAUSS) {
         if (!isfinite(p.blur_radius) || !isfinite(p.blur_sigma)) {
@@ -537,6 +542,7 @@ int do_reorder(slime_ctx* ctx) {
                       partition ? reference_dispatch_updated(ctx->agents.n) : ~0ull),
        "reordering agents");
     ctx->launches += 5;
+    ctx->reorders_done++;
     ctx->reordered = true;
     ctx->reorder_partitioned = partition;
     ctx->last_reorder_step = ctx->steps_done;
@@ -816,6 +822,7 @@ int slime_get_info(const slime_ctx* ctx, SlimeInfo* out) {
     out->l2_window_passes = ctx->l2_persist_bytes ? ctx->l2_window_passes : 0u;
     out->_pad = 0;
     out->reordered = ctx->reordered ? 1u : 0u;
+    out->reorders_done = ctx->reorders_done;
     return SLIME_OK;
 }
 
@@ -1115,6 +1122,31 @@ int slime_profile_steps(slime_ctx* ctx, uint32_t n_steps, double* agents_ms, dou
     if (trail_ms) *trail_ms = tt;
     if (other_ms) *other_ms = to;
     return rc;
+}
+
+int slime_profile_reorder(slime_ctx* ctx, uint32_t reps, double* ms) {
+    if (!ctx || !ms) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    *ms = 0.0;
+    if (ctx->agents.n == 0 || reps == 0) return SLIME_OK;
+    // the first reorder allocates the id map and the sort scratch: untimed
+    int rc = do_reorder(ctx);
+    if (rc != SLIME_OK) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "creating events");
+    CK(cudaEventCreate(&e1), "creating events");
+    cudaError_t e = cudaEventRecord(e0, ctx->stream);
+    for (uint32_t r = 0; r < reps && rc == SLIME_OK && e == cudaSuccess; r++) rc = do_reorder(ctx);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != SLIME_OK) return rc;
+    if (e != cudaSuccess) return cuda_error(ctx->err, e, "timing reorders");
+    *ms = t;
+    return SLIME_OK;
 }
 
 int slime_autotune(slime_ctx* ctx, uint32_t reps) {

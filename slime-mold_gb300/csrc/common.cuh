@@ -34,6 +34,7 @@ struct DevParams {
     uint32_t decay_mode;
     uint32_t blur_mode;
     uint32_t dispatch_mode; // SLIME_DISPATCH_*
+    uint32_t sensor_mode;   // SLIME_SENSOR_*
     int32_t R;      // Gaussian taps per side
     float w[2 * kMaxR + 1];
     float w2sum_m1; // (sum of w)^2 - 1 in binary64, rounded: B(u) - u = sum w w (u_n - u_c) + this * u_c

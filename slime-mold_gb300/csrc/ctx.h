@@ -21,6 +21,7 @@ struct slime_ctx {
     // (identity ids have them first too)
     bool reorder_partitioned = false;
     uint64_t last_reorder_step = ~0ull;
+    uint64_t reorders_done = 0;
     slime::ReorderScratch reorder;
 
     float* trail[2] = {nullptr, nullptr};

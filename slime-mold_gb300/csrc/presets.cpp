@@ -130,6 +130,7 @@ void slime_params_from_settings(const SlimeSettings* s, uint32_t width, uint32_t
     out->decay_mode = SLIME_DECAY_REF_SUBTRACT;
     out->blur_mode = SLIME_BLUR_REF_BOX3;
     out->dispatch_mode = SLIME_DISPATCH_EACH_AGENT;
+    out->sensor_mode = SLIME_SENSOR_SHADER; // cos/sin(angle -/+ a), compute.wgsl:75-86
 }
 
 } // extern "C"

@@ -19,38 +19,29 @@
 // slime_step_noalloc_scratch takes the counts array from the caller instead
 // (width * height 32-bit words of its own device memory): no size limit
 // beyond the context's, and calls with separate arrays may overlap.
-#include <mutex>
-
 #include "kernels.h"
 
 namespace {
 
 constexpr uint64_t kNoAllocMaxCells = 1ull << 20;
-constexpr int kMaxDevices = 64;
 
 // The deposit counts of the step in flight.  In host code this name is only a
-// host-side stand-in, never a device address: the address is looked up once
-// per device with cudaGetSymbolAddress.
+// host-side stand-in, never a device address: the address is looked up with
+// cudaGetSymbolAddress.
 static __device__ __align__(256) uint32_t slime_noalloc_counts[kNoAllocMaxCells];
 
-std::mutex g_setup_mutex;
-uint32_t* g_counts_addr[kMaxDevices] = {};
-
-// Per-device set-up, done on the first call on each device with that device
-// current.
-int counts_address(int device, uint32_t** out) {
-    if (device < 0 || device >= kMaxDevices) return SLIME_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_counts_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, slime_noalloc_counts);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return SLIME_ERR_CUDA;
-        }
-        g_counts_addr[device] = (uint32_t*)p;
+// The array's address on the current device, looked up on every call (the
+// lookup allocates nothing).  A cached address would outlive the module it
+// belongs to: after a cudaDeviceReset the runtime loads the module again,
+// possibly elsewhere.  The first lookup on a device loads the module there.
+int counts_address(uint32_t** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, slime_noalloc_counts);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return SLIME_ERR_CUDA;
     }
-    *out = g_counts_addr[device];
+    *out = (uint32_t*)p;
     return SLIME_OK;
 }
 
@@ -114,7 +105,7 @@ extern "C" int slime_step_noalloc(const SlimeParams* params, uint32_t width, uin
         return SLIME_ERR_NO_DEVICE;
     }
     uint32_t* counts = nullptr;
-    int rc = counts_address(device, &counts);
+    int rc = counts_address(&counts);
     if (rc != SLIME_OK) return rc;
     return step_with_counts(params, width, height, n_agents, d_x, d_y, d_angle, d_speed, d_trail_in, d_trail_out,
                             counts, kNoAllocMaxCells, (cudaStream_t)stream);

@@ -13,14 +13,14 @@ import numpy as np
 
 from . import _abi
 from ._abi import (BLUR_GAUSS, BLUR_REF_BOX3, DECAY_MULTIPLY, DECAY_REF_SUBTRACT, DISPATCH_EACH_AGENT,
-                   DISPATCH_REFERENCE, MAX_BLUR_RADIUS, SlimeGrads,
+                   DISPATCH_REFERENCE, MAX_BLUR_RADIUS, SENSOR_ROTATED, SENSOR_SHADER, SlimeGrads,
                    SlimeInfo, SlimeOptions, SlimeParams, SlimeSettings)
 
 __all__ = [
     "SlimeError", "Settings", "default_settings", "preset_names", "preset", "params_from_settings",
     "Simulation", "Ensemble", "SlimeParams", "SlimeOptions", "SlimeGrads", "lib",
     "DECAY_REF_SUBTRACT", "DECAY_MULTIPLY", "BLUR_REF_BOX3", "BLUR_GAUSS", "MAX_BLUR_RADIUS",
-    "DISPATCH_EACH_AGENT", "DISPATCH_REFERENCE",
+    "DISPATCH_EACH_AGENT", "DISPATCH_REFERENCE", "SENSOR_SHADER", "SENSOR_ROTATED",
 ]
 
 Settings = SlimeSettings
@@ -231,6 +231,12 @@ class Simulation:
         self._check(self._L.slime_profile_steps(self._h, n_steps, C.byref(a), C.byref(t), C.byref(o)),
                     "profile_steps")
         return a.value, t.value, o.value
+
+    def profile_reorder(self, reps=5):
+        """Milliseconds that `reps` back-to-back Morton reorders take on the device."""
+        ms = C.c_double()
+        self._check(self._L.slime_profile_reorder(self._h, reps, C.byref(ms)), "profile_reorder")
+        return ms.value
 
     def autotune(self, reps=5):
         self._check(self._L.slime_autotune(self._h, reps), "autotune")

@@ -24,6 +24,8 @@ BLUR_GAUSS = 1
 MAX_BLUR_RADIUS = 8
 DISPATCH_EACH_AGENT = 0
 DISPATCH_REFERENCE = 1
+SENSOR_SHADER = 0
+SENSOR_ROTATED = 1
 
 
 class SlimeParams(C.Structure):
@@ -46,6 +48,8 @@ class SlimeParams(C.Structure):
         ("decay_mode", C.c_uint32),
         ("blur_mode", C.c_uint32),
         ("dispatch_mode", C.c_uint32),
+        ("sensor_mode", C.c_uint32),
+        ("_pad2", C.c_uint32),
     ]
 
     def copy(self):
@@ -109,6 +113,7 @@ class SlimeInfo(C.Structure):
         ("l2_persist_bytes", C.c_uint64),
         ("l2_window_passes", C.c_uint32),
         ("_pad", C.c_uint32),
+        ("reorders_done", C.c_uint64),
     ]
 
 
@@ -161,6 +166,7 @@ SIGNATURES = {
     "slime_reorder_agents": (C.c_int, [P]),
     "slime_profile_steps": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)]),
+    "slime_profile_reorder": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_double)]),
     "slime_autotune": (C.c_int, [P, C.c_uint32]),
     "slime_forward_record": (C.c_int, [P, C.c_uint32, C.c_uint32]),
     "slime_backward": (C.c_int, [P, F32P, C.POINTER(SlimeGrads), F32P]),

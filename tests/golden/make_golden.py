@@ -25,7 +25,7 @@ def base_params(**kw):
     p = dict(decay_factor=0.97, agent_jitter=0.05, agent_speed_min=30.0, agent_speed_max=50.0,
              agent_turn_speed=0.3, agent_sensor_angle=0.4, agent_sensor_distance=9.0, diffusion_rate=0.5,
              pheromone_deposition_amount=1.0, blur_radius=1.0, blur_sigma=1.0, time_step=0.016,
-             decay_mode=1, blur_mode=1)
+             decay_mode=1, blur_mode=1, sensor_mode=0)
     p.update(kw)
     return {k: (np.float32(v) if k in PARAM_KEYS else int(v)) for k, v in p.items()}
 
@@ -44,6 +44,8 @@ def cases():
     yield "ref_box", W, H, base_params(decay_mode=0, blur_mode=0, decay_factor=10.0, agent_jitter=0.3,
                                        agent_turn_speed=0.43), agents(300, W, H, 30, 50, 1), 3
     yield "mult_gauss_r1", W, H, base_params(), agents(300, W, H, 30, 50, 2), 3
+    # the opt-in rotated side-sensor directions (SLIME_SENSOR_ROTATED)
+    yield "mult_gauss_r1_rotated", W, H, base_params(sensor_mode=1), agents(300, W, H, 30, 50, 2), 3
     yield "gauss_r2_subtract", W, H, base_params(decay_mode=0, blur_radius=2.0, blur_sigma=1.5,
                                                  decay_factor=20.0, pheromone_deposition_amount=0.3,
                                                  agent_jitter=2.0), agents(300, W, H, 60, 120, 3), 3

@@ -230,12 +230,17 @@ def agent_update(p, W, H, index, a, trail):
     x, y, angle, speed = (f32(v) for v in a)
     speed = clamp(speed, p["agent_speed_min"], p["agent_speed_max"])
     dist = p["agent_sensor_distance"]
-    # cos/sin of angle -/+ a as the rotation of (cos angle, sin angle) by -/+ a
-    sa, ca = sincos(p["agent_sensor_angle"])
     sc, cc = sincos(angle)
-    cca, sca = mul(cc, ca), mul(sc, ca)
-    cl, sl = fma(sc, sa, cca), fma(f32(-cc), sa, sca)
-    cr, sr = fma(f32(-sc), sa, cca), fma(cc, sa, sca)
+    if p.get("sensor_mode", 0) == 1:
+        # rotated mode: (cos angle, sin angle) rotated by -/+ a
+        sa, ca = sincos(p["agent_sensor_angle"])
+        cca, sca = mul(cc, ca), mul(sc, ca)
+        cl, sl = fma(sc, sa, cca), fma(f32(-cc), sa, sca)
+        cr, sr = fma(f32(-sc), sa, cca), fma(cc, sa, sca)
+    else:
+        # compute.wgsl:75-90: cos/sin of the binary32 angles angle -/+ a
+        sl, cl = sincos(sub(angle, p["agent_sensor_angle"]))
+        sr, cr = sincos(add(angle, p["agent_sensor_angle"]))
     left = sample(trail, W, H, add(x, mul(dist, cl)), add(y, mul(dist, sl)))
     right = sample(trail, W, H, add(x, mul(dist, cr)), add(y, mul(dist, sr)))
     center = sample(trail, W, H, add(x, mul(dist, cc)), add(y, mul(dist, sc)))

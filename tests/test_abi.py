@@ -34,10 +34,11 @@ def test_library_exports_every_declared_symbol(built_lib):
 
 def test_struct_layouts():
     from slime_gb300 import SlimeParams, SlimeSettings, SlimeOptions, SlimeGrads
-    # SimSizeUniform is 14 x 4 bytes (src/main.rs:29-46); the extensions add 16.
-    assert C.sizeof(SlimeParams) == 72
+    # SimSizeUniform is 14 x 4 bytes (src/main.rs:29-46); the extensions add 24.
+    assert C.sizeof(SlimeParams) == 80
     assert SlimeParams.blur_sigma.offset == 48 and SlimeParams._pad.offset == 52
     assert SlimeParams.time_step.offset == 56
+    assert SlimeParams.dispatch_mode.offset == 68 and SlimeParams.sensor_mode.offset == 72
     assert C.sizeof(SlimeGrads) == 32
     assert C.sizeof(SlimeOptions) == 32
 

@@ -25,9 +25,9 @@ SIZES = {
 }
 
 
-def bench_params(W, H, lo, hi, dist):
+def bench_params(W, H, lo, hi, dist, sensor_mode=0):
     return config0_params(W, H, decay_mode=1, blur_mode=1, agent_speed_min=lo, agent_speed_max=hi,
-                          agent_sensor_distance=dist)
+                          agent_sensor_distance=dist, sensor_mode=sensor_mode)
 
 
 def expected_counts(agents, W, H):
@@ -39,10 +39,10 @@ def expected_counts(agents, W, H):
     return np.bincount(cy[ok] * W + cx[ok], minlength=W * H).astype(np.uint32).reshape(H, W)
 
 
-@pytest.mark.parametrize("size", ["4096", "8192"])
-def test_full_size_steps_bitexact(gpu, size):
+@pytest.mark.parametrize("size,sensor_mode", [("4096", 0), ("8192", 0), ("4096", 1)])
+def test_full_size_steps_bitexact(gpu, size, sensor_mode):
     W, H, n, lo, hi, dist = SIZES[size]
-    p = bench_params(W, H, lo, hi, dist)
+    p = bench_params(W, H, lo, hi, dist, sensor_mode)
     agents = agents_uniform(n, W, H, lo, hi, seed=11)
     trail = np.random.default_rng(12).random((H, W), dtype=np.float32)
     sim = make_sim(W, H, n, p, agents, trail)

@@ -24,6 +24,8 @@ def load(path):
     p.width, p.height = int(d["W"]), int(d["H"])
     for k in KEYS:
         setattr(p, k, d["p_" + k].item())
+    # the side-sensor evaluation (0, the shader's, unless the case says otherwise)
+    p.sensor_mode = int(d["p_sensor_mode"]) if "p_sensor_mode" in d else 0
     return d, p
 
 

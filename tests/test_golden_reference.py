@@ -30,6 +30,8 @@ def load(path):
     p.width, p.height = int(d["W"]), int(d["H"])
     for k in KEYS:
         setattr(p, k, d["p_" + k].item())
+    # the side-sensor evaluation (0, the shader's, unless the case says otherwise)
+    p.sensor_mode = int(d["p_sensor_mode"]) if "p_sensor_mode" in d else 0
     return d, p
 
 
@@ -45,7 +47,7 @@ def check(d, s, agents, trail, counts):
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) == 3
+    assert len(FIXTURES) == 5
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p))
@@ -60,6 +62,23 @@ def test_oracle_reproduces_reference_frames(path):
             t = oracle.trail_pass(p, W, H, t, c)
             done += 1
         check(d, s, a, t, c)
+
+
+def test_rotated_mode_departs_from_the_reference_frames():
+    """The fixtures discriminate: with the opt-in rotated sensor directions
+    the oracle leaves the reference's run on at least one of them (a flipped
+    near-tie turn, then chaotic divergence), while the default mode
+    reproduces all of them."""
+    departed = []
+    for path in FIXTURES:
+        d, p = load(path)
+        p.sensor_mode = 1
+        W, H = int(d["W"]), int(d["H"])
+        a, t = d["agents0"].copy(), d["trail0"].copy()
+        last = d["frames"].tolist()[-1]
+        oracle.run(p, W, H, a, t, last)
+        departed.append(not np.array_equal(a.view(np.uint32), d[f"agents{last}"].view(np.uint32)))
+    assert any(departed)
 
 
 @pytest.mark.gpu

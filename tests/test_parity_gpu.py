@@ -121,9 +121,10 @@ def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
         assert_bitexact(sim.download_agents(), ca, "agents")
 
 
+@pytest.mark.parametrize("sensor_mode", [0, 1])
 @pytest.mark.parametrize("shape", range(1, 16))
 @pytest.mark.parametrize("W,H", [(256, 150), (201, 150)])
-def test_every_agent_shape_is_bitexact(gpu, shape, W, H):
+def test_every_agent_shape_is_bitexact(gpu, shape, W, H, sensor_mode):
     # 256 wide: the trail has gather textures; 201 wide: its rows are not
     # aligned for one, and the texture shapes (13..15) run their pointer
     # twins.  The largest case runs Morton-reordered (slot -> id map).
@@ -132,7 +133,7 @@ def test_every_agent_shape_is_bitexact(gpu, shape, W, H):
     assert sim0.info().trail_texture == (1 if W == 256 else 0)
     for n in (1, 3, 4097, 20001):
         p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, agent_speed_min=30.0,
-                           agent_speed_max=50.0, agent_jitter=0.3)
+                           agent_speed_max=50.0, agent_jitter=0.3, sensor_mode=sensor_mode)
         agents = agents_uniform(n, W, H, 30.0, 50.0, seed=n)
         trail = np.random.default_rng(n).random((H, W), dtype=np.float32)
         sim = make_sim(W, H, n, p, agents, trail)
@@ -141,8 +142,8 @@ def test_every_agent_shape_is_bitexact(gpu, shape, W, H):
         sim.step(3)
         ca, ct = agents.copy(), trail.copy()
         oracle.run(p, W, H, ca, ct, 3)
-        assert_bitexact(sim.download_agents(), ca, f"agents shape {shape} n {n}")
-        assert_bitexact(sim.download_trail(), ct, f"trail shape {shape} n {n}")
+        assert_bitexact(sim.download_agents(), ca, f"agents shape {shape} n {n} sensor mode {sensor_mode}")
+        assert_bitexact(sim.download_trail(), ct, f"trail shape {shape} n {n} sensor mode {sensor_mode}")
 
 
 def test_autotune_keeps_state(gpu):

@@ -35,7 +35,7 @@ def draw(rng):
         agent_turn_speed=f(-0.5, 4.0), agent_sensor_angle=f(-3.5, 3.5), agent_sensor_distance=f(0.0, 40.0),
         diffusion_rate=f(-0.3, 1.3), pheromone_deposition_amount=f(0.0, 2.5),
         blur_radius=f(0.0, 2.99) if blur_mode == 1 else 1.0, blur_sigma=f(0.3, 3.0),
-        time_step=f(0.0, 0.05), dispatch_mode=int(rng.integers(0, 2)))
+        time_step=f(0.0, 0.05), dispatch_mode=int(rng.integers(0, 2)), sensor_mode=int(rng.integers(0, 2)))
     options = dict(reorder_every=int(rng.choice([0, 1, 3])), use_graphs=int(rng.integers(0, 2)),
                    exact_counts=int(rng.integers(0, 2)))
     return W, H, n, p, options

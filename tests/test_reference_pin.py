@@ -16,11 +16,12 @@ invocation by invocation, and the tests compare with the oracle bit for bit:
     race: deposition 1.0 on a trail in [0, 1], or cells one agent lands on.
 
 WGSL leaves sin and cos to the implementation; both sides take them from
-include/slime_math.h.  The one deliberate difference: the oracle (and the
-GPU) form the side sensors' directions by rotating (cos a, sin a) by the
-sensor angle instead of evaluating cos/sin of the shifted angle.  The update
-is compared exactly with a sensor angle of 0 (the two coincide) and, for
-other angles, agent by agent: it differs exactly where the few-ulp
+include/slime_math.h.  By default (SLIME_SENSOR_SHADER) the side sensors'
+directions are cos/sin of the rounded angle -/+ a, as the shader writes
+them, and everything compares bit for bit at every sensor angle, including
+300 whole frames at the reference's default settings.  The opt-in rotated
+mode (SLIME_SENSOR_ROTATED) forms them by rotating (cos angle, sin angle)
+instead; it is compared agent by agent: it differs exactly where the few-ulp
 difference in a sensor's position flips a turn decision.
 """
 import numpy as np
@@ -121,20 +122,50 @@ def agent_cases(W, H, n, seed, huge_headings=True):
 
 
 def test_agent_update_matches_reference_exactly_with_axis_sensors():
-    """Sensor angle 0: rotation and shifted-angle evaluation coincide, so the
+    """Sensor angle 0: both sensor modes coincide with the shader, so the
     whole update (speed clamp, sampling, turn, jitter hash, wrap, move) must
-    agree bit for bit, huge headings included."""
+    agree bit for bit in either mode, huge headings included."""
     W, H, n = 256, 192, 40000
     trail = np.random.default_rng(5).random((H, W), dtype=np.float32)
-    for jitter, turn in ((0.05, 0.3), (1.0, 0.43), (0.0, 2.0)):
-        p = config0_params(W, H, agent_sensor_angle=0.0, agent_jitter=jitter, agent_turn_speed=turn,
-                           pheromone_deposition_amount=0.0, agent_speed_min=30.0, agent_speed_max=50.0)
-        agents = agent_cases(W, H, n, seed=int(turn * 100))
-        assert same_bits(oracle.sense(p, W, H, agents, trail), wgslref.sense(p, agents, trail))
-        ref_a, _ = wgslref.agents_pass(p, agents, trail)
-        got = agents.copy()
-        oracle.agents_pass(p, W, H, got, trail)
-        assert same_bits(got, ref_a), (jitter, turn)
+    for mode in (0, 1):
+        for jitter, turn in ((0.05, 0.3), (1.0, 0.43), (0.0, 2.0)):
+            p = config0_params(W, H, agent_sensor_angle=0.0, agent_jitter=jitter, agent_turn_speed=turn,
+                               pheromone_deposition_amount=0.0, agent_speed_min=30.0, agent_speed_max=50.0,
+                               sensor_mode=mode)
+            agents = agent_cases(W, H, n, seed=int(turn * 100))
+            assert same_bits(oracle.sense(p, W, H, agents, trail), wgslref.sense(p, agents, trail))
+            ref_a, _ = wgslref.agents_pass(p, agents, trail)
+            got = agents.copy()
+            oracle.agents_pass(p, W, H, got, trail)
+            assert same_bits(got, ref_a), (mode, jitter, turn)
+
+
+def pin_trail(kind, W, H, rng):
+    if kind == "continuous":
+        return rng.random((H, W), dtype=np.float32)
+    return (rng.integers(0, 9, (H, W)) / 8.0).astype(np.float32)  # values 1/8 apart, many exact ties
+
+
+@pytest.mark.parametrize("sensor_angle", [0.3, 0.4, 0.7854, 2.5])
+@pytest.mark.parametrize("trail_kind", ["continuous", "eighths"])
+def test_agent_update_matches_reference_exactly(sensor_angle, trail_kind):
+    """The default sensor mode evaluates cos/sin(angle -/+ a) as the shader
+    does: at the reference's sensor angle (0.3), config 0's (0.4), pi/4 and
+    2.5 rad, on continuous and on tie-rich trails, with negative and huge
+    initial headings, every sensor sample and every agent's whole update is
+    the reference's bit for bit (no differing agent at all)."""
+    W, H, n = 256, 192, 40000
+    trail = pin_trail(trail_kind, W, H, np.random.default_rng(7))
+    p = config0_params(W, H, agent_sensor_angle=sensor_angle, agent_jitter=0.05, agent_turn_speed=0.3,
+                       pheromone_deposition_amount=0.0, agent_speed_min=30.0, agent_speed_max=50.0)
+    assert p.sensor_mode == 0
+    agents = agent_cases(W, H, n, seed=8)
+    assert same_bits(oracle.sense(p, W, H, agents, trail), wgslref.sense(p, agents, trail))
+    ref_a, _ = wgslref.agents_pass(p, agents, trail)
+    got = agents.copy()
+    oracle.agents_pass(p, W, H, got, trail)
+    differ = ~np.all(bits(got) == bits(ref_a), axis=1)
+    assert differ.sum() == 0, differ.sum()
 
 
 def decision(s):
@@ -145,22 +176,19 @@ def decision(s):
 
 @pytest.mark.parametrize("sensor_angle", [0.4, 0.7854, 2.5])
 @pytest.mark.parametrize("trail_kind", ["continuous", "eighths"])
-def test_agent_update_matches_reference_but_for_near_tie_turns(sensor_angle, trail_kind):
-    """Other sensor angles: the two evaluations of the side directions differ
-    by a few ulp, so the sensor samples agree within 2 ulp(W) (trail values
-    in [0, 1]) unless a sensor sits on the sampler's edge (0 on one side),
-    and an agent's update differs from the reference's exactly when that
-    difference flips its turn decision: every other agent, and every other
-    part of the update, is bit for bit the reference's.  Measured: 4 to 5
-    agents in 100,000 flip."""
+def test_rotated_mode_differs_only_at_near_tie_turns(sensor_angle, trail_kind):
+    """The opt-in rotated mode: the two evaluations of the side directions
+    differ by a few ulp, so the sensor samples agree within 2 ulp(W) (trail
+    values in [0, 1]) unless a sensor sits on the sampler's edge (0 on one
+    side), and an agent's update differs from the reference's exactly when
+    that difference flips its turn decision: every other agent, and every
+    other part of the update, is bit for bit the reference's.  Measured: 4 to
+    5 agents in 100,000 flip."""
     W, H, n = 256, 192, 40000
-    rng = np.random.default_rng(7)
-    if trail_kind == "continuous":
-        trail = rng.random((H, W), dtype=np.float32)
-    else:  # values 1/8 apart, many exact ties
-        trail = (rng.integers(0, 9, (H, W)) / 8.0).astype(np.float32)
+    trail = pin_trail(trail_kind, W, H, np.random.default_rng(7))
     p = config0_params(W, H, agent_sensor_angle=sensor_angle, agent_jitter=0.05, agent_turn_speed=0.3,
-                       pheromone_deposition_amount=0.0, agent_speed_min=30.0, agent_speed_max=50.0)
+                       pheromone_deposition_amount=0.0, agent_speed_min=30.0, agent_speed_max=50.0,
+                       sensor_mode=1)
     agents = agent_cases(W, H, n, seed=8, huge_headings=False)
     ours_s, ref_s = oracle.sense(p, W, H, agents, trail), wgslref.sense(p, agents, trail)
     # a sensor position x + d cos is rounded at ulp(x): a few-ulp change of
@@ -183,17 +211,21 @@ def test_agent_update_matches_reference_but_for_near_tie_turns(sensor_angle, tra
 
 def test_sensor_samples_at_huge_headings():
     """Headings far outside [0, 2pi) (possible only in an initial state: every
-    update wraps the heading into [0, 2pi)): the shader's angle -/+ a is
-    rounded at the heading's ulp (at 1e6, 0.0625 rad), the rotation is not,
-    so the side directions differ by up to ulp(heading) / 2 rad and a sensor
-    9 px out moves by up to 9 ulp / 2 px.  With trail values in [0, 1] a
-    sample moves by at most that (outside [-pi, pi] WGSL gives cos and sin no
-    accuracy at all).  The centre sensor is the same on both sides."""
+    update wraps the heading into [0, 2pi)).  The default mode rounds
+    angle -/+ a at the heading's ulp exactly as the shader does, so every
+    sample is the reference's.  In the rotated mode the rotation is not
+    rounded there (at 1e6, ulp = 0.0625 rad), so the side directions differ
+    by up to ulp(heading) / 2 rad and a sensor 9 px out moves by up to
+    9 ulp / 2 px; with trail values in [0, 1] a sample moves by at most that
+    (outside [-pi, pi] WGSL gives cos and sin no accuracy at all).  The
+    centre sensor is the same in both."""
     W, H, n = 256, 192, 20000
     trail = np.random.default_rng(10).random((H, W), dtype=np.float32)
     p = config0_params(W, H, pheromone_deposition_amount=0.0)
     agents = agents_uniform(n, W, H, 1.0, 2.0, seed=12)
     agents[:, 2] = np.random.default_rng(13).uniform(-1e6, 1e6, n).astype(np.float32)
+    assert same_bits(oracle.sense(p, W, H, agents, trail), wgslref.sense(p, agents, trail))
+    p.sensor_mode = 1
     ours_s, ref_s = oracle.sense(p, W, H, agents, trail), wgslref.sense(p, agents, trail)
     assert same_bits(ours_s[:, 2], ref_s[:, 2])
     bound = 9.0 * np.spacing(np.abs(agents[:, 2])).astype(np.float64) / 2 + 2 * np.spacing(np.float32(W)) + 1e-6
@@ -202,15 +234,15 @@ def test_sensor_samples_at_huge_headings():
     assert np.all((d <= bound[:, None]) | off_edge)
 
 
-@pytest.mark.parametrize("W,H", [(256, 192), (97, 61)])
-def test_full_steps_match_reference_at_saturating_deposition(W, H):
+@pytest.mark.parametrize("W,H,sensor_angle", [(256, 192, 0.0), (97, 61, 0.0), (256, 192, 0.4), (97, 61, 0.7854)])
+def test_full_steps_match_reference_at_saturating_deposition(W, H, sensor_angle):
     """Deposition 1.0 (the reference's default) on a trail in [0, 1]: every
     deposit leaves its cell at 1 whatever order the racing invocations take,
-    so the reference's frame is deterministic.  Sensor angle 0 (no rotation
-    rounding): 25 whole frames, agents and trail, bit for bit."""
+    so the reference's frame is deterministic.  25 whole frames, agents and
+    trail, bit for bit, with axis sensors and at config 0's sensor angle."""
     n = 20000
     p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=0.97, diffusion_rate=0.5,
-                       agent_sensor_angle=0.0, pheromone_deposition_amount=1.0)
+                       agent_sensor_angle=sensor_angle, pheromone_deposition_amount=1.0)
     agents = agents_uniform(n, W, H, 1.0, 2.0, seed=14)
     trail = np.random.default_rng(15).random((H, W), dtype=np.float32)
     ref_a, ref_t = agents, trail
@@ -280,26 +312,51 @@ def _stat_distance(a, b):
             float(np.max(np.abs(np.log(a[2][1:] / b[2][1:])))))
 
 
-def test_long_run_statistics_match_reference():
+def default_settings_params(W, H, **kw):
+    """The reference's default settings (src/settings.rs:10-27) in its own
+    decay and blur."""
+    return config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, diffusion_rate=1.0,
+                          agent_sensor_angle=0.3, agent_sensor_distance=20.0, agent_turn_speed=0.43, agent_jitter=0.0,
+                          agent_speed_min=30.0, agent_speed_max=50.0, pheromone_deposition_amount=1.0, **kw)
+
+
+def test_long_run_matches_reference_bit_for_bit():
     """300 frames at the reference's default settings (sensor angle 0.3,
     deposition 1.0, so the shader's frame is deterministic), 8,192 agents on
-    128^2 from a zero trail.  The rotated sensor directions flip a near-tie
-    turn now and then and the dynamics are chaotic, so the two runs part ways
-    (nearly every agent differs at the end).  Their trails must agree
-    statistically: trail mass, value histogram and radial power spectrum are
-    closer between the reference and the oracle from the same start than
-    between the oracle and itself from three other random starts (measured:
-    0.026 / 0.036 / 0.25 against at least 0.091 / 0.086 / 0.68)."""
+    128^2 from a zero trail: in the default sensor mode the oracle's run is
+    the reference's, every agent and every trail cell of the last frame bit
+    for bit, although the dynamics are chaotic (one flipped turn would make
+    the runs part ways)."""
     W = H = 128
     n, frames = 8192, 300
-    p = config0_params(W, H, decay_mode=0, blur_mode=0, decay_factor=10.0, diffusion_rate=1.0,
-                       agent_sensor_angle=0.3, agent_sensor_distance=20.0, agent_turn_speed=0.43, agent_jitter=0.0,
-                       agent_speed_min=30.0, agent_speed_max=50.0, pheromone_deposition_amount=1.0)
+    p = default_settings_params(W, H)
+    ref_a, ref_t = agents_uniform(n, W, H, 30.0, 50.0, seed=1), np.zeros((H, W), np.float32)
+    our_a, our_t = ref_a.copy(), ref_t.copy()
+    for _ in range(frames):
+        ref_a, ref_t = wgslref.frame(p, ref_a, ref_t)
+    oracle.run(p, W, H, our_a, our_t, frames)
+    assert same_bits(our_a, ref_a)
+    assert same_bits(our_t, ref_t)
+    assert ref_t.max() > 0.9  # deposits reached the trail (1.0, then one decay step)
+
+
+def test_rotated_mode_long_run_statistics_match_reference():
+    """The same 300 frames in the rotated sensor mode: its sensor directions
+    flip a near-tie turn now and then and the dynamics are chaotic, so the
+    two runs part ways (nearly every agent differs at the end).  Their trails
+    must agree statistically: trail mass, value histogram and radial power
+    spectrum are closer between the reference and the oracle from the same
+    start than between the oracle and itself from three other random starts
+    (measured: 0.026 / 0.036 / 0.25 against at least 0.091 / 0.086 / 0.68)."""
+    W = H = 128
+    n, frames = 8192, 300
+    p = default_settings_params(W, H)
+    ours_p = default_settings_params(W, H, sensor_mode=1)
 
     def ours(seed):
         a = agents_uniform(n, W, H, 30.0, 50.0, seed=seed)
         t = np.zeros((H, W), np.float32)
-        oracle.run(p, W, H, a, t, frames)
+        oracle.run(ours_p, W, H, a, t, frames)
         return a, t
 
     ref_a, ref_t = agents_uniform(n, W, H, 30.0, 50.0, seed=1), np.zeros((H, W), np.float32)
