@@ -55,9 +55,9 @@ def metric_name(cfg_name):
 
 
 def agents_kernel_name(shape):
-    """Kernel of agent-shape table entry `shape` (agents.cu): 9-11, 13 and 14
-    are the persistent kernel (13 and 14 sample through the trail texture)."""
-    return "agents_persistent_kernel" if shape in (9, 10, 11, 13, 14) else "agents_kernel"
+    """Kernel of agent-shape table entry `shape` (agents.cu): 9-11 and 13-15
+    are the persistent kernel (13-15 sample through the trail texture)."""
+    return "agents_persistent_kernel" if shape in (9, 10, 11, 13, 14, 15) else "agents_kernel"
 
 
 def trail_kernel_name(tile, blur_mode):
@@ -720,7 +720,7 @@ def main():
                                     "what": "ms_per_step = timed window - reorders inside it + K x (one "
                                             "reorder's time / reorder_every): every step pays its share"}},
             "roofline": roofline, "e2e": e2e, "e2e_display": e2e_display, "gpu_launches": launches,
-            "clocks": clocks.summary(),
+            "clocks": clocks,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -181,6 +181,26 @@ int slime_preset_find(const char* name, SlimeSettings* out);
  * (src/main.rs:48-66) plus the reference's defaults for the extensions. */
 void slime_params_from_settings(const SlimeSettings* settings, uint32_t width, uint32_t height,
                                 SlimeParams* out);
+/* Settings as a parameter file (the reference keeps Settings only in memory;
+ * `simulation_settings.toml` is named in its .gitignore): one `key = value`
+ * line per field of Settings (src/settings.rs:30-47), in the TOML subset that
+ * struct maps onto: integers, floats with 9 significant digits (every
+ * binary32 round-trips exactly) written with a decimal point or exponent,
+ * `true` / `false`, and the heading range as
+ * `agent_possible_starting_headings = { start = 0.0, end = 360.0 }`.
+ * slime_settings_to_text writes the text and its NUL into buf (cap bytes) and
+ * its length without the NUL into *len; SLIME_ERR_INVALID_ARGUMENT if it did
+ * not fit (buf NULL and cap 0 ask for the length only). */
+int slime_settings_to_text(const SlimeSettings* settings, char* buf, size_t cap, size_t* len);
+/* Parse such text: start from Settings::default() and apply each line; `#`
+ * starts a comment, blank lines are skipped, keys may come in any order, each
+ * at most once.  An unknown or repeated key, a malformed value or an integer
+ * out of its field's range returns SLIME_ERR_INVALID_ARGUMENT with the 1-based
+ * line in *error_line (when not NULL); `out` is written only on success. */
+int slime_settings_from_text(const char* text, SlimeSettings* out, int* error_line);
+/* The same through a file. */
+int slime_settings_save(const SlimeSettings* settings, const char* path);
+int slime_settings_load(const char* path, SlimeSettings* out, int* error_line);
 
 /* ------------------------------------------------ simulation context */
 typedef struct slime_ctx slime_ctx;
@@ -222,6 +242,23 @@ int slime_resize(slime_ctx* ctx, uint32_t width, uint32_t height);
  * seeds every agent anew (seeded; the reference uses rand::random).  Out of
  * device memory it returns SLIME_ERR_OUT_OF_MEMORY with the agents unchanged. */
 int slime_set_agent_count(slime_ctx* ctx, uint64_t n_agents, uint64_t seed);
+
+/* Checkpoint / resume (no counterpart in the reference, whose state lives
+ * only in its GPU buffers).  slime_state_save writes the context's trail size,
+ * agent count, step counter, parameters, agents (AoS, id order) and trail to
+ * a file: the 8 bytes "SLMSTATE", then little-endian uint32 version (1),
+ * width, height, sizeof(SlimeParams), uint64 agent count and step counter,
+ * the SlimeParams bytes, the agents (16 bytes each) and the trail (4 bytes a
+ * cell).  slime_state_load restores such a file into a context of the same
+ * size and agent count (SLIME_ERR_INVALID_ARGUMENT otherwise, with the
+ * context unchanged), including the step counter, so that the Morton reorder
+ * schedule continues where it was; the results of the steps that follow are
+ * those of the uninterrupted run, bit for bit. */
+int slime_state_save(slime_ctx* ctx, const char* path);
+int slime_state_load(slime_ctx* ctx, const char* path);
+/* Set the step counter (SlimeInfo.steps_done), which places the Morton
+ * reorders (one every options.reorder_every steps). */
+int slime_set_steps_done(slime_ctx* ctx, uint64_t steps_done);
 
 /* Advance n_steps steps: the agent dispatch, the decay dispatch and the
  * diffuse dispatch of src/main.rs:1163-1235, n_steps times.  Asynchronous with
@@ -308,6 +345,19 @@ int slime_ensemble_get_stream(slime_ensemble* ens, void** stream);
 int slime_ensemble_autotune(slime_ensemble* ens, uint32_t reps);
 /* Total kernels enqueued so far. */
 int slime_ensemble_launch_count(const slime_ensemble* ens, uint64_t* out);
+typedef struct SlimeEnsembleInfo {
+    uint32_t n_colonies;
+    uint32_t graphs_in_use; /* 1: the last step chunk was replayed from a captured CUDA graph; 0: the
+                               steps ran as direct cooperative launches (no step yet, or the capture
+                               was refused, after which the ensemble keeps launching directly) */
+    uint64_t steps_done;
+    uint64_t kernel_launches;
+    uint64_t total_agents;
+    uint64_t total_cells;
+    uint32_t grid_blocks;   /* blocks of the persistent launch (a multiple of the SM count) */
+    uint32_t strip_rows;    /* trail rows per strip work item (autotuned) */
+} SlimeEnsembleInfo;
+int slime_ensemble_get_info(const slime_ensemble* ens, SlimeEnsembleInfo* out);
 /* Failure-detection self-test: runs one block at the ensemble's grid barrier
  * sized for two, so the release never comes; the bounded wait gives up after
  * ~0.1 s.  Returns SLIME_ERR_DEVICE_TIMEOUT when the timeout was detected and

@@ -40,8 +40,13 @@
 
 #if defined(__CUDACC__)
 #define SLM_FN static __host__ __device__ __forceinline__
+/* Rarely taken paths (huge or non-finite arguments, remainders outside one
+ * period) are compiled once, out of line, so that the kernels' hot loops stay
+ * small enough for the instruction cache. */
+#define SLM_COLD_FN static __host__ __device__ __noinline__
 #else
 #define SLM_FN static inline
+#define SLM_COLD_FN static
 #endif
 
 /* BEGIN GENERATED CONSTANTS (include/gen_slime_math_constants.py) */
@@ -152,6 +157,9 @@ SLM_FN float slm_fract(float x) { return slm_sub(x, slm_floor(x)); }
 SLM_FN float slm_mix(float a, float b, float t) {
     return slm_add(slm_mul(a, slm_sub(1.0f, t)), slm_mul(b, t));
 }
+/* fmodf, out of line: exact on every conforming implementation. */
+SLM_COLD_FN float slm_fmod_exact(float x, float y) { return fmodf(x, y); }
+
 /* The f32 `%` operator: remainder with the sign of the dividend.  fmodf is
  * exact on every conforming implementation, so host and device agree. */
 SLM_FN float slm_fmod(float x, float y) {
@@ -163,7 +171,7 @@ SLM_FN float slm_fmod(float x, float y) {
     int in0 = slm_abs(x) < y;
     int in1 = (x >= y) && (x < y2);
     int in2 = (x <= -y) && (x > -y2);
-    if (!(y > 0.0f) || !(in0 || in1 || in2)) return fmodf(x, y);
+    if (!(y > 0.0f) || !(in0 || in1 || in2)) return slm_fmod_exact(x, y);
     float r1 = slm_sub(x, y);
     float r2 = slm_add(x, y);
     r2 = (r2 == 0.0f) ? -0.0f : r2;
@@ -216,12 +224,79 @@ SLM_FN uint32_t slm_funnel_l(uint32_t lo, uint32_t hi, int d) {
 #endif
 }
 
+/* High 32 bits of a 32x32-bit product. */
+SLM_FN uint32_t slm_umulhi(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+/* Leading zero bits of a nonzero 32-bit value. */
+SLM_FN int slm_clz32(uint32_t a) {
+#if defined(__CUDA_ARCH__)
+    return __clz((int)a);
+#else
+    return __builtin_clz(a);
+#endif
+}
+
 /* Second half of the Payne-Hanek reduction: from the mantissa m of |x|
  * (2^23 <= m < 2^24), the 96 bits w0:w1:w2 of 2/pi that follow the bits
  * dropped as multiples of 4, and the sign of x, the reduced argument and the
- * quadrant. */
+ * quadrant.  Written in 32-bit words (the products' low and high halves,
+ * add-with-carry, funnel shifts, one 32-bit leading-zero count); the same bits
+ * as the 64-bit statement slm_ph_finish_u64 below for every input, which the
+ * oracle's self-test checks over every binary32 with |x| >= 4096. */
 SLM_FN void slm_ph_finish(uint32_t m, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t sign, float* r_out,
                           int* q_out) {
+    /* Q = m * (w0:w1:w2), a 120-bit integer; |x| * 2/pi = Q * 2^-94 (mod 4).
+     * Its low word is limb0, then limb1, then c_lo (bits 64..95); the bits
+     * above do not matter (multiples of 4 after the scaling). */
+    const uint32_t limb0 = m * w2;
+    const uint32_t p2hi = slm_umulhi(m, w2);
+    const uint32_t p1lo = m * w1;
+    const uint32_t limb1 = p1lo + p2hi;
+    const uint32_t b_hi = slm_umulhi(m, w1) + (limb1 < p1lo ? 1u : 0u);
+    const uint32_t c_lo = m * w0 + b_hi;
+    const uint32_t ipart = c_lo >> 30;
+    /* the 64-bit fraction (bits 29..0 of c_lo, limb1, top 2 bits of limb0) */
+    const uint32_t f_hi = slm_funnel_l(limb1, c_lo, 2);
+    const uint32_t f_lo = slm_funnel_l(limb0, limb1, 2);
+    /* Round to the nearest quadrant: a fraction >= 1/2 becomes negative. */
+    const uint32_t neg = f_hi >> 31;
+    uint32_t q = (ipart + neg) & 3u;
+    const uint32_t mask = 0u - neg;
+    const uint32_t a_lo = (f_lo ^ mask) + neg;
+    const uint32_t a_hi = (f_hi ^ mask) + (a_lo < neg ? 1u : 0u); /* |fraction| * 2^64 */
+    float r = 0.0f;
+    if ((a_hi | a_lo) != 0u) {
+        /* the top 32 bits of the normalised fraction, and its leading zeros */
+        const uint32_t h = a_hi ? a_hi : a_lo;
+        const uint32_t l = a_hi ? a_lo : 0u;
+        const int lzh = slm_clz32(h);
+        const int lz = lzh + (a_hi ? 0 : 32);
+        const uint32_t t = slm_funnel_l(l, h, lzh) >> 2; /* in [2^29, 2^30) */
+        float hi = (float)(int32_t)t;
+        float lo = (float)((int32_t)t - (int32_t)hi);
+        float scale = slm_u2f_bits((uint32_t)(127 - 30 - lz) << 23); /* 2^(-30-lz) */
+        float rh = slm_mul(hi, scale);
+        float rl = slm_mul(lo, scale);
+        r = slm_fma(rh, SLM_PIO2_1, slm_fma(rh, SLM_PIO2_2, slm_mul(rl, SLM_PIO2_1)));
+        if (neg) r = -r;
+    }
+    if (sign) {
+        r = -r;
+        q = (4u - q) & 3u;
+    }
+    *r_out = r;
+    *q_out = (int)q;
+}
+
+/* The same in 64-bit integer arithmetic (the statement slm_ph_finish was
+ * derived from; kept for the self-test). */
+SLM_FN void slm_ph_finish_u64(uint32_t m, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t sign, float* r_out,
+                              int* q_out) {
     /* Q = m * (w0:w1:w2), a 120-bit integer; |x| * 2/pi = Q * 2^-94 (mod 4). */
     uint64_t p2 = (uint64_t)m * w2;
     uint64_t p1 = (uint64_t)m * w1;
@@ -257,6 +332,24 @@ SLM_FN void slm_ph_finish(uint32_t m, uint32_t w0, uint32_t w1, uint32_t w2, uin
     }
     *r_out = r;
     *q_out = (int)q;
+}
+
+/* The mantissa of finite |x| >= 4096 and the 96-bit window of 2/pi that
+ * slm_reduce_pio2_ph multiplies it by, from the table. */
+SLM_FN void slm_ph_window_table(float x, uint32_t* m_out, uint32_t* w) {
+    uint32_t ix = slm_f2u_bits(x);
+    uint32_t E = (ix >> 23) & 0xffu;
+    int u = (int)E - 150 - 2 + 32;
+#if defined(__CUDA_ARCH__)
+    const uint32_t* T = slm_two_over_pi_dev;
+#else
+    const uint32_t* T = slm_two_over_pi_host;
+#endif
+    int wi = u >> 5;
+    int sh = u & 31;
+    for (int k = 0; k < 3; k++)
+        w[k] = (uint32_t)(((((uint64_t)T[wi + k]) << 32) | T[wi + k + 1]) >> (32 - sh));
+    *m_out = (ix & 0x7fffffu) | 0x800000u;
 }
 
 /* Payne-Hanek for finite |x| >= 4096, window read from the table of 2/pi. */
@@ -300,40 +393,82 @@ SLM_FN void slm_reduce_pio2_win(float x, float* r_out, int* q_out) {
     slm_ph_finish(m, w0, w1, w2, ix >> 31, r_out, q_out);
 }
 
-/* Reduce x to r in about [-pi/4, pi/4] and quadrant q in 0..3 with
- * x = (4k + q) * pi/2 + r. */
-SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
-    if (slm_abs(x) < 4096.0f) {
-        /* Cody-Waite.  j = rint(x * 2/pi) by adding and removing 1.5 * 2^23
-         * (exact round-to-nearest-even for |j| < 2^22); the low bits of the
-         * biased sum are j mod 4.  SLM_PIO2_1 has its last bit at 2^-23, so
-         * the first fma is exact for every |x| < 4096; the two later parts
-         * restore the lost bits. */
-        float biased = slm_add(slm_mul(x, SLM_TWO_OVER_PI_F), 12582912.0f);
-        float j = slm_sub(biased, 12582912.0f);
-        float r = slm_fma(-j, SLM_PIO2_1, x);
-        r = slm_fma(-j, SLM_PIO2_2, r);
-        r = slm_fma(-j, SLM_PIO2_3, r);
-        *r_out = r;
-        *q_out = (int)(slm_f2u_bits(biased) & 3u);
-        return;
-    }
-    uint32_t E = (slm_f2u_bits(x) >> 23) & 0xffu;
-    if (E == 0xffu) { /* inf or NaN */
-        *r_out = slm_sub(x, x);
-        *q_out = 0;
-        return;
-    }
-    if (E <= 170u)
-        slm_reduce_pio2_win(x, r_out, q_out);
-    else
-        slm_reduce_pio2_ph(x, r_out, q_out);
-}
-
-SLM_FN void slm_sincos(float x, float* s_out, float* c_out) {
+/* Reduced argument and quadrant. */
+typedef struct SlmRQ {
     float r;
     int q;
-    slm_reduce_pio2(x, &r, &q);
+} SlmRQ;
+
+/* Cody-Waite for |x| < 4096.  j = rint(x * 2/pi) by adding and removing
+ * 1.5 * 2^23 (exact round-to-nearest-even for |j| < 2^22); the low bits of
+ * the biased sum are j mod 4.  SLM_PIO2_1 has its last bit at 2^-23, so the
+ * first fma is exact for every |x| < 4096; the two later parts restore the
+ * lost bits. */
+SLM_FN SlmRQ slm_reduce_pio2_cw(float x) {
+    float biased = slm_add(slm_mul(x, SLM_TWO_OVER_PI_F), 12582912.0f);
+    float j = slm_sub(biased, 12582912.0f);
+    float r = slm_fma(-j, SLM_PIO2_1, x);
+    r = slm_fma(-j, SLM_PIO2_2, r);
+    r = slm_fma(-j, SLM_PIO2_3, r);
+    SlmRQ o;
+    o.r = r;
+    o.q = (int)(slm_f2u_bits(biased) & 3u);
+    return o;
+}
+
+/* |x| >= 4096, inf or NaN. */
+SLM_FN SlmRQ slm_reduce_pio2_large(float x) {
+    SlmRQ o;
+    uint32_t E = (slm_f2u_bits(x) >> 23) & 0xffu;
+    if (E == 0xffu) { /* inf or NaN */
+        o.r = slm_sub(x, x);
+        o.q = 0;
+    } else if (E <= 170u) {
+        slm_reduce_pio2_win(x, &o.r, &o.q);
+    } else {
+        slm_reduce_pio2_ph(x, &o.r, &o.q);
+    }
+    return o;
+}
+SLM_COLD_FN SlmRQ slm_reduce_pio2_large_cold(float x) { return slm_reduce_pio2_large(x); }
+SLM_COLD_FN SlmRQ slm_reduce_pio2_cw_cold(float x) { return slm_reduce_pio2_cw(x); }
+
+/* Reduce x to r in about [-pi/4, pi/4] and quadrant q in 0..3 with
+ * x = (4k + q) * pi/2 + r: Cody-Waite inline for |x| < 4096 (every heading
+ * the shader produces), the rest out of line. */
+SLM_FN void slm_reduce_pio2(float x, float* r_out, int* q_out) {
+    SlmRQ o = slm_abs(x) < 4096.0f ? slm_reduce_pio2_cw(x) : slm_reduce_pio2_large_cold(x);
+    *r_out = o.r;
+    *q_out = o.q;
+}
+
+/* The same split for arguments that are mostly in 4096 <= |x| < 2^44 (the
+ * jitter hash's, whose agent-index term alone exceeds 4096 for every index
+ * above 315): the fixed-window Payne-Hanek inline, the rest out of line.
+ * The same bits as slm_reduce_pio2 for every x. */
+SLM_FN void slm_reduce_pio2_hash(float x, float* r_out, int* q_out) {
+    const uint32_t E = (slm_f2u_bits(x) >> 23) & 0xffu;
+    SlmRQ o;
+    if (E >= 139u && E <= 170u) {
+        slm_reduce_pio2_win(x, &o.r, &o.q);
+    } else {
+        o = slm_abs(x) < 4096.0f ? slm_reduce_pio2_cw_cold(x) : slm_reduce_pio2_large_cold(x);
+    }
+    *r_out = o.r;
+    *q_out = o.q;
+}
+
+/* The quadrant step of slm_sincos: (sin, cos) from the polynomials s, c and
+ * the quadrant q. */
+SLM_FN void slm_sincos_quadrant(float s, float c, int q, float* s_out, float* c_out) {
+    float a = (q & 1) ? c : s;
+    float bb = (q & 1) ? s : c;
+    *s_out = (q & 2) ? -a : a;
+    *c_out = ((q + 1) & 2) ? -bb : bb;
+}
+
+/* sin and cos from the reduced argument r and the quadrant q. */
+SLM_FN void slm_sincos_rq(float r, int q, float* s_out, float* c_out) {
     float z = slm_mul(r, r);
     float ps = slm_fma(z, SLM_S4, SLM_S3);
     ps = slm_fma(z, ps, SLM_S2);
@@ -345,10 +480,14 @@ SLM_FN void slm_sincos(float x, float* s_out, float* c_out) {
     pc = slm_fma(z, pc, SLM_C1);
     float c = slm_fma(z, pc, 1.0f);
     /* quadrant q: (sin, cos) = (s, c), (c, -s), (-s, -c), (-c, s) */
-    float a = (q & 1) ? c : s;
-    float bb = (q & 1) ? s : c;
-    *s_out = (q & 2) ? -a : a;
-    *c_out = ((q + 1) & 2) ? -bb : bb;
+    slm_sincos_quadrant(s, c, q, s_out, c_out);
+}
+
+SLM_FN void slm_sincos(float x, float* s_out, float* c_out) {
+    float r;
+    int q;
+    slm_reduce_pio2(x, &r, &q);
+    slm_sincos_rq(r, q, s_out, c_out);
 }
 
 SLM_FN float slm_sin(float x) { float s, c; slm_sincos(x, &s, &c); return s; }
@@ -382,28 +521,89 @@ SLM_FN uint32_t slm_dispatch_visits(uint64_t n, uint64_t index) {
     return slm_dispatch_visits_in((uint32_t)index, wy, span);
 }
 
-/* Sensor directions of compute.wgsl:75-90 as the shader writes them: the
- * sensor angles angle - a and angle + a are binary32 differences and sums
- * (:75-76), and each of the three directions is slm_sincos of its own angle. */
-SLM_FN void slm_sensor_dirs_shader(float angle, float a, float* cl, float* sl, float* cc, float* sc, float* cr,
-                                   float* sr) {
-    slm_sincos(slm_sub(angle, a), sl, cl);
-    slm_sincos(slm_add(angle, a), sr, cr);
-    slm_sincos(angle, sc, cc);
+#if defined(__CUDACC__)
+/* slm_sincos of two arguments with |x0|, |x1| < 4096 at once, bit for bit.
+ * Each lane's reduction starts with a binary32 product and sum (a packed
+ * product followed by a packed sum may be contracted into one fused
+ * operation, which would round once instead of twice, so these stay
+ * scalar); every later step is a fused multiply-add, or a product that feeds
+ * one as a multiplicand, evaluated for both lanes by one packed instruction
+ * (fma.rn.f32x2, mul.rn.f32x2: each lane rounded as its scalar form). */
+static __device__ __forceinline__ void slm_sincos2_cw(float x0, float x1, float* s0, float* c0, float* s1,
+                                                      float* c1) {
+    const float b0 = slm_add(slm_mul(x0, SLM_TWO_OVER_PI_F), 12582912.0f);
+    const float b1 = slm_add(slm_mul(x1, SLM_TWO_OVER_PI_F), 12582912.0f);
+    /* -j, exactly: 1.5 * 2^23 - biased */
+    const float2 nj = make_float2(slm_sub(12582912.0f, b0), slm_sub(12582912.0f, b1));
+    float2 r = __ffma2_rn(nj, make_float2(SLM_PIO2_1, SLM_PIO2_1), make_float2(x0, x1));
+    r = __ffma2_rn(nj, make_float2(SLM_PIO2_2, SLM_PIO2_2), r);
+    r = __ffma2_rn(nj, make_float2(SLM_PIO2_3, SLM_PIO2_3), r);
+    const float2 z = __fmul2_rn(r, r);
+    float2 ps = __ffma2_rn(z, make_float2(SLM_S4, SLM_S4), make_float2(SLM_S3, SLM_S3));
+    ps = __ffma2_rn(z, ps, make_float2(SLM_S2, SLM_S2));
+    ps = __ffma2_rn(z, ps, make_float2(SLM_S1, SLM_S1));
+    const float2 s = __ffma2_rn(__fmul2_rn(r, z), ps, r);
+    float2 pc = __ffma2_rn(z, make_float2(SLM_C5, SLM_C5), make_float2(SLM_C4, SLM_C4));
+    pc = __ffma2_rn(z, pc, make_float2(SLM_C3, SLM_C3));
+    pc = __ffma2_rn(z, pc, make_float2(SLM_C2, SLM_C2));
+    pc = __ffma2_rn(z, pc, make_float2(SLM_C1, SLM_C1));
+    const float2 c = __ffma2_rn(z, pc, make_float2(1.0f, 1.0f));
+    slm_sincos_quadrant(s.x, c.x, (int)(slm_f2u_bits(b0) & 3u), s0, c0);
+    slm_sincos_quadrant(s.y, c.y, (int)(slm_f2u_bits(b1) & 3u), s1, c1);
 }
 
-/* The rotated form (SLIME_SENSOR_ROTATED): the centre direction is
+/* Two general slm_sincos evaluations, out of line. */
+typedef struct SlmSinCos2 {
+    float s0, c0, s1, c1;
+} SlmSinCos2;
+static __device__ __noinline__ SlmSinCos2 slm_sincos2_cold(float x0, float x1) {
+    SlmSinCos2 o;
+    slm_sincos(x0, &o.s0, &o.c0);
+    slm_sincos(x1, &o.s1, &o.c1);
+    return o;
+}
+
+/* slm_sincos of two arguments, bit for bit: the packed pair when both are
+ * below 4096 in magnitude, the general form out of line otherwise. */
+static __device__ __forceinline__ void slm_sincos2(float x0, float x1, float* s0, float* c0, float* s1, float* c1) {
+    if (slm_abs(x0) < 4096.0f && slm_abs(x1) < 4096.0f) {
+        slm_sincos2_cw(x0, x1, s0, c0, s1, c1);
+    } else {
+        const SlmSinCos2 o = slm_sincos2_cold(x0, x1);
+        *s0 = o.s0;
+        *c0 = o.c0;
+        *s1 = o.s1;
+        *c1 = o.c1;
+    }
+}
+
+/* slm_sincos_rq of two reduced arguments: the polynomials as packed fused
+ * multiply-adds (products only as their multiplicands), the same bits. */
+static __device__ __forceinline__ void slm_sincos_rq2(float r0, int q0, float r1, int q1, float* s0, float* c0,
+                                                      float* s1, float* c1) {
+    const float2 r = make_float2(r0, r1);
+    const float2 z = __fmul2_rn(r, r);
+    float2 ps = __ffma2_rn(z, make_float2(SLM_S4, SLM_S4), make_float2(SLM_S3, SLM_S3));
+    ps = __ffma2_rn(z, ps, make_float2(SLM_S2, SLM_S2));
+    ps = __ffma2_rn(z, ps, make_float2(SLM_S1, SLM_S1));
+    const float2 s = __ffma2_rn(__fmul2_rn(r, z), ps, r);
+    float2 pc = __ffma2_rn(z, make_float2(SLM_C5, SLM_C5), make_float2(SLM_C4, SLM_C4));
+    pc = __ffma2_rn(z, pc, make_float2(SLM_C3, SLM_C3));
+    pc = __ffma2_rn(z, pc, make_float2(SLM_C2, SLM_C2));
+    pc = __ffma2_rn(z, pc, make_float2(SLM_C1, SLM_C1));
+    const float2 c = __ffma2_rn(z, pc, make_float2(1.0f, 1.0f));
+    slm_sincos_quadrant(s.x, c.x, q0, s0, c0);
+    slm_sincos_quadrant(s.y, c.y, q1, s1, c1);
+}
+#endif
+
+/* The rotated form (SLIME_SENSOR_ROTATED): the centre direction (c, s) =
  * slm_sincos(angle); the side directions are that vector rotated by -a and +a
  * with (sin a, cos a) = slm_sincos(sensor_angle), a fixed sequence of
  * binary32 products and fused multiply-adds.  Within a few 1e-8 of cos/sin of
  * the rounded angle -/+ a, but not equal to it: near-ties of the turn
  * decision can go the other way than the shader's. */
-SLM_FN void slm_sensor_dirs(float angle, float sa, float ca, float* cl, float* sl, float* cc, float* sc, float* cr,
-                            float* sr) {
-    float s, c;
-    slm_sincos(angle, &s, &c);
-    *cc = c;
-    *sc = s;
+SLM_FN void slm_rotate_dirs(float c, float s, float sa, float ca, float* cl, float* sl, float* cr, float* sr) {
     /* rotate (c, s) by -a: (c ca + s sa, s ca - c sa); by +a: (c ca - s sa, s ca + c sa) */
     float cca = slm_mul(c, ca), sca = slm_mul(s, ca);
     *cl = slm_fma(s, sa, cca);
@@ -411,16 +611,68 @@ SLM_FN void slm_sensor_dirs(float angle, float sa, float ca, float* cl, float* s
     *cr = slm_fma(-s, sa, cca);
     *sr = slm_fma(c, sa, sca);
 }
+SLM_FN void slm_sensor_dirs(float angle, float sa, float ca, float* cl, float* sl, float* cc, float* sc, float* cr,
+                            float* sr) {
+    float s, c;
+    slm_sincos(angle, &s, &c);
+    *cc = c;
+    *sc = s;
+    slm_rotate_dirs(c, s, sa, ca, cl, sl, cr, sr);
+}
+
+/* The two side directions alone, in the shader's form (the first half of
+ * slm_sensor_dirs_shader). */
+SLM_FN void slm_side_dirs_shader(float angle, float a, float* cl, float* sl, float* cr, float* sr) {
+    const float xl = slm_sub(angle, a), xr = slm_add(angle, a);
+#if defined(__CUDA_ARCH__)
+    slm_sincos2(xl, xr, sl, cl, sr, cr);
+#else
+    slm_sincos(xl, sl, cl);
+    slm_sincos(xr, sr, cr);
+#endif
+}
+
+/* Sensor directions of compute.wgsl:75-90 as the shader writes them: the
+ * sensor angles angle - a and angle + a are binary32 differences and sums
+ * (:75-76), and each of the three directions is slm_sincos of its own angle.
+ * On the device the two side directions are evaluated as one packed pair
+ * when both angles are below 4096 in magnitude (every heading the shader
+ * produces), with the same bits. */
+SLM_FN void slm_sensor_dirs_shader(float angle, float a, float* cl, float* sl, float* cc, float* sc, float* cr,
+                                   float* sr) {
+    slm_side_dirs_shader(angle, a, cl, sl, cr, sr);
+    slm_sincos(angle, sc, cc);
+}
 
 /* The shader's per-agent jitter hash (compute.wgsl:117):
  *   fract(sin(f32(agent_index) * 12.9898 + x * 78.233 + y * 37.719) * 43758.5453)
  * evaluated left to right, unfused. */
-SLM_FN float slm_jitter_hash(int32_t agent_index, float x, float y) {
+SLM_FN float slm_jitter_arg(int32_t agent_index, float x, float y) {
     float a = slm_mul(slm_i2f(agent_index), 12.9898f);
     a = slm_add(a, slm_mul(x, 78.233f));
-    a = slm_add(a, slm_mul(y, 37.719f));
-    return slm_fract(slm_mul(slm_sin(a), 43758.5453f));
+    return slm_add(a, slm_mul(y, 37.719f));
 }
+SLM_FN float slm_jitter_hash(int32_t agent_index, float x, float y) {
+    float r, s, c;
+    int q;
+    slm_reduce_pio2_hash(slm_jitter_arg(agent_index, x, y), &r, &q);
+    slm_sincos_rq(r, q, &s, &c);
+    return slm_fract(slm_mul(s, 43758.5453f));
+}
+#if defined(__CUDACC__)
+/* Two jitter hashes, their sin polynomials as one packed pair; the same
+ * bits as slm_jitter_hash for each. */
+static __device__ __forceinline__ void slm_jitter_hash2(int32_t i0, float x0, float y0, int32_t i1, float x1,
+                                                        float y1, float* h0, float* h1) {
+    float r0, r1, s0, c0, s1, c1;
+    int q0, q1;
+    slm_reduce_pio2_hash(slm_jitter_arg(i0, x0, y0), &r0, &q0);
+    slm_reduce_pio2_hash(slm_jitter_arg(i1, x1, y1), &r1, &q1);
+    slm_sincos_rq2(r0, q0, r1, q1, &s0, &c0, &s1, &c1);
+    *h0 = slm_fract(slm_mul(s0, 43758.5453f));
+    *h1 = slm_fract(slm_mul(s1, 43758.5453f));
+}
+#endif
 
 /* Counter-based generator for seeded initial agent states: SplitMix64
  * (G. Steele, D. Lea, C. Flood, "Fast splittable pseudorandom number

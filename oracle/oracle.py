@@ -58,6 +58,8 @@ def lib():
         L.oracle_dispatch_visits.argtypes = [C.c_uint64, C.POINTER(C.c_uint64), C.c_uint64, u32]
         L.oracle_dispatch_visits.restype = None
         L.oracle_ph_window_mismatches.restype = C.c_uint64
+        L.oracle_ph_finish_mismatches.argtypes = [C.c_uint32, C.c_uint32]
+        L.oracle_ph_finish_mismatches.restype = C.c_uint64
         L.oracle_jitter_hash.argtypes = [C.POINTER(C.c_int32), f32, f32, C.c_uint64, f32]
         L.oracle_uniform01.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, f32]
         L.oracle_gauss_weights.argtypes = [C.c_float, C.c_float, f32]
@@ -177,6 +179,12 @@ def ph_window_mismatches(e_lo=139, e_hi=170):
     """Inputs with biased exponent e_lo..e_hi on which the fixed-window and the
     table-driven Payne-Hanek reductions disagree (0 expected)."""
     return int(lib().oracle_ph_window_mismatches(e_lo, e_hi))
+
+
+def ph_finish_mismatches(e_lo=139, e_hi=254):
+    """Inputs with biased exponent e_lo..e_hi on which the 32-bit-word
+    Payne-Hanek tail and its 64-bit statement disagree (0 expected)."""
+    return int(lib().oracle_ph_finish_mismatches(e_lo, e_hi))
 
 
 def sincos(x):

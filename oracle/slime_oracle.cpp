@@ -608,6 +608,29 @@ uint64_t oracle_ph_window_mismatches(uint32_t e_lo, uint32_t e_hi) {
     }
     return bad;
 }
+/* Number of binary32 inputs with biased exponent in [e_lo, e_hi] (both signs)
+ * on which the 32-bit-word Payne-Hanek tail (slm_ph_finish) differs from its
+ * 64-bit statement (slm_ph_finish_u64), both fed the table's window;
+ * 139 <= e_lo <= e_hi <= 254. */
+uint64_t oracle_ph_finish_mismatches(uint32_t e_lo, uint32_t e_hi) {
+    if (e_lo < 139 || e_hi > 254 || e_lo > e_hi) return ~0ull;
+    const int64_t per_sign = (int64_t)(e_hi - e_lo + 1) << 23;
+    uint64_t bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+    for (int64_t i = 0; i < 2 * per_sign; i++) {
+        uint32_t sign = i >= per_sign ? 1u : 0u;
+        uint32_t rem = (uint32_t)(i - (sign ? per_sign : 0));
+        uint32_t bits = (sign << 31) | ((e_lo + (rem >> 23)) << 23) | (rem & 0x7fffffu);
+        uint32_t m, w[3];
+        slm_ph_window_table(slm_u2f_bits(bits), &m, w);
+        float r1, r2;
+        int q1, q2;
+        slm_ph_finish(m, w[0], w[1], w[2], sign, &r1, &q1);
+        slm_ph_finish_u64(m, w[0], w[1], w[2], sign, &r2, &q2);
+        bad += (slm_f2u_bits(r1) != slm_f2u_bits(r2) || q1 != q2) ? 1u : 0u;
+    }
+    return bad;
+}
 int oracle_gauss_weights(float radius, float sigma, float* w) {
     int R = slm_gauss_radius(radius, SLIME_MAX_BLUR_RADIUS);
     if (slm_gauss_weights(R, sigma, w) != 0) return -1;

@@ -23,15 +23,20 @@ namespace slime {
 // (x0 + 1, y0 + 1) selects texels x0..x0+1, y0..y0+1, returned as
 // w = (x0, y0), z = (x0+1, y0), x = (x0, y0+1), y = (x0+1, y0+1).  An
 // out-of-grid sample gathers at (1, 1) (always inside a trail of at least
-// 2x2) and is discarded.
+// 2x2) and is discarded.  The in-grid test needs no integer x0: with
+// fx = floor(px), 0 <= i32(fx) < W - 1 holds exactly when
+// !(fx < 0) && !(fx >= W - 1) for every fx, NaN included (i32(NaN) = 0 is
+// in the grid, and NaN fails both compares), on trails at least 2 wide and
+// high, the only ones that have a texture.
 struct TrailPtr {
     const float* __restrict__ t;
     struct Tap {
         float v00, v10, v01, v11, dx, dy;
         bool ok;
     };
-    __device__ __forceinline__ Tap fetch(int W, int H, float px, float py) const {
+    __device__ __forceinline__ Tap fetch(const DevParams& p, float px, float py) const {
         Tap k;
+        const int W = p.W, H = p.H;
         float fx = floorf(px), fy = floorf(py);
         int x0 = slm_f2i(fx);
         int y0 = slm_f2i(fy);
@@ -51,8 +56,8 @@ struct TrailPtr {
         float v1 = slm_mix(k.v01, k.v11, k.dx);
         return k.ok ? slm_mix(v0, v1, k.dy) : 0.0f;
     }
-    __device__ __forceinline__ float operator()(int W, int H, float px, float py) const {
-        return value(fetch(W, H, px, py));
+    __device__ __forceinline__ float operator()(const DevParams& p, float px, float py) const {
+        return value(fetch(p, px, py));
     }
 };
 struct TrailTex {
@@ -62,12 +67,10 @@ struct TrailTex {
         float dx, dy;
         bool ok;
     };
-    __device__ __forceinline__ Tap fetch(int W, int H, float px, float py) const {
+    __device__ __forceinline__ Tap fetch(const DevParams& p, float px, float py) const {
         Tap k;
         float fx = floorf(px), fy = floorf(py);
-        int x0 = slm_f2i(fx);
-        int y0 = slm_f2i(fy);
-        k.ok = (unsigned)x0 < (unsigned)(W - 1) && (unsigned)y0 < (unsigned)(H - 1);
+        k.ok = !(fx < 0.0f) && !(fx >= p.Wm1f) && !(fy < 0.0f) && !(fy >= p.Hm1f);
         k.dx = slm_sub(px, fx);
         k.dy = slm_sub(py, fy);
         // in range, f32(x0 + 1) == floor(px) + 1 exactly (|x0| < 2^24); a NaN
@@ -81,8 +84,8 @@ struct TrailTex {
         float v1 = slm_mix(k.g.x, k.g.y, k.dx);
         return k.ok ? slm_mix(v0, v1, k.dy) : 0.0f;
     }
-    __device__ __forceinline__ float operator()(int W, int H, float px, float py) const {
-        return value(fetch(W, H, px, py));
+    __device__ __forceinline__ float operator()(const DevParams& p, float px, float py) const {
+        return value(fetch(p, px, py));
     }
 };
 
@@ -104,17 +107,17 @@ __device__ __forceinline__ Senses<Trail> agent_sense(const DevParams& p, float x
     else
         slm_sensor_dirs_shader(angle, p.sensor_angle, &cl, &sl, &cc, &sc, &cr, &sr);
     Senses<Trail> s;
-    s.left = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cl)), slm_add(y, slm_mul(p.sensor_dist, sl)));
-    s.right = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cr)), slm_add(y, slm_mul(p.sensor_dist, sr)));
-    s.center = trail.fetch(p.W, p.H, slm_add(x, slm_mul(p.sensor_dist, cc)), slm_add(y, slm_mul(p.sensor_dist, sc)));
+    s.left = trail.fetch(p, slm_add(x, slm_mul(p.sensor_dist, cl)), slm_add(y, slm_mul(p.sensor_dist, sl)));
+    s.right = trail.fetch(p, slm_add(x, slm_mul(p.sensor_dist, cr)), slm_add(y, slm_mul(p.sensor_dist, sr)));
+    s.center = trail.fetch(p, slm_add(x, slm_mul(p.sensor_dist, cc)), slm_add(y, slm_mul(p.sensor_dist, sc)));
     return s;
 }
 
-// The rest of the agent (compute.wgsl:72 and 98-144) once its sensor samples
-// and its jitter hash `rv` (slm_jitter_hash of its index and pre-move x, y,
-// :117) are known.  Returns the deposit cell or -1.
-__device__ __forceinline__ int agent_finish(const DevParams& p, float& x, float& y, float& angle, float& speed,
-                                            float rv, float left, float right, float center) {
+// compute.wgsl:72 and 98-122: the speed clamp, the turn from the sensor
+// samples, the jitter from the hash `rv` (slm_jitter_hash of the agent's
+// index and pre-move x, y, :117) and the heading's wrap.
+__device__ __forceinline__ void agent_turn(const DevParams& p, float& angle, float& speed, float rv, float left,
+                                           float right, float center) {
     speed = slm_clamp(speed, p.speed_min, p.speed_max);
 
     // compute.wgsl:98-112: keep straight, or turn toward target = angle -/+ TAU
@@ -127,10 +130,12 @@ __device__ __forceinline__ int agent_finish(const DevParams& p, float& x, float&
 
     angle = slm_add(angle, slm_mul(slm_sub(slm_mul(rv, 2.0f), 1.0f), p.jitter));
     angle = slm_wrap(angle, SLM_WGSL_TWO_PI);
+}
 
+// compute.wgsl:125-141: the move along (cm, sm) = (cos, sin) of the new
+// heading, the position's wrap and the deposit cell (or -1).
+__device__ __forceinline__ int agent_move(const DevParams& p, float& x, float& y, float speed, float sm, float cm) {
     float move = slm_mul(speed, p.time_step);
-    float sm, cm;
-    slm_sincos(angle, &sm, &cm);
     x = slm_add(x, slm_mul(move, cm));
     y = slm_add(y, slm_mul(move, sm));
     x = slm_wrap(x, p.Wf);
@@ -140,6 +145,16 @@ __device__ __forceinline__ int agent_finish(const DevParams& p, float& x, float&
     int dy = slm_f2i(y);
     if ((unsigned)dx < (unsigned)p.W && (unsigned)dy < (unsigned)p.H) return dy * p.W + dx;
     return -1;
+}
+
+// The rest of the agent (compute.wgsl:72 and 98-144) once its sensor samples
+// and its jitter hash are known.  Returns the deposit cell or -1.
+__device__ __forceinline__ int agent_finish(const DevParams& p, float& x, float& y, float& angle, float& speed,
+                                            float rv, float left, float right, float center) {
+    agent_turn(p, angle, speed, rv, left, right, center);
+    float sm, cm;
+    slm_sincos(angle, &sm, &cm);
+    return agent_move(p, x, y, speed, sm, cm);
 }
 
 // One agent, compute.wgsl:65-144.  Returns the deposit cell or -1.
@@ -156,6 +171,42 @@ __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y
 __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y, float& angle, float& speed,
                                           int32_t index, const float* __restrict__ trail) {
     return agent_step(p, x, y, angle, speed, index, TrailPtr{trail});
+}
+
+// Two agents (a and b) at once: agent_step's arithmetic for each, with the
+// sin/cos polynomials that the two evaluate on different arguments (centre
+// directions, jitter hashes, moves) paired into packed fused multiply-adds,
+// as are each agent's two side directions.  Bit for bit agent_step twice.
+template <class Trail>
+__device__ __forceinline__ void agent_step2(const DevParams& p, float& xa, float& ya, float& tha, float& va,
+                                            int32_t ia, float& xb, float& yb, float& thb, float& vb, int32_t ib,
+                                            const Trail& trail, int& cell_a, int& cell_b) {
+    float sca, cca, scb, ccb;
+    slm_sincos2(tha, thb, &sca, &cca, &scb, &ccb);
+    float cla, sla, cra, sra, clb, slb, crb, srb;
+    if (p.sensor_mode == SLIME_SENSOR_ROTATED) {
+        slm_rotate_dirs(cca, sca, p.sensor_sin, p.sensor_cos, &cla, &sla, &cra, &sra);
+        slm_rotate_dirs(ccb, scb, p.sensor_sin, p.sensor_cos, &clb, &slb, &crb, &srb);
+    } else {
+        slm_side_dirs_shader(tha, p.sensor_angle, &cla, &sla, &cra, &sra);
+        slm_side_dirs_shader(thb, p.sensor_angle, &clb, &slb, &crb, &srb);
+    }
+    const float d = p.sensor_dist;
+    const typename Trail::Tap la = trail.fetch(p, slm_add(xa, slm_mul(d, cla)), slm_add(ya, slm_mul(d, sla)));
+    const typename Trail::Tap ra = trail.fetch(p, slm_add(xa, slm_mul(d, cra)), slm_add(ya, slm_mul(d, sra)));
+    const typename Trail::Tap ca = trail.fetch(p, slm_add(xa, slm_mul(d, cca)), slm_add(ya, slm_mul(d, sca)));
+    const typename Trail::Tap lb = trail.fetch(p, slm_add(xb, slm_mul(d, clb)), slm_add(yb, slm_mul(d, slb)));
+    const typename Trail::Tap rb = trail.fetch(p, slm_add(xb, slm_mul(d, crb)), slm_add(yb, slm_mul(d, srb)));
+    const typename Trail::Tap cb = trail.fetch(p, slm_add(xb, slm_mul(d, ccb)), slm_add(yb, slm_mul(d, scb)));
+    // the hashes need no sample: worked out while the footprints load
+    float rva, rvb;
+    slm_jitter_hash2(ia, xa, ya, ib, xb, yb, &rva, &rvb);
+    agent_turn(p, tha, va, rva, Trail::value(la), Trail::value(ra), Trail::value(ca));
+    agent_turn(p, thb, vb, rvb, Trail::value(lb), Trail::value(rb), Trail::value(cb));
+    float sma, cma, smb, cmb;
+    slm_sincos2(tha, thb, &sma, &cma, &smb, &cmb);
+    cell_a = agent_move(p, xa, ya, va, sma, cma);
+    cell_b = agent_move(p, xb, yb, vb, smb, cmb);
 }
 
 } // namespace slime

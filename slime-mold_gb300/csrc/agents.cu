@@ -74,6 +74,21 @@ __device__ __forceinline__ void deposit(uint32_t* __restrict__ counts, uint8_t* 
         atomicAdd(counts + cell, 1u);
 }
 
+// A full group of APT agents: in pairs (agent_step2) when APT is even.
+template <int APT, class Trail>
+__device__ __forceinline__ void step_group(const DevParams& p, float* x, float* y, float* th, float* v,
+                                           const uint32_t* id, const Trail& trail, int* cell) {
+    if (APT % 2 == 0) {
+#pragma unroll
+        for (int j = 0; j < APT; j += 2)
+            agent_step2(p, x[j], y[j], th[j], v[j], (int32_t)id[j], x[j + 1], y[j + 1], th[j + 1], v[j + 1],
+                        (int32_t)id[j + 1], trail, cell[j], cell[j + 1]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < APT; j++) cell[j] = agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail);
+    }
+}
+
 // A thread moves APT consecutive slots with one vector load/store per field.
 // MINB > 0 asks the compiler to fit MINB blocks per SM (caps registers).
 // Trail is the reader of the sensed trail (TrailPtr or TrailTex).
@@ -105,8 +120,7 @@ __global__ void __launch_bounds__(BS, MINB) agents_kernel(const __grid_constant_
     int cell[APT];
     if (base + APT <= n) {
         // full group: no per-agent branch, so the agents' work can interleave
-#pragma unroll
-        for (int j = 0; j < APT; j++) cell[j] = agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail);
+        step_group<APT>(p, x, y, th, v, id, trail, cell);
     } else {
 #pragma unroll
         for (int j = 0; j < APT; j++)
@@ -219,8 +233,7 @@ __global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
         }
         int cell[APT];
         if (base + APT <= n) {
-#pragma unroll
-            for (int j = 0; j < APT; j++) cell[j] = agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail);
+            step_group<APT>(p, x, y, th, v, id, trail, cell);
         } else {
 #pragma unroll
             for (int j = 0; j < APT; j++)
@@ -316,16 +329,18 @@ cudaError_t launch_agents_variant(const DevParams& p, const AgentsSoA& a, const 
 } // namespace
 
 // Agent-kernel shapes: (agents per thread, threads per block, min blocks/SM).
-// Entries 9..11 are the persistent, prefetching variant; 12..14 sample the
-// trail through its texture (12 regular, 13 and 14 persistent) and run as
-// their pointer twins (1, 9, 11) when the trail has no texture.
+// Entries 9..11 are the persistent, prefetching variant; 12..15 sample the
+// trail through its texture (12 regular, 13-15 persistent; 15 capped at four
+// blocks per SM, i.e. 64 registers) and run on the pointer path when the
+// trail has no texture.
 const AgentShape kAgentShapes[] = {{4, 256, 0}, {2, 256, 0}, {1, 256, 0}, {4, 128, 0}, {1, 128, 0},
                                    {2, 256, 5}, {2, 256, 6}, {4, 256, 4}, {1, 256, 8}, {2, 256, 0},
-                                   {1, 256, 0}, {2, 128, 0}, {2, 256, 0}, {2, 256, 0}, {2, 128, 0}};
+                                   {1, 256, 0}, {2, 128, 0}, {2, 256, 0}, {2, 256, 0}, {2, 128, 0},
+                                   {2, 256, 4}};
 
 int agent_shape_count() { return (int)(sizeof(kAgentShapes) / sizeof(kAgentShapes[0])); }
 AgentShape agent_shape(int i) { return kAgentShapes[(i >= 0 && i < agent_shape_count()) ? i : 0]; }
-bool agent_shape_uses_texture(int i) { return i >= 12 && i <= 14; }
+bool agent_shape_uses_texture(int i) { return i >= 12 && i <= 15; }
 
 uint64_t reference_dispatch_updated(uint64_t n) {
     if (n == 0) return 0;
@@ -366,6 +381,7 @@ cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* t
         switch (shape) {
         case 12: return launch_agents_variant<2, 256, 0>(p, a, tt, counts, marks, s, win, pdl);
         case 13: return launch_agents_persistent<2, 256, 0>(p, a, tt, counts, marks, s, win, pdl);
+        case 15: return launch_agents_persistent<2, 256, 4>(p, a, tt, counts, marks, s, win, pdl);
         default: return launch_agents_persistent<2, 128, 0>(p, a, tt, counts, marks, s, win, pdl);
         }
     }
@@ -384,6 +400,7 @@ cudaError_t launch_agents(const DevParams& p, const AgentsSoA& a, const float* t
     case 10: return launch_agents_persistent<1, 256, 0>(p, a, tp, counts, marks, s, win, pdl);
     case 11:
     case 14: return launch_agents_persistent<2, 128, 0>(p, a, tp, counts, marks, s, win, pdl);
+    case 15: return launch_agents_persistent<2, 256, 4>(p, a, tp, counts, marks, s, win, pdl);
     default: return launch_agents_variant<4, 256, 0>(p, a, tp, counts, marks, s, win, pdl);
     }
 }

@@ -24,6 +24,7 @@
 #include <string>
 #include <unordered_map>
 #include <utility>
+#include <vector>
 
 #include "ctx.h"
 
@@ -70,6 +71,8 @@ bool make_dev_params(const SlimeParams& p, uint32_t W, uint32_t H, DevParams* ou
     d.H = (int32_t)H;
     d.Wf = (float)W;
     d.Hf = (float)H;
+    d.Wm1f = (float)(W - 1);
+    d.Hm1f = (float)(H - 1);
     d.speed_min = p.agent_speed_min;
     d.speed_max = p.agent_speed_max;
     d.turn = p.agent_turn_speed;
@@ -964,6 +967,92 @@ int slime_set_agent_count(slime_ctx* ctx, uint64_t n, uint64_t seed) {
     ctx->reordered = false;
     // src/main.rs:700-712 draws x, y, angle in [0, 2*pi) and speed anew.
     return slime_seed_agents(ctx, seed, 0.0f, 6.28318530718f);
+}
+
+int slime_set_steps_done(slime_ctx* ctx, uint64_t steps_done) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    ctx->steps_done = steps_done;
+    // no reorder has happened at this count yet: one falls due here when
+    // steps_done is a multiple of reorder_every, as in the run being resumed
+    ctx->last_reorder_step = ~0ull;
+    return SLIME_OK;
+}
+
+namespace {
+constexpr char kStateMagic[8] = {'S', 'L', 'M', 'S', 'T', 'A', 'T', 'E'};
+constexpr uint32_t kStateVersion = 1;
+
+// The fixed-size head of a state file (little-endian on the hosts this
+// library builds for: x86-64 and AArch64).
+struct StateHead {
+    char magic[8];
+    uint32_t version, width, height, params_bytes;
+    uint64_t n_agents, steps_done;
+};
+static_assert(sizeof(StateHead) == 40, "state file head is 40 bytes");
+} // namespace
+
+int slime_state_save(slime_ctx* ctx, const char* path) {
+    if (!ctx || !path) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    const uint64_t n = ctx->agents.n;
+    const size_t cells = (size_t)ctx->W * ctx->H;
+    std::vector<float> agents(4 * n), trail(cells);
+    int rc;
+    if ((rc = slime_download_agents(ctx, agents.data(), n)) != SLIME_OK) return rc;
+    if ((rc = slime_download_trail(ctx, trail.data(), cells)) != SLIME_OK) return rc;
+    StateHead h;
+    memcpy(h.magic, kStateMagic, 8);
+    h.version = kStateVersion;
+    h.width = ctx->W;
+    h.height = ctx->H;
+    h.params_bytes = (uint32_t)sizeof(SlimeParams);
+    h.n_agents = n;
+    h.steps_done = ctx->steps_done;
+    FILE* f = fopen(path, "wb");
+    if (!f) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "cannot open %s for writing", path);
+    bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(&ctx->params, sizeof(SlimeParams), 1, f) == 1 &&
+              fwrite(agents.data(), sizeof(float), agents.size(), f) == agents.size() &&
+              fwrite(trail.data(), sizeof(float), trail.size(), f) == trail.size();
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "writing %s failed", path);
+    return SLIME_OK;
+}
+
+int slime_state_load(slime_ctx* ctx, const char* path) {
+    if (!ctx || !path) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    FILE* f = fopen(path, "rb");
+    if (!f) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "cannot open %s", path);
+    StateHead h;
+    SlimeParams p;
+    const size_t cells = (size_t)ctx->W * ctx->H;
+    std::vector<float> agents, trail;
+    const char* why = nullptr;
+    if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, kStateMagic, 8) != 0) why = "not a state file";
+    else if (h.version != kStateVersion) why = "unknown state file version";
+    else if (h.params_bytes != sizeof(SlimeParams)) why = "state file holds parameters of another layout";
+    else if (h.width != ctx->W || h.height != ctx->H || h.n_agents != ctx->agents.n)
+        why = "state file is of another trail size or agent count";
+    else if (fread(&p, sizeof p, 1, f) != 1) why = "truncated state file";
+    if (!why) {
+        agents.resize(4 * h.n_agents);
+        trail.resize(cells);
+        if (fread(agents.data(), sizeof(float), agents.size(), f) != agents.size() ||
+            fread(trail.data(), sizeof(float), trail.size(), f) != trail.size())
+            why = "truncated state file";
+    }
+    fclose(f);
+    if (why) return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "%s: %s", path, why);
+    DevParams d;
+    const char* bad = nullptr;
+    if (!make_dev_params(p, ctx->W, ctx->H, &d, &bad))
+        return set_error(ctx->err, SLIME_ERR_INVALID_ARGUMENT, "%s: %s", path, bad);
+    int rc;
+    if ((rc = slime_set_params(ctx, &p)) != SLIME_OK) return rc;
+    if ((rc = slime_upload_agents(ctx, agents.data(), h.n_agents)) != SLIME_OK) return rc;
+    if ((rc = slime_upload_trail(ctx, trail.data(), cells)) != SLIME_OK) return rc;
+    return slime_set_steps_done(ctx, h.steps_done);
 }
 
 int slime_step(slime_ctx* ctx, uint32_t n_steps) {

@@ -21,6 +21,7 @@ constexpr int kMaxR = SLIME_MAX_BLUR_RADIUS;
 struct DevParams {
     int32_t W, H;
     float Wf, Hf;
+    float Wm1f, Hm1f; // W - 1 and H - 1 (exact: sides are <= 2^24)
     float speed_min, speed_max;
     float turn;
     float sensor_angle, sensor_dist;

@@ -230,6 +230,7 @@ struct slime_ensemble {
     int grid = 0;
     int blocks_per_sm = 0;
     bool use_graphs = true;
+    bool last_chunk_graph = false; // the last chunk of steps replayed a graph
     std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs;
     uint64_t launches = 0;
     std::string err;
@@ -411,8 +412,10 @@ int run_ens_steps(slime_ensemble* e, uint32_t n) {
             }
             ECK(cudaGraphLaunch(exec, e->stream), "launching ensemble graph");
             if (m & 1) e->cur = 1 - e->cur;
+            e->last_chunk_graph = true;
         } else {
             for (uint32_t i = 0; i < m; i++) ECK(enqueue_ens_step(e), "launching ensemble step");
+            e->last_chunk_graph = false;
         }
         e->launches += m;
         e->steps_done += m;
@@ -801,6 +804,22 @@ int slime_ensemble_selftest_barrier_timeout(slime_ensemble* e) {
 int slime_ensemble_launch_count(const slime_ensemble* e, uint64_t* out) {
     if (!e || !out) return SLIME_ERR_INVALID_ARGUMENT;
     *out = e->launches;
+    return SLIME_OK;
+}
+
+int slime_ensemble_get_info(const slime_ensemble* e, SlimeEnsembleInfo* out) {
+    if (!e || !out) return SLIME_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    out->n_colonies = (uint32_t)e->colonies.size();
+    out->graphs_in_use = e->last_chunk_graph ? 1u : 0u;
+    out->steps_done = e->steps_done;
+    out->kernel_launches = e->launches;
+    for (const Colony& c : e->colonies) {
+        out->total_agents += c.n;
+        out->total_cells += (uint64_t)c.W * c.H;
+    }
+    out->grid_blocks = (uint32_t)e->grid;
+    out->strip_rows = (uint32_t)e->rows;
     return SLIME_OK;
 }
 

@@ -13,11 +13,12 @@ import numpy as np
 
 from . import _abi
 from ._abi import (BLUR_GAUSS, BLUR_REF_BOX3, DECAY_MULTIPLY, DECAY_REF_SUBTRACT, DISPATCH_EACH_AGENT,
-                   DISPATCH_REFERENCE, MAX_BLUR_RADIUS, SENSOR_ROTATED, SENSOR_SHADER, SlimeGrads,
-                   SlimeInfo, SlimeOptions, SlimeParams, SlimeSettings)
+                   DISPATCH_REFERENCE, MAX_BLUR_RADIUS, SENSOR_ROTATED, SENSOR_SHADER, SlimeEnsembleInfo,
+                   SlimeGrads, SlimeInfo, SlimeOptions, SlimeParams, SlimeSettings)
 
 __all__ = [
     "SlimeError", "Settings", "default_settings", "preset_names", "preset", "params_from_settings",
+    "settings_to_text", "settings_from_text", "save_settings", "load_settings", "SlimeEnsembleInfo",
     "Simulation", "Ensemble", "SlimeParams", "SlimeOptions", "SlimeGrads", "lib",
     "DECAY_REF_SUBTRACT", "DECAY_MULTIPLY", "BLUR_REF_BOX3", "BLUR_GAUSS", "MAX_BLUR_RADIUS",
     "DISPATCH_EACH_AGENT", "DISPATCH_REFERENCE", "SENSOR_SHADER", "SENSOR_ROTATED",
@@ -85,6 +86,37 @@ def params_from_settings(settings, width, height, **overrides):
     for k, v in overrides.items():
         setattr(p, k, v)
     return p
+
+
+def settings_to_text(settings):
+    """The settings as parameter-file text (slime_settings_to_text)."""
+    L = lib()
+    n = C.c_size_t()
+    L.slime_settings_to_text(C.byref(settings), None, 0, C.byref(n))
+    buf = C.create_string_buffer(n.value + 1)
+    if L.slime_settings_to_text(C.byref(settings), buf, n.value + 1, C.byref(n)) != 0:
+        raise SlimeError(_abi.SLIME_ERR_INVALID_ARGUMENT, "settings_to_text failed")
+    return buf.value.decode()
+
+
+def settings_from_text(text):
+    """Settings parsed from parameter-file text; ValueError names the bad line."""
+    s, line = SlimeSettings(), C.c_int()
+    if lib().slime_settings_from_text(text.encode(), C.byref(s), C.byref(line)) != 0:
+        raise ValueError(f"settings text: bad line {line.value}")
+    return s
+
+
+def save_settings(settings, path):
+    if lib().slime_settings_save(C.byref(settings), str(path).encode()) != 0:
+        raise OSError(f"cannot write settings to {path}")
+
+
+def load_settings(path):
+    s, line = SlimeSettings(), C.c_int()
+    if lib().slime_settings_load(str(path).encode(), C.byref(s), C.byref(line)) != 0:
+        raise ValueError(f"{path}: cannot read settings" + (f" (bad line {line.value})" if line.value else ""))
+    return s
 
 
 class Simulation:
@@ -243,23 +275,31 @@ class Simulation:
 
     # -- checkpoint / resume
     def save_state(self, path):
-        """Write agents (id order, AoS), trail, parameters and the step
-        counter to an .npz file."""
-        p = self.params()
-        np.savez(path, agents=self.download_agents(), trail=self.download_trail(),
-                 params=np.frombuffer(bytes(p), dtype=np.uint8), steps_done=np.uint64(self.info().steps_done),
-                 size=np.array([self.width, self.height, self.n_agents], np.uint64))
+        """Write trail size, agent count, step counter, parameters, agents
+        (id order, AoS) and trail to a state file (slime_state_save)."""
+        self._check(self._L.slime_state_save(self._h, str(path).encode()), "save_state")
+
+    def restore_state(self, path):
+        """Load a state file of this simulation's size and agent count into
+        it, step counter included (slime_state_load)."""
+        self._check(self._L.slime_state_load(self._h, str(path).encode()), "load_state")
 
     @classmethod
     def load_state(cls, path):
         """A new Simulation holding the state saved by save_state."""
-        d = np.load(path)
-        W, H, n = (int(v) for v in d["size"])
-        p = SlimeParams.from_buffer_copy(d["params"].tobytes())
-        sim = cls(W, H, n, p)
-        sim.upload_agents(d["agents"])
-        sim.upload_trail(d["trail"])
+        import struct
+        with open(path, "rb") as f:
+            head = f.read(40)
+        if len(head) != 40 or head[:8] != b"SLMSTATE":
+            raise ValueError(f"{path}: not a state file")
+        _, W, H, _ = struct.unpack_from("<4I", head, 8)
+        n, _ = struct.unpack_from("<2Q", head, 24)
+        sim = cls(W, H, n)
+        sim.restore_state(path)
         return sim
+
+    def set_steps_done(self, steps):
+        self._check(self._L.slime_set_steps_done(self._h, steps), "set_steps_done")
 
     # -- adjoint
     def forward_record(self, n_steps, ckpt_every=50):
@@ -387,3 +427,8 @@ class Ensemble:
         v = C.c_uint64()
         self._check(self._L.slime_ensemble_launch_count(self._h, C.byref(v)), "launch_count")
         return v.value
+
+    def info(self):
+        i = SlimeEnsembleInfo()
+        self._check(self._L.slime_ensemble_get_info(self._h, C.byref(i)), "get_info")
+        return i

@@ -117,6 +117,19 @@ class SlimeInfo(C.Structure):
     ]
 
 
+class SlimeEnsembleInfo(C.Structure):
+    _fields_ = [
+        ("n_colonies", C.c_uint32),
+        ("graphs_in_use", C.c_uint32),
+        ("steps_done", C.c_uint64),
+        ("kernel_launches", C.c_uint64),
+        ("total_agents", C.c_uint64),
+        ("total_cells", C.c_uint64),
+        ("grid_blocks", C.c_uint32),
+        ("strip_rows", C.c_uint32),
+    ]
+
+
 class SlimeGrads(C.Structure):
     _fields_ = [
         ("d_decay_factor", C.c_double),
@@ -140,6 +153,10 @@ SIGNATURES = {
     "slime_preset_get": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(SlimeSettings)]),
     "slime_preset_find": (C.c_int, [C.c_char_p, C.POINTER(SlimeSettings)]),
     "slime_params_from_settings": (None, [C.POINTER(SlimeSettings), C.c_uint32, C.c_uint32, C.POINTER(SlimeParams)]),
+    "slime_settings_to_text": (C.c_int, [C.POINTER(SlimeSettings), C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "slime_settings_from_text": (C.c_int, [C.c_char_p, C.POINTER(SlimeSettings), C.POINTER(C.c_int)]),
+    "slime_settings_save": (C.c_int, [C.POINTER(SlimeSettings), C.c_char_p]),
+    "slime_settings_load": (C.c_int, [C.c_char_p, C.POINTER(SlimeSettings), C.POINTER(C.c_int)]),
     "slime_create": (P, [C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(C.c_int)]),
     "slime_destroy": (None, [P]),
     "slime_last_error": (C.c_char_p, [P]),
@@ -157,6 +174,9 @@ SIGNATURES = {
     "slime_clear_trail": (C.c_int, [P]),
     "slime_resize": (C.c_int, [P, C.c_uint32, C.c_uint32]),
     "slime_set_agent_count": (C.c_int, [P, C.c_uint64, C.c_uint64]),
+    "slime_state_save": (C.c_int, [P, C.c_char_p]),
+    "slime_state_load": (C.c_int, [P, C.c_char_p]),
+    "slime_set_steps_done": (C.c_int, [P, C.c_uint64]),
     "slime_step": (C.c_int, [P, C.c_uint32]),
     "slime_sync": (C.c_int, [P]),
     "slime_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
@@ -186,6 +206,7 @@ SIGNATURES = {
     "slime_ensemble_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
     "slime_ensemble_autotune": (C.c_int, [P, C.c_uint32]),
     "slime_ensemble_launch_count": (C.c_int, [P, C.POINTER(C.c_uint64)]),
+    "slime_ensemble_get_info": (C.c_int, [P, C.POINTER(SlimeEnsembleInfo)]),
     "slime_ensemble_selftest_barrier_timeout": (C.c_int, [P]),
     "slime_colorize": (C.c_int, [P, U8P, C.c_uint32, C.c_uint32, U8P]),
     "slime_colorize_async": (C.c_int, [P, U8P, C.c_uint32, C.c_uint32, U8P]),

@@ -42,9 +42,16 @@ def test_ensemble_matches_plain_runs(gpu, blur_mode, radius, reorder):
     for j, (W, H, n, p, agents, trail) in enumerate(cols):
         ens.upload_agents(j, agents)
         ens.upload_trail(j, trail)
+    assert ens.info().graphs_in_use == 0  # no step yet
     ens.step(7)
     ens.sync()
     assert ens.launch_count() >= 7
+    info = ens.info()
+    # the cooperative step launches were captured and replayed as graphs
+    assert info.graphs_in_use == 1, "capture of the cooperative launch fell back to direct launches"
+    assert (info.n_colonies, info.steps_done) == (len(cols), 7)
+    assert info.total_agents == sum(c[2] for c in cols) and info.total_cells == sum(c[0] * c[1] for c in cols)
+    assert info.grid_blocks > 0 and info.strip_rows in (8, 16, 32)
     for j, (W, H, n, p, agents, trail) in enumerate(cols):
         with sg.Simulation(W, H, n, p) as sim:
             sim.upload_agents(agents)

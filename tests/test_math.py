@@ -29,6 +29,11 @@ def test_payne_hanek_window_equals_table_exhaustively():
     assert oracle.ph_window_mismatches(139, 170) == 0
 
 
+def test_payne_hanek_tail_in_32_bit_words_equals_64_bit_statement_exhaustively():
+    # every finite binary32 with |x| >= 4096, both signs (1.9e9 inputs)
+    assert oracle.ph_finish_mismatches(139, 254) == 0
+
+
 def _ulp_errors(x):
     mpmath = pytest.importorskip("mpmath")
     mpmath.mp.prec = 200

@@ -122,7 +122,7 @@ def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
 
 
 @pytest.mark.parametrize("sensor_mode", [0, 1])
-@pytest.mark.parametrize("shape", range(1, 16))
+@pytest.mark.parametrize("shape", range(1, 17))
 @pytest.mark.parametrize("W,H", [(256, 150), (201, 150)])
 def test_every_agent_shape_is_bitexact(gpu, shape, W, H, sensor_mode):
     # 256 wide: the trail has gather textures; 201 wide: its rows are not
@@ -437,13 +437,85 @@ def test_checkpoint_resume_continues_bit_identically(gpu, tmp_path):
     a = make_sim(W, H, n, p, agents_uniform(n, W, H, 30.0, 50.0, seed=41))
     a.set_options(reorder_every=4)
     a.step(6)
-    path = str(tmp_path / "state.npz")
+    path = str(tmp_path / "run.slmstate")
     a.save_state(path)
     b = sg.Simulation.load_state(path)
+    b.set_options(reorder_every=4)
+    # the step counter comes back, so the reorders fall on the same steps
+    assert b.info().steps_done == a.info().steps_done == 6
+    ra, rb = a.info().reorders_done, b.info().reorders_done
     a.step(5)
     b.step(5)
+    assert a.info().reorders_done - ra == b.info().reorders_done - rb == 1  # at step 8
+    assert b.info().steps_done == 11
     assert_bitexact(a.download_agents(), b.download_agents(), "agents after resume")
     assert_bitexact(a.download_trail(), b.download_trail(), "trail after resume")
+    assert bytes(a.params()) == bytes(b.params())
+    # a state of another size or agent count is refused, the context unchanged
+    c = make_sim(W, H, n + 1, p, agents_uniform(n + 1, W, H, 30.0, 50.0, seed=42))
+    before = c.download_agents()
+    with pytest.raises(sg.SlimeError):
+        c.restore_state(path)
+    assert_bitexact(c.download_agents(), before, "agents after a refused load")
+    with open(path, "r+b") as f:
+        f.write(b"NOTSTATE")
+    with pytest.raises(sg.SlimeError):
+        b.restore_state(path)
+
+
+def seeded_agents(seed, n, W, H, hmin, hmax, smin, smax):
+    """slime_seed_agents' draws restated on the host: x ~ U[0,W), y ~ U[0,H),
+    angle ~ hmin + U[0,1) (hmax - hmin), speed ~ smin + U[0,1) (smax - smin),
+    each U[0,1) the seeded generator's draw for (seed, id, field), binary32."""
+    u = [oracle.uniform01(seed, n, f) for f in range(4)]
+    a = np.empty((n, 4), np.float32)
+    a[:, 0] = np.minimum(u[0] * np.float32(W), np.nextafter(np.float32(W), np.float32(0)))
+    a[:, 1] = np.minimum(u[1] * np.float32(H), np.nextafter(np.float32(H), np.float32(0)))
+    a[:, 2] = np.float32(hmin) + u[2] * (np.float32(hmax) - np.float32(hmin))
+    a[:, 3] = np.float32(smin) + u[3] * (np.float32(smax) - np.float32(smin))
+    return a
+
+
+def test_reassign_speeds_matches_generator(gpu):
+    """reassign_agent_speeds (src/main.rs:101-145) on the device: every
+    agent's speed is redrawn from the seeded generator (field 3 of its id) in
+    [speed_min, speed_max], bit for bit the host restatement; positions and
+    headings are untouched, also when the agents sit in Morton order."""
+    W, H, n = 300, 200, 20001
+    p = config0_params(W, H, agent_speed_min=12.5, agent_speed_max=47.0)
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=51)
+    sim = make_sim(W, H, n, p, agents)
+    for reorder in (False, True):
+        if reorder:
+            sim.reorder_agents()
+            assert sim.info().reordered == 1
+        sim.reassign_speeds(777 + reorder)
+        got = sim.download_agents()
+        want = seeded_agents(777 + reorder, n, W, H, 0.0, 1.0, 12.5, 47.0)[:, 3]
+        assert_bitexact(got[:, 3], want, f"speeds (reordered={reorder})")
+        assert_bitexact(got[:, :3], agents[:, :3], "positions and headings")
+
+
+def test_set_agent_count_matches_seed_generator(gpu):
+    """An agent-count change (src/main.rs:682-791) reseeds every agent: the
+    new agents are exactly slime_seed_agents' draws for the seed, with
+    headings in [0, 2pi) and the current speed bounds."""
+    import slime_gb300 as sg
+    W, H = 320, 180
+    p = config0_params(W, H, agent_speed_min=30.0, agent_speed_max=50.0)
+    sim = make_sim(W, H, 1000, p, agents_uniform(1000, W, H, 30.0, 50.0, seed=52))
+    sim.set_options(reorder_every=1)
+    sim.step(2)
+    for n, seed in ((5000, 9), (777, 10)):
+        sim.set_agent_count(n, seed=seed)
+        assert sim.info().reordered == 0
+        want = seeded_agents(seed, n, W, H, 0.0, 6.28318530718, 30.0, 50.0)
+        assert_bitexact(sim.download_agents(), want, f"agents after set_agent_count({n})")
+        other = sg.Simulation(W, H, n, p)
+        other.seed_agents(seed, 0.0, 6.28318530718)
+        assert_bitexact(other.download_agents(), want, "slime_seed_agents")
+        other.close()
+        sim.step(1)  # the new buffer steps
 
 
 def test_memory_cap_reports_out_of_memory(gpu):
