@@ -26,15 +26,28 @@ def build(force=False):
 
 
 # The reference's compute and display shaders, translated to C++ and built
-# beside the oracle to pin it (tests/test_reference_pin.py).  Built only where
-# the reference's source tree is present; outputs go to oracle/_ref/ only.
-REF_WGSL = os.environ.get("SLIME_REFERENCE_WGSL", "/root/reference/src/compute.wgsl")
-REF_DISPLAY_WGSL = os.path.join(os.path.dirname(REF_WGSL), "display.wgsl")
+# beside the oracle to pin it (tests/test_reference_pin.py).  This recipe
+# reads them where the reference's source tree lies: the tree given by the
+# `reference` argument, else $SLIME_REFERENCE_ROOT, else the build machine's
+# checkout below.  Built only where that tree is present; outputs go to
+# oracle/_ref/ only.
+REFERENCE_CHECKOUT = "/root/reference"
+
+
+def reference_shaders(reference=None):
+    root = reference or os.environ.get("SLIME_REFERENCE_ROOT") or REFERENCE_CHECKOUT
+    return os.path.join(root, "src", "compute.wgsl"), os.path.join(root, "src", "display.wgsl")
+
+
+REF_WGSL, REF_DISPLAY_WGSL = reference_shaders()
 REF_DIR = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_DIR, "libwgslref.so")
 
 
-def build_reference(force=False):
+def build_reference(force=False, reference=None):
+    """Translate and build the reference's shaders from `reference` (a source
+    tree), or from the default tree; None where it is absent."""
+    REF_WGSL, REF_DISPLAY_WGSL = reference_shaders(reference)
     if not os.path.exists(REF_WGSL):
         return None
     os.makedirs(REF_DIR, exist_ok=True)
@@ -60,5 +73,6 @@ def build_reference(force=False):
 
 
 if __name__ == "__main__":
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
     print(build(force="--force" in sys.argv))
-    print(build_reference(force="--force" in sys.argv))
+    print(build_reference(force="--force" in sys.argv, reference=args[0] if args else None))

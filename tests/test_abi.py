@@ -145,17 +145,85 @@ def test_host_destinations_are_checked_before_the_library_writes():
         sg.Ensemble([64, 64], [64], [10, 10], [None, None])
 
 
-def test_rust_binding_in_the_integration_notes_matches_the_header():
-    """Every `fn slime_*` of the Rust extern block shown in INTEGRATION.md is
-    declared in include/slime.h with the same number of arguments."""
+C_TO_RUST = {
+    "uint32_t": "u32", "uint64_t": "u64", "int": "c_int", "float": "f32", "double": "f64", "size_t": "usize",
+    "uint8_t": "u8", "char": "c_char", "void": "c_void",
+}
+
+
+def c_type_to_rust(t):
+    """A C parameter or return type of include/slime.h in the Rust binding's
+    spelling: `const float*` -> `*const f32`, `void**` -> `*mut *mut c_void`,
+    `const char**` -> `*mut *const c_char`, `slime_ctx*` -> `*mut slime_ctx`."""
+    t = " ".join(t.replace("*", " * ").split())
+    stars = t.count("*")
+    base = t.replace("*", "").split()
+    const = base[0] == "const"
+    name = base[-1]
+    rust = C_TO_RUST.get(name, name)
+    if stars == 0:
+        return rust
+    inner = ("*const " if const else "*mut ") + rust
+    return "*mut " * (stars - 1) + inner
+
+
+def header_declarations():
     src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "slime.h")).read(), flags=re.S)
-    arity = {}
-    for m in re.finditer(r"\b(slime_\w+)\s*\(([^;{]*?)\)\s*;", src):
-        args = [a for a in m.group(2).split(",") if a.strip() and a.strip() != "void"]
-        arity[m.group(1)] = len(args)
-    notes = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    bound = re.findall(r"fn (slime_\w+)\(([^)]*)\)", notes)
-    assert len(bound) >= 15
-    for name, args in bound:
-        assert name in arity, name
-        assert len([a for a in args.split(",") if a.strip()]) == arity[name], name
+    decls = {}
+    for m in re.finditer(r"^([\w\s\*]+?)\b(slime_\w+)\s*\(([^;{]*?)\)\s*;", src, re.M):
+        ret = c_type_to_rust(m.group(1).strip())
+        args = []
+        for a in m.group(3).split(","):
+            a = " ".join(a.split())
+            if not a or a == "void":
+                continue
+            ty = re.sub(r"\s*\b\w+$", "", a)  # drop the parameter name
+            args.append(c_type_to_rust(ty))
+        decls[m.group(2)] = (args, None if ret == "c_void" else ret)
+    return decls, src
+
+
+def rust_source():
+    return open(os.path.join(ROOT, "rust", "slime_cuda", "src", "lib.rs")).read()
+
+
+def test_rust_binding_declares_every_entry_point_with_the_header_types():
+    """rust/slime_cuda/src/lib.rs (not compiled here: no Rust toolchain in
+    this image) declares every function of include/slime.h with the same
+    argument and return types, and nothing else."""
+    decls, _ = header_declarations()
+    src = rust_source()
+    block = src[src.index('unsafe extern "C" {'):]
+    block = block[:block.index("\n    }\n")]
+    bound = {}
+    for m in re.finditer(r"pub fn (slime_\w+)\((.*?)\)\s*(?:->\s*([^;]+))?;", block, re.S):
+        args = [" ".join(a.split(":", 1)[1].split()) for a in m.group(2).split(",") if a.strip()]
+        ret = " ".join(m.group(3).split()) if m.group(3) else None
+        bound[m.group(1)] = (args, ret)
+    assert set(bound) == set(decls), (sorted(set(decls) - set(bound)), sorted(set(bound) - set(decls)))
+    for name, (args, ret) in decls.items():
+        assert bound[name] == (args, ret), (name, bound[name], (args, ret))
+
+
+def test_rust_binding_structs_and_constants_match_the_header():
+    _, src_h = header_declarations()
+    src_r = rust_source()
+    structs = re.findall(r"typedef struct (\w+) \{(.*?)\} \1;", src_h, re.S)
+    assert len(structs) == 6
+    for name, body in structs:
+        c_fields = []
+        for line in body.split(";"):
+            line = " ".join(line.split())
+            if line:
+                ty, field = line.rsplit(" ", 1)
+                c_fields.append((field, c_type_to_rust(ty)))
+        m = re.search(r"pub struct %s \{(.*?)\n    \}" % name, src_r, re.S)
+        assert m, name
+        r_fields = [tuple(x.strip() for x in f.split(":")) for f in re.findall(r"pub (\w+: \w+),", m.group(1))]
+        r_fields = [(f, t) for f, t in r_fields]
+        assert r_fields == c_fields, name
+        assert "#[repr(C)]" in src_r[:m.start()].rsplit("pub struct", 1)[-1] or \
+            src_r[:m.start()].rstrip().endswith(")]")
+    defines = dict(re.findall(r"#define (SLIME_\w+) \(?(-?\d+)u?\)?", src_h))
+    consts = dict(re.findall(r"pub const (SLIME_\w+): \w+ = (-?\d+);", src_r))
+    assert defines == consts
