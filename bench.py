@@ -271,7 +271,7 @@ def run_ensemble(args):
     import torch
     import slime_gb300 as sg
     torch.cuda.set_device(0)
-    cols = ensemble_colonies()
+    cols = ensemble_colonies(k=args.colonies)
     cells = sum(c[0] * c[1] for c in cols)
     agents_total = sum(c[2] for c in cols)
     ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
@@ -342,7 +342,7 @@ def run_ensemble(args):
         "value": ens_cells, "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "ensemble-64", "colonies": len(cols), "cells": cells, "agents": agents_total,
+        "config": {"workload": f"ensemble-{len(cols)}", "colonies": len(cols), "cells": cells, "agents": agents_total,
                    "sides": sorted(set(c[0] for c in cols)), "reorder_every": args.reorder_every},
         "agent_steps_per_s": ens_agents,
         "sequential_plain_cells_per_s": seq_cells, "ensemble_over_sequential": ens_cells / seq_cells,
@@ -363,7 +363,7 @@ def run_adjoint(args):
     import slime_gb300 as sg
     torch.cuda.set_device(0)
     W, H, n, lo, hi, dist = CONFIGS["adjoint-1024"]
-    steps = 2000
+    steps = args.adjoint_steps
     p = make_params(W, H, lo, hi, dist)
     agents = make_agents(n, W, H, lo, hi, seed=0)
     sim = sg.Simulation(W, H, n, p)
@@ -400,7 +400,7 @@ def run_adjoint(args):
     sim.sync()
     t_plain = time.perf_counter() - t0
     line = {
-        "metric": "adjoint cost / forward cost (1024x1024, 1,048,576 agents, 2000 steps, checkpoints every 50)",
+        "metric": f"adjoint cost / forward cost (1024x1024, 1,048,576 agents, {steps} steps, checkpoints every 50)",
         "value": t_bwd / t_fwd, "unit": "ratio", "n_gpus": 1, "steps": steps, "warmup": 0,
         "ms_per_step": 1000 * t_bwd / steps, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
@@ -565,6 +565,10 @@ def main():
                     help="1 + shape-table index of the agent kernel (0: autotuned)")
     ap.add_argument("--dispatch", default="each", choices=["each", "reference"],
                     help="agents updated per step: every agent once, or the reference's own dispatch")
+    ap.add_argument("--colonies", type=int, default=64,
+                    help="ensemble-64: the first K of the 64 seeded colonies (smaller captures)")
+    ap.add_argument("--adjoint-steps", type=int, default=2000,
+                    help="adjoint-1024: steps recorded and back-propagated (2000 in the configuration)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -24,11 +24,11 @@ def assert_rel(got, ref, what, tol=REL):
         assert abs(got - ref) <= tol * abs(ref), (what, got, ref, abs(got - ref) / abs(ref))
 
 
-def run_case(W, H, n, steps, K, dm, bm, dep, seed=0, radius=1.0, t_lo=0.0):
+def run_case(W, H, n, steps, K, dm, bm, dep, seed=0, radius=1.0, t_lo=0.0, decay=None):
     import slime_gb300 as sg
     p = config0_params(W, H, decay_mode=dm, blur_mode=bm, pheromone_deposition_amount=dep,
-                       decay_factor=0.97 if dm else 10.0, agent_speed_min=30.0, agent_speed_max=50.0,
-                       blur_radius=radius)
+                       decay_factor=decay if decay is not None else (0.97 if dm else 10.0), agent_speed_min=30.0,
+                       agent_speed_max=50.0, blur_radius=radius)
     agents = agents_uniform(n, W, H, 30.0, 50.0, seed=seed)
     rng = np.random.default_rng(seed + 1)
     t0 = (t_lo + rng.random((H, W)) * (0.5 - t_lo)).astype(np.float32)
@@ -81,6 +81,43 @@ def test_adjoint_matches_finite_differences(gpu):
         fd = fd4(lin_loss, theta, i, h)
         assert_rel(got[i], fd, f"parameter {i} vs finite differences")
     assert target is None
+
+
+def test_adjoint_at_the_1024_configuration_size(gpu):
+    """The adjoint at the size of the 1024^2 gradient configuration:
+    1,048,576 agents on a 1024x1024 trail, 200 steps recorded with
+    checkpoints every 50 (four segments replayed), multiplicative decay and
+    the 3-tap Gaussian, off the clamp kinks (deposition 2e-4, decay 0.95,
+    trail in [0.1, 0.5]: the agents gather into networks with up to ~350 of
+    them on a cell, yet no fold input comes near the clamp at 1).  The
+    parameter gradients of L = 0.5 ||T_200 - target||^2 must lie within 1e-6
+    relative of the binary64 adjoint and of binary64 fourth-order central
+    differences (h = 1e-4) of the frozen-trajectory forward; the
+    initial-trail gradient within 1e-6 of its largest entry."""
+    W = H = 1024
+    n, steps, K, dep = 1_048_576, 200, 50, 2e-4
+    p, t0, counts, theta, grads, d0, ref, d0_ref, g = run_case(W, H, n, steps, K, 1, 1, dep, seed=11, t_lo=0.1,
+                                                               decay=0.95)
+    # every fold input t + dep k of the binary64 forward stays below 0.9, so
+    # the differences (which move the trail by a few per cent) see no kink
+    t, worst = t0.astype(np.float64), 0.0
+    for s in range(steps):
+        worst = max(worst, float((t + theta[2] * counts[s]).max()))
+        _, t = oracle.chain_loss_f64(p, W, H, *theta, t, counts[s:s + 1], np.zeros((H, W)))
+    assert worst < 0.9, worst
+    got = [grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount]
+    for i in range(3):
+        assert_rel(got[i], ref[i], f"parameter {i} vs the binary64 adjoint")
+    assert np.abs(d0 - d0_ref).max() <= REL * np.abs(d0_ref).max()
+    gf = g.astype(np.float64)
+
+    def lin_loss(th):
+        # <g, T_n> has the same gradient as the loss at the forward the GPU ran
+        _, fin = oracle.chain_loss_f64(p, W, H, *th, t0, counts, np.zeros((H, W)))
+        return (fin * gf).sum()
+
+    for i in range(3):
+        assert_rel(got[i], fd4(lin_loss, theta, i, 1e-4), f"parameter {i} vs finite differences")
 
 
 def test_adjoint_radius2_and_ragged_segments(gpu):
