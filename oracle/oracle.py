@@ -45,6 +45,9 @@ def lib():
         L.oracle_chain_adjoint_f64.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
                                                f64, u32, C.c_uint32, f64, f64, f64, f64, C.c_int]
         L.oracle_chain_adjoint_f64.restype = C.c_double
+        L.oracle_chain_adjoint_f64_along.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                                     f32, u32, C.c_uint32, f64, f64, f64, C.c_int]
+        L.oracle_chain_adjoint_f64_along.restype = C.c_double
         L.oracle_colorize.argtypes = [C.c_uint32, C.c_uint32, f32, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint32,
                                       C.POINTER(C.c_uint8)]
         L.oracle_colorize.restype = None
@@ -136,6 +139,21 @@ def chain_adjoint_f64(params, W, H, decay, rate, dep, trail0, counts, target=Non
                                           _p(gf, C.c_double) if gf is not None else None,
                                           _p(d0, C.c_double), _p(grads, C.c_double), threads)
     return loss, grads, d0.reshape(H, W)
+
+
+def chain_adjoint_f64_along(params, W, H, decay, rate, dep, trails, counts, g_final, threads=0):
+    """The binary64 adjoint along given trails T_0..T_steps (steps + 1 grids,
+    binary32), e.g. those of the binary32 forward a GPU backward differentiates."""
+    tr = np.ascontiguousarray(trails, np.float32)
+    cn = np.ascontiguousarray(counts, np.uint32)
+    assert tr.shape[0] == cn.shape[0] + 1
+    gf = np.ascontiguousarray(g_final, np.float64).reshape(-1)
+    d0 = np.empty(W * H, np.float64)
+    grads = np.zeros(3, np.float64)
+    lib().oracle_chain_adjoint_f64_along(C.byref(params), W, H, decay, rate, dep, _p(tr, C.c_float),
+                                         _p(cn, C.c_uint32), cn.shape[0], _p(gf, C.c_double), _p(d0, C.c_double),
+                                         _p(grads, C.c_double), threads)
+    return grads, d0.reshape(H, W)
 
 
 def colorize(W, H, trail, lut768, tw, th):

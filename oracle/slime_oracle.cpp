@@ -466,6 +466,10 @@ double oracle_chain_loss_f64(const SlimeParams* p, uint32_t W, uint32_t H, doubl
  * unclamped iff k == 0 or 0 < Fold < 1; the subtractive decay is active iff
  * f - decay*0.001 > 0; the diffusion-rate clamp passes the gradient iff
  * 0 < rate < 1. */
+static double chain_adjoint(const ChainParams& c, uint32_t W, uint32_t H, const std::vector<double>& trails,
+                            double loss, const uint32_t* counts, uint32_t steps, const double* target,
+                            const double* g_final, double* d_trail0, double* grads, int nt);
+
 double oracle_chain_adjoint_f64(const SlimeParams* p, uint32_t W, uint32_t H, double decay, double rate,
                                 double dep, const double* trail0, const uint32_t* counts, uint32_t steps,
                                 const double* target, const double* g_final, double* d_trail0, double* grads,
@@ -476,6 +480,31 @@ double oracle_chain_adjoint_f64(const SlimeParams* p, uint32_t W, uint32_t H, do
     const size_t ncell = (size_t)W * H;
     std::vector<double> trails((size_t)(steps + 1) * ncell);
     double loss = chain_forward(&c, trail0, counts, steps, target, nullptr, trails.data(), nt);
+    return chain_adjoint(c, W, H, trails, loss, counts, steps, target, g_final, d_trail0, grads, nt);
+}
+
+/* The same adjoint (binary64 arithmetic) along a given trajectory: the
+ * trails T_0 .. T_steps of a binary32 forward (trails_f32, steps + 1 grids)
+ * instead of the binary64 forward.  It separates the error of a binary32
+ * backward's own arithmetic from the difference between the binary32 and
+ * binary64 forwards it differentiates.  g_final = dL/dT_steps is required. */
+double oracle_chain_adjoint_f64_along(const SlimeParams* p, uint32_t W, uint32_t H, double decay, double rate,
+                                      double dep, const float* trails_f32, const uint32_t* counts, uint32_t steps,
+                                      const double* g_final, double* d_trail0, double* grads, int threads) {
+    const int nt = resolve_threads(threads);
+    ChainParams c;
+    chain_setup(&c, p, W, H, decay, rate, dep);
+    const size_t n = (size_t)(steps + 1) * W * H;
+    std::vector<double> trails(n);
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t i = 0; i < (int64_t)n; i++) trails[i] = (double)trails_f32[i];
+    return chain_adjoint(c, W, H, trails, 0.0, counts, steps, nullptr, g_final, d_trail0, grads, nt);
+}
+
+static double chain_adjoint(const ChainParams& c, uint32_t W, uint32_t H, const std::vector<double>& trails,
+                            double loss, const uint32_t* counts, uint32_t steps, const double* target,
+                            const double* g_final, double* d_trail0, double* grads, int nt) {
+    const size_t ncell = (size_t)W * H;
     std::vector<double> g(ncell), gu(ncell), f(ncell), u(ncell), bu(ncell), bg(ncell), tmp(ncell);
     const double* tf = trails.data() + (size_t)steps * ncell;
     for (size_t i = 0; i < ncell; i++) g[i] = target ? (tf[i] - target[i]) : g_final[i];

@@ -89,27 +89,60 @@ def test_adjoint_at_the_1024_configuration_size(gpu):
     checkpoints every 50 (four segments replayed), multiplicative decay and
     the 3-tap Gaussian, off the clamp kinks (deposition 2e-4, decay 0.95,
     trail in [0.1, 0.5]: the agents gather into networks with up to ~350 of
-    them on a cell, yet no fold input comes near the clamp at 1).  The
-    parameter gradients of L = 0.5 ||T_200 - target||^2 must lie within 1e-6
-    relative of the binary64 adjoint and of binary64 fourth-order central
-    differences (h = 1e-4) of the frozen-trajectory forward; the
-    initial-trail gradient within 1e-6 of its largest entry."""
+    them on a cell, yet no fold input comes near the clamp at 1), loss
+    L = 0.5 ||T_200 - target||^2.
+
+    Two references, two tolerances:
+      * the binary64 adjoint run along the binary32 trajectory the GPU ran
+        (its trails replayed bit for bit by the oracle): the backward's own
+        arithmetic, within 1e-6 relative (measured 2.5e-7 for the rate);
+      * the binary64 adjoint of the binary64 forward, and binary64
+        fourth-order central differences (h = 1e-4) of the frozen-trajectory
+        forward: within 2e-6 relative.  Over 200 steps the binary32 forward
+        itself departs from the binary64 one enough to move the gradients by
+        up to 8.8e-7 relative (the rate's B(u) - u is a small difference of
+        nearly equal trails); with the backward's share the GPU measured
+        1.13e-6 there.
+    The initial-trail gradient: within 1e-6 of its largest entry against
+    the first reference."""
+    import slime_gb300 as sg
     W = H = 1024
     n, steps, K, dep = 1_048_576, 200, 50, 2e-4
-    p, t0, counts, theta, grads, d0, ref, d0_ref, g = run_case(W, H, n, steps, K, 1, 1, dep, seed=11, t_lo=0.1,
-                                                               decay=0.95)
-    # every fold input t + dep k of the binary64 forward stays below 0.9, so
-    # the differences (which move the trail by a few per cent) see no kink
-    t, worst = t0.astype(np.float64), 0.0
+    p = config0_params(W, H, decay_mode=1, blur_mode=1, pheromone_deposition_amount=dep, decay_factor=0.95,
+                       agent_speed_min=30.0, agent_speed_max=50.0)
+    agents = agents_uniform(n, W, H, 30.0, 50.0, seed=11)
+    rng = np.random.default_rng(12)
+    t0 = (0.1 + rng.random((H, W)) * 0.4).astype(np.float32)
+    target = rng.random((H, W)).astype(np.float32)
+    with sg.Simulation(W, H, n, p) as sim:
+        sim.upload_agents(agents)
+        sim.upload_trail(t0)
+        sim.forward_record(steps, K)
+        tn = sim.download_trail()
+        g = tn - target
+        grads, d0 = sim.backward(g)
+    # the oracle's replay of the same binary32 forward, step by step
+    a, t = agents.copy(), t0.copy()
+    trails = np.empty((steps + 1, H, W), np.float32)
+    counts = np.empty((steps, H, W), np.uint32)
+    trails[0] = t
     for s in range(steps):
-        worst = max(worst, float((t + theta[2] * counts[s]).max()))
-        _, t = oracle.chain_loss_f64(p, W, H, *theta, t, counts[s:s + 1], np.zeros((H, W)))
-    assert worst < 0.9, worst
+        counts[s] = oracle.agents_pass(p, W, H, a, t)
+        t = oracle.trail_pass(p, W, H, t, counts[s])
+        trails[s + 1] = t
+    assert np.array_equal(t, tn), "forward differs from the oracle"
+    theta = [float(np.float32(0.95)), float(np.float32(p.diffusion_rate)), float(np.float32(dep))]
+    # every fold input t + dep k stays below 0.9: the differences (which move
+    # the trail by a few per cent) see no kink
+    assert float((trails[:-1] + np.float32(dep) * counts).max()) < 0.9
     got = [grads.d_decay_factor, grads.d_diffusion_rate, grads.d_deposition_amount]
-    for i in range(3):
-        assert_rel(got[i], ref[i], f"parameter {i} vs the binary64 adjoint")
-    assert np.abs(d0 - d0_ref).max() <= REL * np.abs(d0_ref).max()
     gf = g.astype(np.float64)
+    along, d0_along = oracle.chain_adjoint_f64_along(p, W, H, *theta, trails, counts, gf)
+    for i in range(3):
+        assert_rel(got[i], along[i], f"parameter {i} vs the binary64 adjoint along the binary32 forward")
+    assert np.abs(d0 - d0_along).max() <= REL * np.abs(d0_along).max()
+    del trails
+    _, ref, _ = oracle.chain_adjoint_f64(p, W, H, *theta, t0, counts, g_final=gf)
 
     def lin_loss(th):
         # <g, T_n> has the same gradient as the loss at the forward the GPU ran
@@ -117,7 +150,8 @@ def test_adjoint_at_the_1024_configuration_size(gpu):
         return (fin * gf).sum()
 
     for i in range(3):
-        assert_rel(got[i], fd4(lin_loss, theta, i, 1e-4), f"parameter {i} vs finite differences")
+        assert_rel(got[i], ref[i], f"parameter {i} vs the binary64 adjoint", tol=2 * REL)
+        assert_rel(got[i], fd4(lin_loss, theta, i, 1e-4), f"parameter {i} vs finite differences", tol=2 * REL)
 
 
 def test_adjoint_radius2_and_ragged_segments(gpu):
