@@ -241,6 +241,34 @@ SLM_FN int slm_clz32(uint32_t a) {
 #endif
 }
 
+/* |r| = |fraction| * pi/2 from the fraction's magnitude a = a_hi:a_lo
+ * (times 2^64, a_hi nonzero): its 30 leading bits as a 24-bit head plus an
+ * exact correction, both scaled by a power of two built in the exponent
+ * field, so only 32-bit conversions are needed. */
+SLM_FN float slm_ph_abs_r(uint32_t a_lo, uint32_t a_hi) {
+    const int lz = slm_clz32(a_hi);
+    const uint32_t t = slm_funnel_l(a_lo, a_hi, lz) >> 2; /* in [2^29, 2^30) */
+    float hi = (float)(int32_t)t;
+    float lo = (float)((int32_t)t - (int32_t)hi);
+    float scale = slm_u2f_bits((uint32_t)(127 - 30 - lz) << 23); /* 2^(-30-lz) */
+    float rh = slm_mul(hi, scale);
+    float rl = slm_mul(lo, scale);
+    return slm_fma(rh, SLM_PIO2_1, slm_fma(rh, SLM_PIO2_2, slm_mul(rl, SLM_PIO2_1)));
+}
+/* The same for a_hi == 0 (|fraction| < 2^-32, or zero), out of line. */
+SLM_COLD_FN float slm_ph_abs_r_small(uint32_t a_lo) {
+    if (a_lo == 0u) return 0.0f;
+    const int lzh = slm_clz32(a_lo);
+    const int lz = lzh + 32;
+    const uint32_t t = (a_lo << lzh) >> 2;
+    float hi = (float)(int32_t)t;
+    float lo = (float)((int32_t)t - (int32_t)hi);
+    float scale = slm_u2f_bits((uint32_t)(127 - 30 - lz) << 23);
+    float rh = slm_mul(hi, scale);
+    float rl = slm_mul(lo, scale);
+    return slm_fma(rh, SLM_PIO2_1, slm_fma(rh, SLM_PIO2_2, slm_mul(rl, SLM_PIO2_1)));
+}
+
 /* Second half of the Payne-Hanek reduction: from the mantissa m of |x|
  * (2^23 <= m < 2^24), the 96 bits w0:w1:w2 of 2/pi that follow the bits
  * dropped as multiples of 4, and the sign of x, the reduced argument and the
@@ -269,28 +297,13 @@ SLM_FN void slm_ph_finish(uint32_t m, uint32_t w0, uint32_t w1, uint32_t w2, uin
     const uint32_t mask = 0u - neg;
     const uint32_t a_lo = (f_lo ^ mask) + neg;
     const uint32_t a_hi = (f_hi ^ mask) + (a_lo < neg ? 1u : 0u); /* |fraction| * 2^64 */
-    float r = 0.0f;
-    if ((a_hi | a_lo) != 0u) {
-        /* the top 32 bits of the normalised fraction, and its leading zeros */
-        const uint32_t h = a_hi ? a_hi : a_lo;
-        const uint32_t l = a_hi ? a_lo : 0u;
-        const int lzh = slm_clz32(h);
-        const int lz = lzh + (a_hi ? 0 : 32);
-        const uint32_t t = slm_funnel_l(l, h, lzh) >> 2; /* in [2^29, 2^30) */
-        float hi = (float)(int32_t)t;
-        float lo = (float)((int32_t)t - (int32_t)hi);
-        float scale = slm_u2f_bits((uint32_t)(127 - 30 - lz) << 23); /* 2^(-30-lz) */
-        float rh = slm_mul(hi, scale);
-        float rl = slm_mul(lo, scale);
-        r = slm_fma(rh, SLM_PIO2_1, slm_fma(rh, SLM_PIO2_2, slm_mul(rl, SLM_PIO2_1)));
-        if (neg) r = -r;
-    }
-    if (sign) {
-        r = -r;
-        q = (4u - q) & 3u;
-    }
-    *r_out = r;
-    *q_out = (int)q;
+    /* |r| from |fraction|; a fraction below 2^-32 (or zero) out of line */
+    const float r_abs = a_hi != 0u ? slm_ph_abs_r(a_lo, a_hi) : slm_ph_abs_r_small(a_lo);
+    /* r takes the sign of the fraction times that of x (bit 31 of f_hi and of
+     * x); the quadrant of -x is -q (mod 4) */
+    *r_out = slm_u2f_bits(slm_f2u_bits(r_abs) ^ ((f_hi ^ (sign << 31)) & 0x80000000u));
+    const uint32_t smask = 0u - sign;
+    *q_out = (int)(((q ^ smask) - smask) & 3u);
 }
 
 /* The same in 64-bit integer arithmetic (the statement slm_ph_finish was
