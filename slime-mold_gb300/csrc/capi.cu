@@ -285,6 +285,9 @@ int alloc_trail(slime_ctx* ctx, uint32_t W, uint32_t H) {
         ctx->counts_dirty[i] = false;
         ctx->marks_dirty[i] = false;
     }
+    // tensor maps for the tensor-copy trail tile (none for widths it cannot take)
+    make_trail_maps(&ctx->tmaps, ctx->trail, ctx->counts, ctx->marks, W, H);
+    cudaGetLastError();
     ctx->cur = 0;
     ctx->last_counts_valid = false;
     ctx->trail_clean = true;
@@ -466,9 +469,9 @@ cudaError_t enqueue_trail_pass(slime_ctx* ctx, bool marks, bool pdl) {
     bool ht = trail_window(ctx, ctx->trail[1 - cur], &wt, kWindowTrail);
     if (marks)
         return launch_trail_marks(ctx->dev, ctx->tile, ctx->trail[cur], ctx->marks[cur], ctx->trail[1 - cur],
-                                  ctx->marks[1 - cur], ctx->stream, ht ? &wt : nullptr, pdl);
+                                  ctx->marks[1 - cur], ctx->stream, ht ? &wt : nullptr, pdl, &ctx->tmaps, cur);
     return launch_trail(ctx->dev, ctx->tile, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                        ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr, pdl);
+                        ctx->counts[1 - cur], ctx->stream, ht ? &wt : nullptr, pdl, &ctx->tmaps, cur);
 }
 
 // `chained`: the operation before this step on the stream is the previous
@@ -1065,6 +1068,9 @@ int slime_sync(slime_ctx* ctx) {
     if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->stream), "synchronising");
+    if (ctx->tile == kTrailTileTma && trail_tma_take_error())
+        return set_error(ctx->err, SLIME_ERR_DEVICE_TIMEOUT,
+                         "a trail tile gave up waiting for its tensor copies; its cells were not written");
     return SLIME_OK;
 }
 
@@ -1255,13 +1261,13 @@ int slime_autotune(slime_ctx* ctx, uint32_t reps) {
     int best_tile = ctx->tile;
     const bool marks_ok = marks_allowed(ctx);
     for (int t = 0; t < trail_tile_count(); t++) {
-        if (!trail_tile_supported(ctx->dev, t)) continue;
+        if (!trail_tile_supported(ctx->dev, t) || (t == kTrailTileTma && !ctx->tmaps.ok)) continue;
         const bool mk = marks_ok && trail_tile_streams(ctx->dev, t);
         auto trial = [&]() {
             return mk ? launch_trail_marks(ctx->dev, t, ctx->trail[cur], ctx->marks[cur], ctx->trail[1 - cur],
-                                           ctx->marks[1 - cur], ctx->stream)
+                                           ctx->marks[1 - cur], ctx->stream, nullptr, false, &ctx->tmaps, cur)
                       : launch_trail(ctx->dev, t, ctx->trail[cur], ctx->counts[cur], ctx->trail[1 - cur],
-                                     ctx->counts[1 - cur], ctx->stream);
+                                     ctx->counts[1 - cur], ctx->stream, nullptr, false, &ctx->tmaps, cur);
         };
         cudaError_t e = trial(); // warm-up
         if (e != cudaSuccess) continue;

@@ -26,6 +26,7 @@ struct slime_ctx {
 
     float* trail[2] = {nullptr, nullptr};
     cudaTextureObject_t trail_tex[2] = {0, 0}; // gather textures over trail[] (0 = none)
+    slime::TrailMaps tmaps;                    // tensor maps over trail[], counts[], marks[] (tmaps.ok)
     uint32_t* counts[2] = {nullptr, nullptr};
     int cur = 0;
     bool last_counts_valid = false;

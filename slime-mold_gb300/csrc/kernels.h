@@ -1,6 +1,7 @@
 // kernels.h - launch wrappers of the CUDA kernels (host side, internal).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -69,14 +70,26 @@ int trail_tile_default();
 // Whether tile `index` can run this parameter set / grid (the streaming
 // tiles need W % 4 == 0 and a blur radius of 1 or 2).
 bool trail_tile_supported(const DevParams& p, int tile);
+// Tensor maps (for the tensor-copy tile) over a context's two trails and
+// their deposit records, one set per blur radius (the box is the window).
+struct TrailMaps {
+    CUtensorMap trail[2], counts[2], marks[2];
+    CUtensorMap trail_r2[2], counts_r2[2], marks_r2[2];
+    bool ok = false;
+};
+// The trail-table index of the tensor-copy tile.
+constexpr int kTrailTileTma = 10;
+
 // Fused trail pass: out = Diffuse(Decay(Fold(in, counts_in))); zeroes
 // counts_zero (the other step's count buffer, may be null) over the same cells.
 // With `pdl` a streaming tile launches as a programmatic dependent of the
 // kernel before it in the stream (the agent pass); the shared-memory tiles
 // always launch in order.
+// The tensor-copy tile needs `maps` over the context's buffers and the index
+// `cur` of the buffers `in`/`counts_in` are.
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
                          uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr,
-                         bool pdl = false);
+                         bool pdl = false, const TrailMaps* maps = nullptr, int cur = 0);
 // Whether tile `index` is a streaming tile that runs here (the only ones that
 // read deposit marks).
 bool trail_tile_streams(const DevParams& p, int tile);
@@ -84,7 +97,22 @@ bool trail_tile_streams(const DevParams& p, int tile);
 // marks_zero.  Streaming tiles only (cudaErrorInvalidValue otherwise).
 cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, const uint8_t* marks_in, float* out,
                                uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win = nullptr,
-                               bool pdl = false);
+                               bool pdl = false, const TrailMaps* maps = nullptr, int cur = 0);
+
+// ---- trail_tma.cu
+// The tensor-copy tile: W % 16 == 0 and a blur radius of 1 or 2.
+bool trail_tma_supported(const DevParams& p);
+bool make_trail_maps(TrailMaps* m, const float* const trail[2], const uint32_t* const counts[2],
+                     const uint8_t* const marks[2], uint32_t W, uint32_t H);
+cudaError_t launch_trail_tma(const DevParams& p, const TrailMaps& maps, int cur, const float* in,
+                             const uint32_t* counts_in, float* out, uint32_t* counts_zero, cudaStream_t s,
+                             const cudaAccessPolicyWindow* win, bool pdl);
+cudaError_t launch_trail_tma_marks(const DevParams& p, const TrailMaps& maps, int cur, const float* in,
+                                   const uint8_t* marks_in, float* out, uint8_t* marks_zero, cudaStream_t s,
+                                   const cudaAccessPolicyWindow* win, bool pdl);
+// Whether a tensor-copy tile gave up waiting for its copies since the last
+// call (the flag is cleared).
+bool trail_tma_take_error();
 
 // ---- adjoint.cu
 // One backward step of the frozen-trajectory chain: from g_in = dL/dT_{s+1}

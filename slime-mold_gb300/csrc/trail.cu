@@ -183,15 +183,19 @@ cudaError_t launch_tile(const DevParams& p, const float* in, const uint32_t* cin
 } // namespace
 
 // Tile table: entries 0..kNumTiles-1 are the shared-memory tiles, the next
-// kNumStream entries the streaming kernel with 8, 16 and 32 rows per strip.
+// kNumStream entries the streaming kernel with 8, 16 and 32 rows per strip,
+// the last one (kTrailTileTma) the tensor-copy tile of 128 x 32 cells.
 constexpr int kNumStream = 3;
-int trail_tile_count() { return kNumTiles + kNumStream; }
+static_assert(kNumTiles + kNumStream == kTrailTileTma, "the tensor-copy tile follows the streaming ones");
+int trail_tile_count() { return kNumTiles + kNumStream + 1; }
 TrailTile trail_tile(int index) {
+    if (index == kTrailTileTma) return TrailTile{128, 32};
     if (index >= kNumTiles && index < kNumTiles + kNumStream) return TrailTile{128, 8 << (index - kNumTiles)};
     return kTiles[(index >= 0 && index < kNumTiles) ? index : 0];
 }
 int trail_tile_default() { return 3; }
 bool trail_tile_supported(const DevParams& p, int tile) {
+    if (tile == kTrailTileTma) return trail_tma_supported(p);
     if (tile < 0 || tile >= kNumTiles + kNumStream) return false;
     if (tile < kNumTiles) return true;
     // streaming kernel: whole float4 groups per row and radius <= 2, grid
@@ -203,8 +207,13 @@ bool trail_tile_supported(const DevParams& p, int tile) {
 bool trail_tile_streams(const DevParams& p, int tile) { return tile >= kNumTiles && trail_tile_supported(p, tile); }
 
 cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, const uint8_t* marks_in, float* out,
-                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl) {
+                               uint8_t* marks_zero, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl,
+                               const TrailMaps* maps, int cur) {
     if (!trail_tile_streams(p, tile)) return cudaErrorInvalidValue;
+    if (tile == kTrailTileTma) {
+        if (!maps || !maps->ok) return cudaErrorInvalidValue;
+        return launch_trail_tma_marks(p, *maps, cur, in, marks_in, out, marks_zero, s, win, pdl);
+    }
     switch (tile) {
     case 7: return launch_stream_rows<8>(p, in, marks_in, out, marks_zero, s, win, pdl);
     case 8: return launch_stream_rows<16>(p, in, marks_in, out, marks_zero, s, win, pdl);
@@ -213,8 +222,10 @@ cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, co
 }
 
 cudaError_t launch_trail(const DevParams& p, int tile, const float* in, const uint32_t* counts_in, float* out,
-                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl) {
-    if (!trail_tile_supported(p, tile)) tile = trail_tile_default();
+                         uint32_t* counts_zero, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl,
+                         const TrailMaps* maps, int cur) {
+    if (!trail_tile_supported(p, tile) || (tile == kTrailTileTma && !(maps && maps->ok))) tile = trail_tile_default();
+    if (tile == kTrailTileTma) return launch_trail_tma(p, *maps, cur, in, counts_in, out, counts_zero, s, win, pdl);
     switch (tile) {
     case 0: return launch_tile<32, 8>(p, in, counts_in, out, counts_zero, s, win);
     case 1: return launch_tile<64, 8>(p, in, counts_in, out, counts_zero, s, win);

@@ -104,10 +104,12 @@ def test_graph_chunks_match_single_steps(gpu):
     assert a.info().steps_done == 23
 
 
-@pytest.mark.parametrize("tile", range(1, 11))
+@pytest.mark.parametrize("tile", range(1, 12))
 @pytest.mark.parametrize("W,H", [(333, 77), (336, 77), (256, 40), (8, 9)])
 def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
-    n = 5000  # sizes ragged against every tile shape; the streaming tiles need W % 4 == 0
+    # sizes ragged against every tile shape; the streaming tiles need W % 4 == 0,
+    # the tensor-copy tile (11) W % 16 == 0 and has interior tiles at 336 x 77
+    n = 5000
     for blur_mode, radius in ((0, 1.0), (1, 1.0), (1, 2.0), (1, 3.0)):
         p = config0_params(W, H, decay_mode=1, blur_mode=blur_mode, blur_radius=radius, blur_sigma=1.5)
         agents = agents_uniform(n, W, H, 1.0, 2.0, seed=4)
@@ -580,7 +582,10 @@ def test_l2_carveout_only_for_trails_that_fit(gpu):
 STREAM8 = 8  # 1 + the tile-table index of the 8-row streaming trail kernel
 
 
-@pytest.mark.parametrize("tile", [STREAM8, 9, 10])
+TMA_TILE = 11  # 1 + the tile-table index of the tensor-copy trail tile
+
+
+@pytest.mark.parametrize("tile", [STREAM8, 9, 10, TMA_TILE])
 @pytest.mark.parametrize("decay_mode,decay,dep", [(0, 10.0, 1.0), (1, 0.97, 1.0), (1, 0.9, 2.5), (0, 0.0, 1.0)])
 def test_deposit_marks_match_counts(gpu, decay_mode, decay, dep, tile):
     """Steps that record deposit marks (deposition >= 1 on a non-negative
@@ -646,3 +651,33 @@ def test_deposit_marks_only_when_every_deposit_saturates(gpu):
     sim.step(1)
     with pytest.raises(RuntimeError):
         sim.download_deposit_counts()
+
+
+@pytest.mark.parametrize("W,H", [(1024, 512), (4096, 64), (528, 97), (160, 34)])
+def test_tensor_copy_trail_tile(gpu, W, H):
+    """The trail pass whose input window arrives by 2-D tensor copies (one
+    box of trail and one of deposit record per 128 x 32 tile, the border tiles
+    by wrapped loads): bit for bit the oracle over several steps, with byte
+    marks and with 32-bit counts, box blur and Gaussian radius 1 and 2, both
+    decays.  160 x 34 is the smallest grid with an interior tile at radius 1
+    (a 16-column margin of byte marks on each side and one halo row)."""
+    n = W * H // 2
+    for blur_mode, radius, decay_mode, decay in ((0, 1.0, 0, 10.0), (1, 1.0, 1, 0.97), (1, 2.0, 1, 0.9),
+                                                 (1, 1.0, 0, 3.0)):
+        for exact_counts in (0, 1):
+            p = config0_params(W, H, decay_mode=decay_mode, blur_mode=blur_mode, blur_radius=radius, blur_sigma=1.2,
+                               decay_factor=decay)
+            agents = agents_uniform(n, W, H, 1.0, 2.0, seed=W + H)
+            trail = np.random.default_rng(H).random((H, W), dtype=np.float32)
+            sim = make_sim(W, H, n, p, agents, trail)
+            sim.set_options(trail_tile=TMA_TILE, exact_counts=exact_counts)
+            assert sim.info().trail_tile == TMA_TILE - 1
+            sim.step(3)
+            sim.sync()
+            ca, ct = agents.copy(), trail.copy()
+            oracle.run(p, W, H, ca, ct, 3)
+            what = f"{W}x{H} blur {blur_mode} r {radius} decay {decay_mode} counts {exact_counts}"
+            assert_bitexact(sim.download_trail(), ct, "trail " + what)
+            assert_bitexact(sim.download_agents(), ca, "agents " + what)
+            sim.close()
+
