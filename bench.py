@@ -61,8 +61,11 @@ def agents_kernel_name(shape):
 
 
 def trail_kernel_name(tile, blur_mode):
-    """Kernel of trail-tile table entry `tile` (trail.cu): 7-9 stream rows,
-    0-6 are shared-memory tiles of the box or Gaussian kernel."""
+    """Kernel of trail-tile table entry `tile` (trail.cu): 10 is the
+    tensor-copy tile, 7-9 stream rows, 0-6 are shared-memory tiles of the box
+    or Gaussian kernel."""
+    if tile == 10:
+        return "trail_tma_kernel"
     if tile >= 7:
         return "trail_stream_kernel"
     return "trail_gauss_kernel" if blur_mode == 1 else "trail_box3_kernel"

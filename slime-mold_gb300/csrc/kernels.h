@@ -113,6 +113,8 @@ cudaError_t launch_trail_tma_marks(const DevParams& p, const TrailMaps& maps, in
 // Whether a tensor-copy tile gave up waiting for its copies since the last
 // call (the flag is cleared).
 bool trail_tma_take_error();
+// Blocks that found their shared-memory boxes misaligned and used plain loads.
+int trail_tma_misaligned_blocks();
 
 // ---- adjoint.cu
 // One backward step of the frozen-trajectory chain: from g_in = dL/dT_{s+1}

@@ -211,7 +211,8 @@ cudaError_t launch_trail_marks(const DevParams& p, int tile, const float* in, co
                                const TrailMaps* maps, int cur) {
     if (!trail_tile_streams(p, tile)) return cudaErrorInvalidValue;
     if (tile == kTrailTileTma) {
-        if (!maps || !maps->ok) return cudaErrorInvalidValue;
+        // without tensor maps, the 8-row streaming tile (same requirements, same bits)
+        if (!maps || !maps->ok) return launch_stream_rows<8>(p, in, marks_in, out, marks_zero, s, win, pdl);
         return launch_trail_tma_marks(p, *maps, cur, in, marks_in, out, marks_zero, s, win, pdl);
     }
     switch (tile) {

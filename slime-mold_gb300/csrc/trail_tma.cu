@@ -41,6 +41,13 @@ constexpr int kTrailLead = 4;               // window column of x0 in the trail 
 constexpr int kMarkLead = 16;               // window column of x0 in the mark box
 
 __device__ int g_tma_wait_failed;
+// Blocks whose box destinations were not 128-byte aligned in the shared
+// window (they took the plain-load path instead; 0 expected).
+__device__ int g_tma_misaligned;
+
+// Rounds a byte count up to a 128-byte boundary (a tensor copy's shared
+// destination must be 128-byte aligned).
+__host__ __device__ constexpr size_t align128(size_t b) { return (b + 127) / 128 * 128; }
 
 template <class D>
 struct DepBox {
@@ -64,21 +71,38 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// Wait for phase 0 of the barrier; false after ~2^31 cycles (about a second).
-__device__ __forceinline__ bool mbar_wait0(uint64_t* bar) {
+
+// Parity wait on a barrier; false after ~2^31 cycles (about a second).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const long long t0 = clock64();
     while (true) {
         uint32_t done;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(smem_u32(bar))
+            : "r"(smem_u32(bar)), "r"(parity)
             : "memory");
         if (done) return true;
         if (clock64() - t0 > (1ll << 31)) return false;
     }
 }
 
+// Shared-memory layout of a block: the mbarrier, then the trail box, then the
+// deposit box, each box on a 128-byte boundary.
+template <int R, class D>
+struct Layout {
+    static constexpr int WR = kTmaRows + 2 * R;
+    static constexpr size_t trail_off = 128;
+    static constexpr size_t dep_off = trail_off + align128(sizeof(float) * WR * kTrailBoxCols);
+    static constexpr size_t bytes = dep_off + sizeof(D) * WR * DepBox<D>::cols;
+    static constexpr uint32_t tx_bytes = (uint32_t)(sizeof(float) * WR * kTrailBoxCols + sizeof(D) * WR * DepBox<D>::cols);
+};
+
+// One block, one tile.  Every tile's window comes by the two tensor copies;
+// a box that reaches outside the array is filled with zeros there, and a
+// border tile then overwrites those halo cells with the opposite side's cells
+// (plain loads of the wrapped rows and columns only).  One thread waits on
+// the barrier; the others wait at the block barrier after it.
 template <int R, bool kGauss, int kDecay, class D>
 __global__ void __launch_bounds__(kTmaThreads) trail_tma_kernel(const __grid_constant__ DevParams p,
                                                                 const __grid_constant__ CUtensorMap map_t,
@@ -87,51 +111,68 @@ __global__ void __launch_bounds__(kTmaThreads) trail_tma_kernel(const __grid_con
                                                                 const D* __restrict__ din, float* __restrict__ out,
                                                                 D* __restrict__ dzero) {
     constexpr bool kMarks = sizeof(D) == 1;
-    constexpr int WR = kTmaRows + 2 * R; // window rows
+    typedef Layout<R, D> L;
+    constexpr int WR = L::WR;
     constexpr int DC = DepBox<D>::cols, DL = DepBox<D>::lead;
+    constexpr int WC = kTmaCols + 2 * R; // window columns x0-R .. x0+127+R
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-    float* tw = reinterpret_cast<float*>(smem + 128);                               // WR x kTrailBoxCols
-    D* dw = reinterpret_cast<D*>(smem + 128 + sizeof(float) * WR * kTrailBoxCols); // WR x DC
+    float* tw = reinterpret_cast<float*>(smem + L::trail_off); // WR x kTrailBoxCols
+    D* dw = reinterpret_cast<D*>(smem + L::dep_off);           // WR x DC
+    __shared__ int fail;
     const int W = p.W, H = p.H;
     const int x0 = blockIdx.x * kTmaCols, y0 = blockIdx.y * kTmaRows;
-    // interior tiles: both boxes inside the array (block-uniform)
-    const bool interior = x0 - DL >= 0 && x0 - DL + DC <= W && y0 - R >= 0 && y0 - R + WR <= H;
-    __shared__ int ok;
-    if (interior) {
+    // the copies' destinations must be 128-byte aligned in the shared window:
+    // checked, and a misaligned block loads its whole window by plain loads
+    const bool aligned = ((smem_u32(tw) | smem_u32(dw)) & 127u) == 0u;
+    const bool border = x0 - R < 0 || x0 + kTmaCols + R > W || y0 - R < 0 || y0 - R + WR > H;
+    if (aligned) {
         if (threadIdx.x == 0) {
+            fail = 0;
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const uint32_t bytes = (uint32_t)(sizeof(float) * WR * kTrailBoxCols + sizeof(D) * WR * DC);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                         "r"(L::tx_bytes)
                          : "memory");
             // the trail this reads is not written by the agent pass
             tma_load_2d(tw, &map_t, x0 - kTrailLead, y0 - R, bar);
         }
         // the deposit record is the agent pass's output
         pdl_wait();
-        if (threadIdx.x == 0) tma_load_2d(dw, &map_d, x0 - DL, y0 - R, bar);
-        pdl_trigger();
-        __syncthreads(); // the barrier is initialised before anyone waits on it
-        const bool done = mbar_wait0(bar);
-        if (threadIdx.x == 0) ok = done ? 1 : 0;
-        __syncthreads();
-        if (!ok) {
-            if (threadIdx.x == 0) atomicExch(&g_tma_wait_failed, 1);
-            return;
+        if (threadIdx.x == 0) {
+            tma_load_2d(dw, &map_d, x0 - DL, y0 - R, bar);
+            if (!mbar_wait(bar, 0)) {
+                fail = 1;
+                atomicExch(&g_tma_wait_failed, 1);
+            }
         }
-        // fold + decay of the window's cells in place (columns x0-R .. x0+127+R)
-        for (int i = threadIdx.x; i < WR * (kTmaCols + 2 * R); i += kTmaThreads) {
-            const int r = i / (kTmaCols + 2 * R), c = i - r * (kTmaCols + 2 * R) - R; // c = column - x0
+        pdl_trigger();
+        __syncthreads();
+        if (fail) return;
+        if (border) {
+            // the window's cells outside the array: the opposite side's
+            for (int i = threadIdx.x; i < WR * WC; i += kTmaThreads) {
+                const int r = i / WC, c = i - r * WC - R;
+                const int gy = y0 - R + r, gx = x0 + c;
+                if (gy >= 0 && gy < H && gx >= 0 && gx < W) continue;
+                const size_t gi = (size_t)wrap_coord(gy, H) * W + wrap_coord(gx, W);
+                tw[r * kTrailBoxCols + kTrailLead + c] = __ldg(in + gi);
+                dw[r * DC + DL + c] = __ldg(din + gi);
+            }
+            __syncthreads();
+        }
+        // fold + decay of the window's cells in place
+        for (int i = threadIdx.x; i < WR * WC; i += kTmaThreads) {
+            const int r = i / WC, c = i - r * WC - R; // c = column - x0
             float& v = tw[r * kTrailBoxCols + kTrailLead + c];
             v = apply_decay_m<kDecay>(p, fold_dep<kMarks>(v, (uint32_t)dw[r * DC + DL + c], p.dep));
         }
     } else {
+        if (threadIdx.x == 0) atomicAdd(&g_tma_misaligned, 1);
         pdl_wait();
         pdl_trigger();
-        // border tile: the same window from wrapped plain loads, folded and decayed
-        for (int i = threadIdx.x; i < WR * (kTmaCols + 2 * R); i += kTmaThreads) {
-            const int r = i / (kTmaCols + 2 * R), c = i - r * (kTmaCols + 2 * R) - R;
+        for (int i = threadIdx.x; i < WR * WC; i += kTmaThreads) {
+            const int r = i / WC, c = i - r * WC - R;
             const size_t gi = (size_t)wrap_coord(y0 - R + r, H) * W + wrap_coord(x0 + c, W);
             tw[r * kTrailBoxCols + kTrailLead + c] =
                 apply_decay_m<kDecay>(p, fold_dep<kMarks>(__ldg(in + gi), (uint32_t)__ldg(din + gi), p.dep));
@@ -139,65 +180,84 @@ __global__ void __launch_bounds__(kTmaThreads) trail_tma_kernel(const __grid_con
     }
     __syncthreads();
 
-    // blur: lane -> 4 columns, warp -> 4 rows
+    // blur: lane -> 4 columns, warp -> 4 output rows, the window's rows walked
+    // once with a rolling window of 2R+1 rows in registers (the horizontal
+    // pass of each row for the Gaussian, the row itself for the box)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c0 = lane * 4;
     const int ry = warp * 4; // first output row of the warp within the tile
-    float e[4 + 2 * R][4 + 2 * R]; // window rows ry .. ry+3+2R, columns c0-R .. c0+3+R
+    const int x = x0 + c0;
+    constexpr int NWIN = 2 * R + 1;
+    float win[NWIN][4 + 2 * R]; // box: window rows, columns c0-R .. c0+3+R
+    float hwin[NWIN][4];        // Gaussian: their horizontal passes
+    float ctr[NWIN][4];         // the rows' own cells (the mix's centre)
 #pragma unroll
     for (int r = 0; r < 4 + 2 * R; r++) {
+        // shift the window
+#pragma unroll
+        for (int q = 0; q < NWIN - 1; q++) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) ctr[q][j] = ctr[q + 1][j];
+            if (kGauss) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) hwin[q][j] = hwin[q + 1][j];
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4 + 2 * R; j++) win[q][j] = win[q + 1][j];
+            }
+        }
         const float* row = tw + (ry + r) * kTrailBoxCols + kTrailLead;
         const float4 v = *reinterpret_cast<const float4*>(row + c0);
         const float d[4] = {v.x, v.y, v.z, v.w};
+        float e[4 + 2 * R];
 #pragma unroll
-        for (int j = 0; j < 4; j++) e[r][R + j] = d[j];
+        for (int j = 0; j < 4; j++) e[R + j] = d[j];
 #pragma unroll
         for (int j = 0; j < R; j++) {
-            e[r][j] = __shfl_up_sync(0xffffffffu, d[4 - R + j], 1);
-            e[r][R + 4 + j] = __shfl_down_sync(0xffffffffu, d[j], 1);
+            e[j] = __shfl_up_sync(0xffffffffu, d[4 - R + j], 1);
+            e[R + 4 + j] = __shfl_down_sync(0xffffffffu, d[j], 1);
         }
         if (lane == 0) {
 #pragma unroll
-            for (int j = 0; j < R; j++) e[r][j] = row[c0 - R + j];
+            for (int j = 0; j < R; j++) e[j] = row[c0 - R + j];
         }
         if (lane == 31) {
 #pragma unroll
-            for (int j = 0; j < R; j++) e[r][R + 4 + j] = row[c0 + 4 + j];
+            for (int j = 0; j < R; j++) e[R + 4 + j] = row[c0 + 4 + j];
         }
-    }
-    float h[4 + 2 * R][4]; // Gaussian: the horizontal pass of each window row
-    if (kGauss) {
 #pragma unroll
-        for (int r = 0; r < 4 + 2 * R; r++)
+        for (int j = 0; j < 4; j++) ctr[NWIN - 1][j] = d[j];
+        if (kGauss) {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 float acc = 0.0f;
 #pragma unroll
-                for (int q = 0; q <= 2 * R; q++) acc = slm_fma(p.w[q], e[r][j + q], acc);
-                h[r][j] = acc;
+                for (int q = 0; q <= 2 * R; q++) acc = slm_fma(p.w[q], e[j + q], acc);
+                hwin[NWIN - 1][j] = acc;
             }
-    }
-    const int x = x0 + c0;
+        } else {
 #pragma unroll
-    for (int o = 0; o < 4; o++) {
-        const int y = y0 + ry + o;
+            for (int j = 0; j < 4 + 2 * R; j++) win[NWIN - 1][j] = e[j];
+        }
+        if (r < 2 * R) continue;
+        const int y = y0 + ry + r - 2 * R;
         if (y >= H || x >= W) continue;
         float res[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const float center = e[o + R][R + j];
+            const float center = ctr[R][j];
             float blur;
             if (kGauss) {
                 float acc = 0.0f;
 #pragma unroll
-                for (int q = 0; q <= 2 * R; q++) acc = slm_fma(p.w[q], h[o + q][j], acc);
+                for (int q = 0; q <= 2 * R; q++) acc = slm_fma(p.w[q], hwin[q][j], acc);
                 blur = acc;
             } else {
                 float sum = 0.0f;
 #pragma unroll
                 for (int dy = 0; dy < 3; dy++)
 #pragma unroll
-                    for (int dx = 0; dx < 3; dx++) sum = slm_add(sum, e[o + dy][j + dx]);
+                    for (int dx = 0; dx < 3; dx++) sum = slm_add(sum, win[dy][j + dx]);
                 blur = slm_div(sum, 9.0f);
             }
             res[j] = slm_mix(center, blur, p.rate);
@@ -211,8 +271,8 @@ __global__ void __launch_bounds__(kTmaThreads) trail_tma_kernel(const __grid_con
 template <int R, bool kGauss, int kDecay, class D>
 cudaError_t launch_tma_k(const DevParams& p, const TrailMaps& maps, int cur, const float* in, const D* din,
                          float* out, D* dz, cudaStream_t s, const cudaAccessPolicyWindow* win, bool pdl) {
-    constexpr int WR = kTmaRows + 2 * R;
-    const size_t smem = 128 + sizeof(float) * WR * kTrailBoxCols + sizeof(D) * WR * DepBox<D>::cols;
+    typedef Layout<R, D> L;
+    const size_t smem = L::bytes;
     // the maps' box height is the window's: 34 rows for radius 1, 36 for 2
     const CUtensorMap& mt = R == 1 ? maps.trail[cur] : maps.trail_r2[cur];
     const CUtensorMap& md = sizeof(D) == 1 ? (R == 1 ? maps.marks[cur] : maps.marks_r2[cur])
@@ -272,14 +332,15 @@ bool encode_2d(CUtensorMap* map, const void* base, CUtensorMapDataType type, siz
 
 bool trail_tma_supported(const DevParams& p) {
     const int R = p.blur_mode == SLIME_BLUR_GAUSS ? p.R : 1;
-    // byte-mark rows must be whole 16-byte units for a tensor map
-    return p.W % 16 == 0 && p.W >= 16 && p.H >= 1 && R >= 1 && R <= 2;
+    // byte-mark rows must be whole 16-byte units for a tensor map, and the
+    // boxes (160 columns of marks, 36 rows) no larger than the array
+    return p.W % 16 == 0 && p.W >= kMarkBoxCols && p.H >= kTmaRows + 4 && R >= 1 && R <= 2;
 }
 
 bool make_trail_maps(TrailMaps* m, const float* const trail[2], const uint32_t* const counts[2],
                      const uint8_t* const marks[2], uint32_t W, uint32_t H) {
     m->ok = false;
-    if (W % 16 != 0 || W < 16) return false;
+    if (W % 16 != 0 || W < (uint32_t)kMarkBoxCols || H < (uint32_t)kTmaRows + 4) return false;
     // one set of maps per blur radius: the box is the window, 32 rows plus a
     // halo of R on each side
     for (int i = 0; i < 2; i++) {
@@ -310,6 +371,15 @@ cudaError_t launch_trail_tma_marks(const DevParams& p, const TrailMaps& maps, in
                                    const uint8_t* marks_in, float* out, uint8_t* marks_zero, cudaStream_t s,
                                    const cudaAccessPolicyWindow* win, bool pdl) {
     return launch_tma<uint8_t>(p, maps, cur, in, marks_in, out, marks_zero, s, win, pdl);
+}
+
+int trail_tma_misaligned_blocks() {
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tma_misaligned, sizeof v) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return v;
 }
 
 bool trail_tma_take_error() {

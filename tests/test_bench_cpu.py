@@ -20,6 +20,7 @@ def test_every_agent_shape_has_a_kernel_name():
     assert names.count("agents_persistent_kernel") == 5
     assert set(names) == {"agents_kernel", "agents_persistent_kernel"}
     assert bench.trail_kernel_name(7, 1) == bench.trail_kernel_name(9, 0) == "trail_stream_kernel"
+    assert bench.trail_kernel_name(10, 1) == "trail_tma_kernel"
     assert bench.trail_kernel_name(3, 1) == "trail_gauss_kernel"
     assert bench.trail_kernel_name(3, 0) == "trail_box3_kernel"
 

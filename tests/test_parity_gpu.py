@@ -653,14 +653,15 @@ def test_deposit_marks_only_when_every_deposit_saturates(gpu):
         sim.download_deposit_counts()
 
 
-@pytest.mark.parametrize("W,H", [(1024, 512), (4096, 64), (528, 97), (160, 34)])
+@pytest.mark.parametrize("W,H", [(1024, 512), (4096, 64), (528, 97), (272, 66)])
 def test_tensor_copy_trail_tile(gpu, W, H):
     """The trail pass whose input window arrives by 2-D tensor copies (one
     box of trail and one of deposit record per 128 x 32 tile, the border tiles
     by wrapped loads): bit for bit the oracle over several steps, with byte
     marks and with 32-bit counts, box blur and Gaussian radius 1 and 2, both
-    decays.  160 x 34 is the smallest grid with an interior tile at radius 1
-    (a 16-column margin of byte marks on each side and one halo row)."""
+    decays.  272 x 66 is the smallest grid with an interior tile (a 16-column
+    margin of byte marks on each side of a 128-column tile, and its halo rows);
+    4096 x 64 has border tiles only."""
     n = W * H // 2
     for blur_mode, radius, decay_mode, decay in ((0, 1.0, 0, 10.0), (1, 1.0, 1, 0.97), (1, 2.0, 1, 0.9),
                                                  (1, 1.0, 0, 3.0)):
