@@ -264,6 +264,11 @@ int slime_set_steps_done(slime_ctx* ctx, uint64_t steps_done);
  * diffuse dispatch of src/main.rs:1163-1235, n_steps times.  Asynchronous with
  * respect to the host; use slime_sync or any download to wait. */
 int slime_step(slime_ctx* ctx, uint32_t n_steps);
+/* Capture now the CUDA graphs that the next n_steps steps will replay (the
+ * same chunks slime_step cuts), without stepping: the first slime_step over
+ * them then only replays.  Graphs stay valid until a parameter, option or
+ * buffer change (or the first reorder, which adds the id buffer) drops them. */
+int slime_prepare_steps(slime_ctx* ctx, uint32_t n_steps);
 int slime_sync(slime_ctx* ctx);
 /* The cudaStream_t the context enqueues on. */
 int slime_get_stream(slime_ctx* ctx, void** stream);
@@ -340,9 +345,30 @@ int slime_ensemble_download_trail(slime_ensemble* ens, uint32_t colony, float* t
  * results do not change, only the memory order of the agents. */
 int slime_ensemble_set_reorder(slime_ensemble* ens, uint32_t every, uint32_t cell_log2);
 int slime_ensemble_step(slime_ensemble* ens, uint32_t n_steps);
+/* As slime_prepare_steps: capture the graphs of the next n_steps steps now. */
+int slime_ensemble_prepare_steps(slime_ensemble* ens, uint32_t n_steps);
 int slime_ensemble_sync(slime_ensemble* ens);
 int slime_ensemble_get_stream(slime_ensemble* ens, void** stream);
 int slime_ensemble_autotune(slime_ensemble* ens, uint32_t reps);
+/* Engines of slime_ensemble_step (slime_ensemble_autotune times both):
+ * COOPERATIVE - one cooperative persistent launch per step (all colonies'
+ *   agents, a bounded grid barrier, all colonies' trail strips);
+ * LANES - each colony's steps as a chain of the single-colony kernels on one
+ *   of up to 64 lanes forked from the ensemble's stream, one CUDA graph per
+ *   chunk of steps, so that the colonies' chains run concurrently. */
+#define SLIME_ENSEMBLE_COOPERATIVE 0u
+#define SLIME_ENSEMBLE_LANES 1u
+/* Choose the engine by hand; for LANES also the agent-kernel shape and trail
+ * tile (indices of the single-colony tables; the tensor-copy tile is not
+ * available here).  Results do not change. */
+int slime_ensemble_set_engine(slime_ensemble* ens, uint32_t engine, uint32_t lane_agent_shape,
+                              uint32_t lane_trail_tile);
+/* Choose the cooperative step's launch shape by hand (what slime_ensemble_autotune picks
+ * by timing): trail rows per strip item (8, 16 or 32), resident blocks per SM
+ * (0 = as many as fit, else 1..4) and agents per thread of the agent phase
+ * (4: each stepped alone; 2: stepped as one pair).  Results do not change. */
+int slime_ensemble_set_shape(slime_ensemble* ens, uint32_t strip_rows, uint32_t blocks_per_sm,
+                             uint32_t agents_per_thread);
 /* Total kernels enqueued so far. */
 int slime_ensemble_launch_count(const slime_ensemble* ens, uint64_t* out);
 typedef struct SlimeEnsembleInfo {
@@ -356,6 +382,13 @@ typedef struct SlimeEnsembleInfo {
     uint64_t total_cells;
     uint32_t grid_blocks;   /* blocks of the persistent launch (a multiple of the SM count) */
     uint32_t strip_rows;    /* trail rows per strip work item (autotuned) */
+    uint32_t agents_per_thread; /* cooperative engine: agents a thread steps per agent work item, 4
+                                   (each alone) or 2 (as one pair); autotuned */
+    uint32_t engine;            /* SLIME_ENSEMBLE_COOPERATIVE or SLIME_ENSEMBLE_LANES */
+    uint32_t lanes;             /* capture lanes of the lanes engine (0 until it first steps) */
+    uint32_t lane_agent_shape;  /* lanes engine: agent-kernel shape (slime_set_agent_shape's table) */
+    uint32_t lane_trail_tile;   /* lanes engine: trail tile (slime_set_trail_tile's table) */
+    uint32_t reserved;
 } SlimeEnsembleInfo;
 int slime_ensemble_get_info(const slime_ensemble* ens, SlimeEnsembleInfo* out);
 /* Failure-detection self-test: runs one block at the ensemble's grid barrier

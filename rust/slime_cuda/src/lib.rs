@@ -43,6 +43,8 @@ pub mod ffi {
     pub const SLIME_DISPATCH_REFERENCE: u32 = 1;
     pub const SLIME_SENSOR_SHADER: u32 = 0;
     pub const SLIME_SENSOR_ROTATED: u32 = 1;
+    pub const SLIME_ENSEMBLE_COOPERATIVE: u32 = 0;
+    pub const SLIME_ENSEMBLE_LANES: u32 = 1;
 
     /// `SimSizeUniform` (src/main.rs:29-46) in its first 14 fields, then the
     /// constants the shader hard-codes and the engine's modes.
@@ -146,6 +148,12 @@ pub mod ffi {
         pub total_cells: u64,
         pub grid_blocks: u32,
         pub strip_rows: u32,
+        pub agents_per_thread: u32,
+        pub engine: u32,
+        pub lanes: u32,
+        pub lane_agent_shape: u32,
+        pub lane_trail_tile: u32,
+        pub reserved: u32,
     }
 
     #[repr(C)]
@@ -194,6 +202,7 @@ pub mod ffi {
         pub fn slime_state_load(ctx: *mut slime_ctx, path: *const c_char) -> c_int;
         pub fn slime_set_steps_done(ctx: *mut slime_ctx, steps_done: u64) -> c_int;
         pub fn slime_step(ctx: *mut slime_ctx, n_steps: u32) -> c_int;
+        pub fn slime_prepare_steps(ctx: *mut slime_ctx, n_steps: u32) -> c_int;
         pub fn slime_sync(ctx: *mut slime_ctx) -> c_int;
         pub fn slime_get_stream(ctx: *mut slime_ctx, stream: *mut *mut c_void) -> c_int;
         pub fn slime_download_trail_async(ctx: *mut slime_ctx, trail: *mut f32, n_cells: u64) -> c_int;
@@ -221,9 +230,22 @@ pub mod ffi {
         pub fn slime_ensemble_download_trail(ens: *mut slime_ensemble, colony: u32, trail: *mut f32, n_cells: u64) -> c_int;
         pub fn slime_ensemble_set_reorder(ens: *mut slime_ensemble, every: u32, cell_log2: u32) -> c_int;
         pub fn slime_ensemble_step(ens: *mut slime_ensemble, n_steps: u32) -> c_int;
+        pub fn slime_ensemble_prepare_steps(ens: *mut slime_ensemble, n_steps: u32) -> c_int;
         pub fn slime_ensemble_sync(ens: *mut slime_ensemble) -> c_int;
         pub fn slime_ensemble_get_stream(ens: *mut slime_ensemble, stream: *mut *mut c_void) -> c_int;
         pub fn slime_ensemble_autotune(ens: *mut slime_ensemble, reps: u32) -> c_int;
+        pub fn slime_ensemble_set_engine(
+            ens: *mut slime_ensemble,
+            engine: u32,
+            lane_agent_shape: u32,
+            lane_trail_tile: u32,
+        ) -> c_int;
+        pub fn slime_ensemble_set_shape(
+            ens: *mut slime_ensemble,
+            strip_rows: u32,
+            blocks_per_sm: u32,
+            agents_per_thread: u32,
+        ) -> c_int;
         pub fn slime_ensemble_launch_count(ens: *const slime_ensemble, out: *mut u64) -> c_int;
         pub fn slime_ensemble_get_info(ens: *const slime_ensemble, out: *mut SlimeEnsembleInfo) -> c_int;
         pub fn slime_ensemble_selftest_barrier_timeout(ens: *mut slime_ensemble) -> c_int;
@@ -539,6 +561,10 @@ impl Simulation {
     pub fn step(&mut self, n_steps: u32) -> Result<()> {
         self.check(unsafe { ffi::slime_step(self.ctx, n_steps) })
     }
+    /// Capture the CUDA graphs the next `n_steps` steps replay, without stepping.
+    pub fn prepare_steps(&mut self, n_steps: u32) -> Result<()> {
+        self.check(unsafe { ffi::slime_prepare_steps(self.ctx, n_steps) })
+    }
     pub fn sync(&mut self) -> Result<()> {
         self.check(unsafe { ffi::slime_sync(self.ctx) })
     }
@@ -753,6 +779,9 @@ impl Ensemble {
     pub fn step(&mut self, n_steps: u32) -> Result<()> {
         self.check(unsafe { ffi::slime_ensemble_step(self.ens, n_steps) })
     }
+    pub fn prepare_steps(&mut self, n_steps: u32) -> Result<()> {
+        self.check(unsafe { ffi::slime_ensemble_prepare_steps(self.ens, n_steps) })
+    }
     pub fn sync(&mut self) -> Result<()> {
         self.check(unsafe { ffi::slime_ensemble_sync(self.ens) })
     }
@@ -763,6 +792,16 @@ impl Ensemble {
     }
     pub fn autotune(&mut self, reps: u32) -> Result<()> {
         self.check(unsafe { ffi::slime_ensemble_autotune(self.ens, reps) })
+    }
+    /// Engine by hand (`SLIME_ENSEMBLE_COOPERATIVE` / `SLIME_ENSEMBLE_LANES`),
+    /// with the lanes engine's agent shape and trail tile.
+    pub fn set_engine(&mut self, engine: u32, lane_agent_shape: u32, lane_trail_tile: u32) -> Result<()> {
+        self.check(unsafe { ffi::slime_ensemble_set_engine(self.ens, engine, lane_agent_shape, lane_trail_tile) })
+    }
+    /// Cooperative launch shape by hand: strip rows (8, 16, 32), blocks per SM (0 = all
+    /// that fit), agents per thread (4 or 2).
+    pub fn set_shape(&mut self, strip_rows: u32, blocks_per_sm: u32, agents_per_thread: u32) -> Result<()> {
+        self.check(unsafe { ffi::slime_ensemble_set_shape(self.ens, strip_rows, blocks_per_sm, agents_per_thread) })
     }
     pub fn launch_count(&self) -> Result<u64> {
         let mut v = 0u64;
@@ -844,7 +883,7 @@ mod tests {
         assert_eq!(std::mem::size_of::<SlimeOptions>(), 32);
         assert_eq!(std::mem::size_of::<SlimeInfo>(), 72);
         assert_eq!(std::mem::size_of::<SlimeGrads>(), 32);
-        assert_eq!(std::mem::size_of::<SlimeEnsembleInfo>(), 48);
+        assert_eq!(std::mem::size_of::<SlimeEnsembleInfo>(), 72);
     }
 
     #[test]

@@ -501,7 +501,9 @@ int run_steps_direct(slime_ctx* ctx, uint32_t m, bool marks) {
     return SLIME_OK;
 }
 
-int run_steps_graph(slime_ctx* ctx, uint32_t m, bool marks) {
+// The graph of m steps from the current parity with this deposit record,
+// captured on first use.
+int step_graph(slime_ctx* ctx, uint32_t m, bool marks, cudaGraphExec_t* out) {
     auto key = std::make_pair(m, ctx->cur | (marks ? 2 : 0));
     auto it = ctx->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
@@ -525,6 +527,14 @@ int run_steps_graph(slime_ctx* ctx, uint32_t m, bool marks) {
     } else {
         exec = it->second;
     }
+    *out = exec;
+    return SLIME_OK;
+}
+
+int run_steps_graph(slime_ctx* ctx, uint32_t m, bool marks) {
+    cudaGraphExec_t exec = nullptr;
+    int rc = step_graph(ctx, m, marks, &exec);
+    if (rc != SLIME_OK) return rc;
     CK(cudaGraphLaunch(exec, ctx->stream), "launching step graph");
     ctx->cur = (m & 1) ? 1 - ctx->cur : ctx->cur;
     ctx->launches += kernels_per_step(ctx, marks) * m;
@@ -637,6 +647,32 @@ int ensure_dispatch_order(slime_ctx* ctx) {
     if (ctx->dev.dispatch_mode != SLIME_DISPATCH_REFERENCE || !ctx->reordered || ctx->reorder_partitioned)
         return SLIME_OK;
     return do_reorder(ctx);
+}
+
+// Capture the graphs that the next n steps replay (same chunking as
+// run_steps: graph_chunk steps, cut at reorder boundaries), without stepping.
+int prepare_steps(slime_ctx* ctx, uint32_t n) {
+    if (!ctx->opt.use_graphs || ctx->agents.n == 0) return SLIME_OK;
+    const bool marks = use_marks(ctx);
+    const uint32_t chunk = ctx->opt.graph_chunk ? ctx->opt.graph_chunk : 50;
+    const int saved = ctx->cur;
+    uint64_t steps = ctx->steps_done;
+    int rc = SLIME_OK;
+    while (n > 0 && rc == SLIME_OK) {
+        uint32_t m = n;
+        if (ctx->opt.reorder_every) {
+            uint64_t to_next = ctx->opt.reorder_every - steps % ctx->opt.reorder_every;
+            if (to_next < m) m = (uint32_t)to_next;
+        }
+        const uint32_t take = m < chunk ? m : chunk;
+        cudaGraphExec_t exec = nullptr;
+        rc = step_graph(ctx, take, marks, &exec);
+        if (take & 1) ctx->cur = 1 - ctx->cur;
+        steps += take;
+        n -= take;
+    }
+    ctx->cur = saved;
+    return rc;
 }
 
 int run_steps(slime_ctx* ctx, uint32_t n) {
@@ -1056,6 +1092,12 @@ int slime_state_load(slime_ctx* ctx, const char* path) {
     if ((rc = slime_upload_agents(ctx, agents.data(), h.n_agents)) != SLIME_OK) return rc;
     if ((rc = slime_upload_trail(ctx, trail.data(), cells)) != SLIME_OK) return rc;
     return slime_set_steps_done(ctx, h.steps_done);
+}
+
+int slime_prepare_steps(slime_ctx* ctx, uint32_t n_steps) {
+    if (!ctx) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    return prepare_steps(ctx, n_steps);
 }
 
 int slime_step(slime_ctx* ctx, uint32_t n_steps) {

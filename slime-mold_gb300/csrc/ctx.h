@@ -123,6 +123,7 @@ uint64_t kernels_per_step(const slime_ctx* ctx, bool marks);
 // the agents it updates first.
 int ensure_dispatch_order(slime_ctx* ctx);
 int run_steps(slime_ctx* ctx, uint32_t n);
+int prepare_steps(slime_ctx* ctx, uint32_t n);
 void free_adjoint(slime_ctx* ctx);
 void setup_l2(slime_ctx* ctx);
 constexpr unsigned kWindowAgents = 1, kWindowTrail = 2;

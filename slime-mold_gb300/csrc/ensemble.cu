@@ -1,15 +1,25 @@
-// ensemble.cu - independent colonies of uneven sizes in one persistent launch
-// per step.
+// ensemble.cu - independent colonies of uneven sizes stepped together.
 //
 // All colonies' agents live in one SoA block (each colony padded to a
 // multiple of 128 slots) and all trails/counts in one ping-pong pair of
-// buffers.  One cooperative launch per step runs
-//   phase 1: agent work items (1,024 agents of one colony per block item),
+// buffers.  Two engines step them (the autotuner times both):
+//
+// SLIME_ENSEMBLE_COOPERATIVE - one cooperative launch per step runs
+//   phase 1: agent work items (256 groups of 4 or 2 agents of one colony
+//            per block item),
 //   a grid-wide barrier (bounded spin: gives up after about a second and
 //            reports SLIME_ERR_DEVICE_TIMEOUT instead of hanging),
 //   phase 2: trail strips (128 columns x ROWS rows of one colony per warp
 //            item) through the same streaming code as the single-colony
 //            kernel.
+// SLIME_ENSEMBLE_LANES - every colony's steps are a chain of the
+//   single-colony kernels (persistent agent pass, streaming trail pass, PDL
+//   between them, the colony's parameters as kernel arguments) on one of up
+//   to 64 capture lanes; the lanes fork from and join the ensemble's stream
+//   and a chunk of steps is captured as one CUDA graph, so the chains of
+//   different colonies run concurrently: small colonies fill the SMs that a
+//   large colony's pass leaves idle, and the trail passes (memory-bound)
+//   overlap the agent passes (issue-bound) of other colonies.
 // Each colony keeps its own parameter block, so the colonies are exactly the
 // runs a single Simulation would produce for them (the tests compare bit for
 // bit).  The blur mode and radius must be common to all colonies (they select
@@ -17,6 +27,7 @@
 // parameters may differ.
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -114,41 +125,39 @@ __device__ __forceinline__ void steps4(const DevParams& sp, float4& x, float4& y
     }
 }
 
-// Four blocks per SM (64 registers, a few bytes spilled by the strip phase):
-// 3.33 ms per step on 64 colonies against 3.49 with the three blocks that the
-// uncapped register use allows; two agents per thread instead of four were
-// slower again (3.44 ms).
-template <int R, bool kGauss, int ROWS>
-__global__ void __launch_bounds__(kEnsThreads, 4) ensemble_step_kernel(
-    const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
-    const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
-    float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS, const float* __restrict__ trail_in,
-    uint32_t* counts_in, float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar,
-    int parity) {
-    __shared__ DevParams sp;
-    // ---- phase 1: agents
-    for (uint32_t item = blockIdx.x; item < n_agent_items; item += gridDim.x) {
-        const uint2 it = agent_items[item];
-        __syncthreads();
-        {
-            const uint32_t* src = reinterpret_cast<const uint32_t*>(&cols[it.x].p);
-            uint32_t* dst = reinterpret_cast<uint32_t*>(&sp);
-            for (int w = threadIdx.x; w < (int)(sizeof(DevParams) / 4); w += kEnsThreads) dst[w] = src[w];
-        }
-        __syncthreads();
-        const DevColony& c = cols[it.x];
-        const uint64_t g = (uint64_t)it.y + threadIdx.x; // float4 group within the colony
-        const uint64_t base = 4 * g;
-        if (base >= c.n) continue;
-        const uint64_t slot = c.agent_off + base;
+// Two consecutive agents of one colony stepped as one pair (agent_step2), or
+// the first alone when the second is past the colony's end.
+template <class Trail>
+__device__ __forceinline__ void steps2(const DevParams& sp, float2& x, float2& y, float2& th, float2& v, const uint2& id,
+                                       uint64_t base, uint64_t n, const Trail& trail, int& c0, int& c1) {
+    if (base + 2 <= n) {
+        agent_step2(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, x.y, y.y, th.y, v.y, (int32_t)id.y, trail, c0, c1);
+    } else {
+        c0 = agent_step(sp, x.x, y.x, th.x, v.x, (int32_t)id.x, trail);
+    }
+}
+
+// One agent work item of a block: APT consecutive agents of one colony per
+// thread (APT = 4: float4 accesses, each agent stepped alone; APT = 2: float2
+// accesses, the two stepped as one pair).
+template <int APT>
+__device__ __forceinline__ void agent_item(const DevParams& sp, const DevColony& c, uint32_t g0, int parity,
+                                           float* __restrict__ X, float* __restrict__ Y, float* __restrict__ TH,
+                                           float* __restrict__ V, const uint32_t* __restrict__ IDS,
+                                           const float* __restrict__ trail_in, uint32_t* counts_in) {
+    const uint64_t g = (uint64_t)g0 + threadIdx.x; // APT-agent group within the colony
+    const uint64_t base = APT * g;
+    if (base >= c.n) return;
+    const uint64_t slot = c.agent_off + base;
+    uint32_t* counts = counts_in + c.trail_off;
+    const cudaTextureObject_t tex = c.tex[parity];
+    if (APT == 4) {
         float4* px = reinterpret_cast<float4*>(X + slot);
         float4* py = reinterpret_cast<float4*>(Y + slot);
         float4* pt = reinterpret_cast<float4*>(TH + slot);
         float4* pv = reinterpret_cast<float4*>(V + slot);
         float4 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
         const uint4 id = __ldcs(reinterpret_cast<const uint4*>(IDS + slot)); // colony-local agent ids
-        uint32_t* counts = counts_in + c.trail_off;
-        const cudaTextureObject_t tex = c.tex[parity];
         int c0, c1 = -1, c2 = -1, c3 = -1;
         // the colony's trail through its gather texture when it has one,
         // else through the padded buffer (block-uniform choice)
@@ -165,6 +174,50 @@ __global__ void __launch_bounds__(kEnsThreads, 4) ensemble_step_kernel(
         __stcs(py, y);
         __stcs(pt, th);
         __stcs(pv, v);
+    } else {
+        float2* px = reinterpret_cast<float2*>(X + slot);
+        float2* py = reinterpret_cast<float2*>(Y + slot);
+        float2* pt = reinterpret_cast<float2*>(TH + slot);
+        float2* pv = reinterpret_cast<float2*>(V + slot);
+        float2 x = __ldcs(px), y = __ldcs(py), th = __ldcs(pt), v = __ldcs(pv);
+        const uint2 id = __ldcs(reinterpret_cast<const uint2*>(IDS + slot));
+        int c0, c1 = -1;
+        if (tex) {
+            steps2(sp, x, y, th, v, id, base, c.n, TrailTex{tex}, c0, c1);
+        } else {
+            steps2(sp, x, y, th, v, id, base, c.n, TrailPtr{trail_in + c.trail_off}, c0, c1);
+        }
+        if (c0 >= 0) atomicAdd(counts + c0, 1u);
+        if (c1 >= 0) atomicAdd(counts + c1, 1u);
+        __stcs(px, x);
+        __stcs(py, y);
+        __stcs(pt, th);
+        __stcs(pv, v);
+    }
+}
+
+// Four agents per thread at four blocks per SM (a 64-register cap; a few
+// bytes spilled), or two per thread stepped as one pair at three blocks per
+// SM (80 registers): the autotuner times both.
+template <int R, bool kGauss, int ROWS, int APT>
+__global__ void __launch_bounds__(kEnsThreads, APT == 4 ? 4 : 3) ensemble_step_kernel(
+    const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
+    const uint4* __restrict__ strip_items, uint32_t n_strip_items, float* __restrict__ X, float* __restrict__ Y,
+    float* __restrict__ TH, float* __restrict__ V, const uint32_t* __restrict__ IDS, const float* __restrict__ trail_in,
+    uint32_t* counts_in, float* __restrict__ trail_out, uint32_t* __restrict__ counts_zero, GridBarrier* bar,
+    int parity) {
+    __shared__ DevParams sp;
+    // ---- phase 1: agents
+    for (uint32_t item = blockIdx.x; item < n_agent_items; item += gridDim.x) {
+        const uint2 it = agent_items[item];
+        __syncthreads();
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(&cols[it.x].p);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&sp);
+            for (int w = threadIdx.x; w < (int)(sizeof(DevParams) / 4); w += kEnsThreads) dst[w] = src[w];
+        }
+        __syncthreads();
+        agent_item<APT>(sp, cols[it.x], it.y, parity, X, Y, TH, V, IDS, trail_in, counts_in);
     }
     // ---- grid-wide barrier: all deposits of this step are counted
     __threadfence();
@@ -184,19 +237,24 @@ __global__ void __launch_bounds__(kEnsThreads, 4) ensemble_step_kernel(
 typedef void (*EnsKernel)(const DevColony*, const uint2*, uint32_t, const uint4*, uint32_t, float*, float*, float*,
                           float*, const uint32_t*, const float*, uint32_t*, float*, uint32_t*, GridBarrier*, int);
 
-template <int ROWS>
+template <int ROWS, int APT>
 EnsKernel pick_rows(int R, bool gauss) {
-    if (!gauss) return ensemble_step_kernel<1, false, ROWS>;
-    if (R == 1) return ensemble_step_kernel<1, true, ROWS>;
-    return ensemble_step_kernel<2, true, ROWS>;
+    if (!gauss) return ensemble_step_kernel<1, false, ROWS, APT>;
+    if (R == 1) return ensemble_step_kernel<1, true, ROWS, APT>;
+    return ensemble_step_kernel<2, true, ROWS, APT>;
 }
 
-EnsKernel pick_kernel(int rows, int R, bool gauss) {
+template <int APT>
+EnsKernel pick_apt(int rows, int R, bool gauss) {
     switch (rows) {
-    case 8: return pick_rows<8>(R, gauss);
-    case 32: return pick_rows<32>(R, gauss);
-    default: return pick_rows<16>(R, gauss);
+    case 8: return pick_rows<8, APT>(R, gauss);
+    case 32: return pick_rows<32, APT>(R, gauss);
+    default: return pick_rows<16, APT>(R, gauss);
     }
+}
+
+EnsKernel pick_kernel(int rows, int R, bool gauss, int apt) {
+    return apt == 2 ? pick_apt<2>(rows, R, gauss) : pick_apt<4>(rows, R, gauss);
 }
 
 } // namespace
@@ -225,12 +283,20 @@ struct slime_ensemble {
     float4* staging = nullptr;
     size_t staging_bytes = 0;
     int rows = 16;
+    int apt = 4; // agents per thread of the agent phase (4 or 2)
     int R = 1;
     bool gauss = false;
     int grid = 0;
     int blocks_per_sm = 0;
     bool use_graphs = true;
     bool last_chunk_graph = false; // the last chunk of steps replayed a graph
+    int engine = SLIME_ENSEMBLE_COOPERATIVE;
+    int lane_agent_shape = 13; // agent-kernel shape of the lanes engine (persistent, texture gather)
+    int lane_trail_tile = 8;   // trail tile of the lanes engine (streaming, 16-row strips)
+    std::vector<cudaStream_t> lanes;
+    std::vector<cudaEvent_t> lane_ev;
+    cudaEvent_t fork_ev = nullptr;
+    std::vector<std::vector<uint32_t>> lane_cols; // colonies of each lane, in launch order
     std::map<std::pair<uint32_t, int>, cudaGraphExec_t> graphs;
     uint64_t launches = 0;
     std::string err;
@@ -290,8 +356,26 @@ int build_strip_items(slime_ensemble* e) {
     return SLIME_OK;
 }
 
+// Agent work items: 256 groups of `apt` agents of one colony each.
+int build_agent_items(slime_ensemble* e) {
+    std::vector<uint2> ai;
+    for (uint32_t j = 0; j < (uint32_t)e->colonies.size(); j++) {
+        const uint64_t groups = (e->colonies[j].n + e->apt - 1) / e->apt;
+        for (uint64_t g0 = 0; g0 < groups; g0 += kEnsThreads) ai.push_back(make_uint2(j, (uint32_t)g0));
+    }
+    if (e->d_agent_items) dev_free(e->d_agent_items);
+    e->d_agent_items = nullptr;
+    e->n_agent_items = 0;
+    ECK(dev_alloc((void**)&e->d_agent_items, (ai.size() ? ai.size() : 1) * sizeof(uint2)), "allocating agent items");
+    if (ai.size())
+        ECK(cudaMemcpy(e->d_agent_items, ai.data(), ai.size() * sizeof(uint2), cudaMemcpyHostToDevice),
+            "uploading agent items");
+    e->n_agent_items = (uint32_t)ai.size();
+    return SLIME_OK;
+}
+
 int size_grid(slime_ensemble* e) {
-    EnsKernel k = pick_kernel(e->rows, e->R, e->gauss);
+    EnsKernel k = pick_kernel(e->rows, e->R, e->gauss, e->apt);
     int per_sm = 0, sms = 0;
     ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEnsThreads, 0), "occupancy query");
     ECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device), "SM count");
@@ -303,7 +387,7 @@ int size_grid(slime_ensemble* e) {
 
 cudaError_t enqueue_ens_step(slime_ensemble* e) {
     const int cur = e->cur;
-    EnsKernel k = pick_kernel(e->rows, e->R, e->gauss);
+    EnsKernel k = pick_kernel(e->rows, e->R, e->gauss, e->apt);
     float* X = e->agent_block;
     float* Y = X + e->total_slots;
     float* TH = Y + e->total_slots;
@@ -350,6 +434,95 @@ AgentsSoA colony_soa(slime_ensemble* e, const Colony& c) {
     return a;
 }
 
+constexpr size_t kMaxLanes = 64;
+
+// Lanes and their colonies: the colonies by descending work (agents plus a
+// quarter of the cells), each onto the lane with the least work so far.
+int ensure_lanes(slime_ensemble* e) {
+    if (!e->lanes.empty()) return SLIME_OK;
+    const size_t k = e->colonies.size();
+    const size_t nl = k < kMaxLanes ? k : kMaxLanes;
+    ECK(cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming), "creating lane events");
+    for (size_t l = 0; l < nl; l++) {
+        cudaStream_t s = nullptr;
+        cudaEvent_t ev = nullptr;
+        ECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "creating lanes");
+        e->lanes.push_back(s);
+        ECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "creating lane events");
+        e->lane_ev.push_back(ev);
+    }
+    std::vector<uint32_t> order(k);
+    for (size_t j = 0; j < k; j++) order[j] = (uint32_t)j;
+    auto work = [&](uint32_t j) {
+        const Colony& c = e->colonies[j];
+        return c.n + (uint64_t)c.W * c.H / 4;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return work(a) > work(b); });
+    e->lane_cols.assign(nl, {});
+    std::vector<uint64_t> load(nl, 0);
+    for (uint32_t j : order) {
+        size_t best = 0;
+        for (size_t l = 1; l < nl; l++)
+            if (load[l] < load[best]) best = l;
+        e->lane_cols[best].push_back(j);
+        load[best] += work(j);
+    }
+    return SLIME_OK;
+}
+
+void destroy_lanes(slime_ensemble* e) {
+    for (cudaStream_t s : e->lanes) cudaStreamDestroy(s);
+    for (cudaEvent_t ev : e->lane_ev) cudaEventDestroy(ev);
+    if (e->fork_ev) cudaEventDestroy(e->fork_ev);
+    e->lanes.clear();
+    e->lane_ev.clear();
+    e->fork_ev = nullptr;
+    e->lane_cols.clear();
+}
+
+// Kernels one lanes-engine step enqueues.
+uint64_t lane_kernels_per_step(const slime_ensemble* e) {
+    uint64_t k = 0;
+    for (const Colony& c : e->colonies) k += 1 + (uint64_t)agent_pass_kernels(c.dev, c.n, false);
+    return k;
+}
+
+// m steps of every colony on the lanes (fork from the ensemble's stream,
+// join back into it); flips e->cur when m is odd, as m cooperative steps do.
+cudaError_t enqueue_lane_steps(slime_ensemble* e, uint32_t m) {
+    cudaError_t ce = cudaEventRecord(e->fork_ev, e->stream);
+    const bool tex_shape = agent_shape_uses_texture(e->lane_agent_shape);
+    for (size_t l = 0; l < e->lanes.size() && ce == cudaSuccess; l++) {
+        cudaStream_t s = e->lanes[l];
+        if ((ce = cudaStreamWaitEvent(s, e->fork_ev, 0)) != cudaSuccess) break;
+        bool after_kernel = false; // PDL only behind a kernel of this lane
+        for (uint32_t j : e->lane_cols[l]) {
+            const Colony& c = e->colonies[j];
+            AgentsSoA a = colony_soa(e, c);
+            int cur = e->cur;
+            for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) {
+                float* tin = e->trail[cur] + c.trail_off;
+                uint32_t* cin = e->counts[cur] + c.trail_off;
+                if (c.n) {
+                    ce = launch_agents(c.dev, a, tin, cin, s, e->lane_agent_shape, nullptr, tex_shape ? c.tex[cur] : 0,
+                                       nullptr, after_kernel);
+                    after_kernel = true;
+                    if (ce != cudaSuccess) break;
+                }
+                ce = launch_trail(c.dev, e->lane_trail_tile, tin, cin, e->trail[1 - cur] + c.trail_off,
+                                  e->counts[1 - cur] + c.trail_off, s, nullptr, after_kernel);
+                after_kernel = true;
+                cur = 1 - cur;
+            }
+            if (ce != cudaSuccess) break;
+        }
+        if (ce == cudaSuccess) ce = cudaEventRecord(e->lane_ev[l], s);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->lane_ev[l], 0);
+    }
+    if (ce == cudaSuccess && (m & 1)) e->cur = 1 - e->cur;
+    return ce;
+}
+
 // Morton-reorder every colony's slots (results are unchanged: each slot keeps
 // its colony-local id).
 int reorder_all(slime_ensemble* e) {
@@ -375,10 +548,64 @@ int check_barrier(slime_ensemble* e) {
     return SLIME_OK;
 }
 
-int run_ens_steps(slime_ensemble* e, uint32_t n) {
-    const uint32_t chunk = 50;
+// The graph of m steps of the current engine from the current parity,
+// captured on first use; null when the capture fails (the caller then
+// launches directly).
+cudaGraphExec_t chunk_graph(slime_ensemble* e, uint32_t m) {
+    auto key = std::make_pair(m, e->cur);
+    auto it = e->graphs.find(key);
+    if (it != e->graphs.end()) return it->second;
+    const int saved = e->cur;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+    if (e->engine == SLIME_ENSEMBLE_LANES) {
+        if (ce == cudaSuccess) ce = enqueue_lane_steps(e, m);
+    } else {
+        for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_ens_step(e);
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(e->stream, &g);
+    e->cur = saved;
+    if (ce == cudaSuccess && ee == cudaSuccess) ee = cudaGraphInstantiate(&exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    e->graphs[key] = exec;
+    return exec;
+}
+
+constexpr uint32_t kEnsChunk = 50;
+
+// Capture the graphs that the next n steps replay (run_ens_steps' chunks).
+int prepare_ens_steps(slime_ensemble* e, uint32_t n) {
+    const bool lanes = e->engine == SLIME_ENSEMBLE_LANES;
+    if (!e->use_graphs && !lanes) return SLIME_OK;
+    if (lanes) {
+        int rc = ensure_lanes(e);
+        if (rc != SLIME_OK) return rc;
+    }
+    const int saved = e->cur;
+    uint64_t steps = e->steps_done;
     while (n > 0) {
-        uint32_t m = n < chunk ? n : chunk;
+        uint32_t m = n < kEnsChunk ? n : kEnsChunk;
+        if (e->reorder_every) {
+            uint64_t to_next = e->reorder_every - steps % e->reorder_every;
+            if (to_next < m) m = (uint32_t)to_next;
+        }
+        if (!chunk_graph(e, m)) break; // stepping will launch directly
+        if (m & 1) e->cur = 1 - e->cur;
+        steps += m;
+        n -= m;
+    }
+    e->cur = saved;
+    return SLIME_OK;
+}
+
+int run_ens_steps(slime_ensemble* e, uint32_t n) {
+    while (n > 0) {
+        uint32_t m = n < kEnsChunk ? n : kEnsChunk;
         if (e->reorder_every) {
             if (e->steps_done % e->reorder_every == 0 && e->last_reorder_step != e->steps_done) {
                 int rc = reorder_all(e);
@@ -387,28 +614,26 @@ int run_ens_steps(slime_ensemble* e, uint32_t n) {
             uint64_t to_next = e->reorder_every - e->steps_done % e->reorder_every;
             if (to_next < m) m = (uint32_t)to_next;
         }
-        if (e->use_graphs) {
-            auto key = std::make_pair(m, e->cur);
-            auto it = e->graphs.find(key);
-            cudaGraphExec_t exec = nullptr;
-            if (it == e->graphs.end()) {
-                const int saved = e->cur;
-                cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
-                for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) ce = enqueue_ens_step(e);
-                cudaGraph_t g = nullptr;
-                cudaError_t ee = cudaStreamEndCapture(e->stream, &g);
-                e->cur = saved;
-                if (ce == cudaSuccess && ee == cudaSuccess) ee = cudaGraphInstantiate(&exec, g, 0);
-                if (g) cudaGraphDestroy(g);
-                if (ce != cudaSuccess || ee != cudaSuccess) {
-                    // cooperative launches that cannot be captured run directly
-                    cudaGetLastError();
-                    e->use_graphs = false;
+        const bool lanes = e->engine == SLIME_ENSEMBLE_LANES;
+        if (lanes) {
+            int rc = ensure_lanes(e);
+            if (rc != SLIME_OK) return rc;
+        }
+        const uint64_t kernels = lanes ? m * lane_kernels_per_step(e) : m;
+        if (e->use_graphs || lanes) {
+            cudaGraphExec_t exec = chunk_graph(e, m);
+            if (!exec) {
+                if (lanes) { // the lane chains run directly
+                    ECK(enqueue_lane_steps(e, m), "launching ensemble lanes");
+                    e->last_chunk_graph = false;
+                    e->launches += kernels;
+                    e->steps_done += m;
+                    n -= m;
                     continue;
                 }
-                e->graphs[key] = exec;
-            } else {
-                exec = it->second;
+                // cooperative launches that cannot be captured run directly
+                e->use_graphs = false;
+                continue;
             }
             ECK(cudaGraphLaunch(exec, e->stream), "launching ensemble graph");
             if (m & 1) e->cur = 1 - e->cur;
@@ -417,7 +642,7 @@ int run_ens_steps(slime_ensemble* e, uint32_t n) {
             for (uint32_t i = 0; i < m; i++) ECK(enqueue_ens_step(e), "launching ensemble step");
             e->last_chunk_graph = false;
         }
-        e->launches += m;
+        e->launches += kernels;
         e->steps_done += m;
         n -= m;
     }
@@ -505,13 +730,6 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
     uint32_t maxw = 0;
     for (const Colony& c : e->colonies) maxw = c.W > maxw ? c.W : maxw;
     e->total_cells = cells + maxw + 4;
-    // agent work items: 1,024 agents of one colony each
-    std::vector<uint2> ai;
-    for (uint32_t j = 0; j < k; j++) {
-        uint64_t groups = (e->colonies[j].n + 3) / 4;
-        for (uint64_t g0 = 0; g0 < groups; g0 += kEnsThreads) ai.push_back(make_uint2(j, (uint32_t)g0));
-    }
-    e->n_agent_items = (uint32_t)ai.size();
     int rc = SLIME_OK;
     cudaError_t ce = cudaSuccess;
     do {
@@ -528,11 +746,6 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         }
         if (ce != cudaSuccess) break;
         if ((ce = dev_alloc((void**)&e->d_cols, k * sizeof(DevColony))) != cudaSuccess) break;
-        if ((ce = dev_alloc((void**)&e->d_agent_items, (ai.size() ? ai.size() : 1) * sizeof(uint2))) != cudaSuccess) break;
-        if (ai.size() &&
-            (ce = cudaMemcpy(e->d_agent_items, ai.data(), ai.size() * sizeof(uint2), cudaMemcpyHostToDevice)) !=
-                cudaSuccess)
-            break;
         if ((ce = dev_alloc((void**)&e->d_bar, sizeof(GridBarrier))) != cudaSuccess) break;
         ce = cudaMemset(e->d_bar, 0, sizeof(GridBarrier));
     } while (0);
@@ -547,6 +760,7 @@ slime_ensemble* slime_ensemble_create(uint32_t k, const uint32_t* widths, const 
         for (int i = 0; i < 2; i++) c.tex[i] = make_trail_texture(e->trail[i] + c.trail_off, c.W, c.H);
     }
     if (rc == SLIME_OK) rc = upload_cols(e);
+    if (rc == SLIME_OK) rc = build_agent_items(e);
     if (rc == SLIME_OK) rc = build_strip_items(e);
     if (rc == SLIME_OK) rc = size_grid(e);
     if (rc != SLIME_OK) {
@@ -563,6 +777,7 @@ void slime_ensemble_destroy(slime_ensemble* e) {
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     ens_invalidate(e);
+    destroy_lanes(e);
     for (Colony& c : e->colonies)
         for (int i = 0; i < 2; i++)
             if (c.tex[i]) cudaDestroyTextureObject(c.tex[i]);
@@ -594,7 +809,13 @@ int slime_ensemble_set_params(slime_ensemble* e, uint32_t j, const SlimeParams* 
     c.params.width = c.W;
     c.params.height = c.H;
     c.dev = d;
-    return upload_cols(e); // the colony table is read by the kernel: graphs stay valid
+    // the cooperative kernel reads the colony table (its graphs stay valid);
+    // the lanes engine's graphs hold the parameters as kernel arguments
+    if (e->engine == SLIME_ENSEMBLE_LANES) {
+        cudaStreamSynchronize(e->stream);
+        ens_invalidate(e);
+    }
+    return upload_cols(e);
 }
 
 int ensure_staging(slime_ensemble* e, size_t bytes) {
@@ -680,6 +901,12 @@ int slime_ensemble_download_trail(slime_ensemble* e, uint32_t j, float* trail, u
     return SLIME_OK;
 }
 
+int slime_ensemble_prepare_steps(slime_ensemble* e, uint32_t n_steps) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(e->device);
+    return prepare_ens_steps(e, n_steps);
+}
+
 int slime_ensemble_step(slime_ensemble* e, uint32_t n_steps) {
     if (!e) return SLIME_ERR_INVALID_ARGUMENT;
     cudaSetDevice(e->device);
@@ -699,7 +926,46 @@ int slime_ensemble_get_stream(slime_ensemble* e, void** stream) {
     return SLIME_OK;
 }
 
-// Time trial steps for every strip height and residency, keep the fastest,
+int slime_ensemble_set_engine(slime_ensemble* e, uint32_t engine, uint32_t agent_shape, uint32_t trail_tile) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    if (engine != SLIME_ENSEMBLE_COOPERATIVE && engine != SLIME_ENSEMBLE_LANES)
+        return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "unknown ensemble engine");
+    if (agent_shape >= (uint32_t)agent_shape_count() || trail_tile >= (uint32_t)kTrailTileTma)
+        return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "agent shape or trail tile out of range");
+    for (const Colony& c : e->colonies)
+        if (!trail_tile_supported(c.dev, (int)trail_tile))
+            return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "trail tile not supported by every colony");
+    cudaSetDevice(e->device);
+    ECK(cudaStreamSynchronize(e->stream), "synchronising");
+    e->engine = (int)engine;
+    e->lane_agent_shape = (int)agent_shape;
+    e->lane_trail_tile = (int)trail_tile;
+    ens_invalidate(e);
+    return SLIME_OK;
+}
+
+int slime_ensemble_set_shape(slime_ensemble* e, uint32_t strip_rows, uint32_t blocks_per_sm,
+                             uint32_t agents_per_thread) {
+    if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    if ((strip_rows != 8 && strip_rows != 16 && strip_rows != 32) || blocks_per_sm > 4 ||
+        (agents_per_thread != 2 && agents_per_thread != 4)) {
+        e->err = "ensemble shape: strip_rows must be 8, 16 or 32, blocks_per_sm at most 4, agents_per_thread 2 or 4";
+        return SLIME_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(e->device);
+    ECK(cudaStreamSynchronize(e->stream), "synchronising");
+    e->rows = (int)strip_rows;
+    e->blocks_per_sm = (int)blocks_per_sm;
+    e->apt = (int)agents_per_thread;
+    ens_invalidate(e);
+    int rc = build_agent_items(e);
+    if (rc == SLIME_OK) rc = build_strip_items(e);
+    if (rc == SLIME_OK) rc = size_grid(e);
+    return rc;
+}
+
+// Time trial steps of both engines (cooperative: agents per thread, strip
+// height and residency; lanes: agent shape and trail tile), keep the fastest,
 // and put the state back (snapshot of agents, trails and counts).
 int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     if (!e) return SLIME_ERR_INVALID_ARGUMENT;
@@ -732,31 +998,74 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    int best_rows = e->rows, best_bps = e->blocks_per_sm;
+    int best_rows = e->rows, best_bps = e->blocks_per_sm, best_apt = e->apt;
+    int best_engine = e->engine, best_shape = e->lane_agent_shape, best_tile = e->lane_trail_tile;
     float best = 1e30f;
     const int rows_opts[] = {8, 16, 32};
     const int bps_opts[] = {0, 2, 4};
+    const int apt_opts[] = {4, 2};
     int rc = SLIME_OK;
-    for (int ro : rows_opts) {
+    auto trial = [&](float* ms) -> int {
+        ens_invalidate(e);
+        // warm-up; the lanes engine captures its chunk graph for both
+        // parities of the trail buffers here, not inside the timed steps
+        run_ens_steps(e, 1);
+        run_ens_steps(e, reps);
+        run_ens_steps(e, reps);
+        cudaEventRecord(e0, e->stream);
+        run_ens_steps(e, reps);
+        cudaEventRecord(e1, e->stream);
+        cudaEventSynchronize(e1);
+        *ms = 0;
+        cudaEventElapsedTime(ms, e0, e1);
+        return check_barrier(e);
+    };
+    // cooperative engine: agents per thread x strip rows x residency
+    e->engine = SLIME_ENSEMBLE_COOPERATIVE;
+    for (int ao : apt_opts) {
+      e->apt = ao;
+      if ((rc = build_agent_items(e)) != SLIME_OK) break;
+      for (int ro : rows_opts) {
         for (int bo : bps_opts) {
             e->rows = ro;
             e->blocks_per_sm = bo;
             if ((rc = build_strip_items(e)) != SLIME_OK || (rc = size_grid(e)) != SLIME_OK) break;
-            run_ens_steps(e, 1); // warm-up
-            cudaEventRecord(e0, e->stream);
-            run_ens_steps(e, reps);
-            cudaEventRecord(e1, e->stream);
-            cudaEventSynchronize(e1);
             float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if ((rc = check_barrier(e)) != SLIME_OK) break;
+            if ((rc = trial(&ms)) != SLIME_OK) break;
             if (ms < best) {
                 best = ms;
+                best_engine = SLIME_ENSEMBLE_COOPERATIVE;
                 best_rows = ro;
                 best_bps = bo;
+                best_apt = ao;
             }
         }
         if (rc != SLIME_OK) break;
+      }
+      if (rc != SLIME_OK) break;
+    }
+    // lanes engine (its chunks are always captured): agent shape x trail tile
+    // (the persistent shapes; the streaming tiles)
+    const int shape_opts[] = {13, 9, 15};
+    const int tile_opts[] = {7, 8, 9};
+    e->engine = SLIME_ENSEMBLE_LANES;
+    for (int so : shape_opts) {
+        if (rc != SLIME_OK || so >= agent_shape_count()) break;
+        for (int to : tile_opts) {
+            bool ok = true;
+            for (const Colony& c : e->colonies) ok = ok && trail_tile_supported(c.dev, to);
+            if (!ok) continue;
+            e->lane_agent_shape = so;
+            e->lane_trail_tile = to;
+            float ms = 0;
+            if ((rc = trial(&ms)) != SLIME_OK) break;
+            if (ms < best) {
+                best = ms;
+                best_engine = SLIME_ENSEMBLE_LANES;
+                best_shape = so;
+                best_tile = to;
+            }
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -774,7 +1083,12 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     e->reorder_every = saved_reorder;
     e->rows = best_rows;
     e->blocks_per_sm = best_bps;
+    e->apt = best_apt;
+    e->engine = best_engine;
+    e->lane_agent_shape = best_shape;
+    e->lane_trail_tile = best_tile;
     ens_invalidate(e);
+    if (rc == SLIME_OK) rc = build_agent_items(e);
     if (rc == SLIME_OK) rc = build_strip_items(e);
     if (rc == SLIME_OK) rc = size_grid(e);
     return rc;
@@ -820,6 +1134,11 @@ int slime_ensemble_get_info(const slime_ensemble* e, SlimeEnsembleInfo* out) {
     }
     out->grid_blocks = (uint32_t)e->grid;
     out->strip_rows = (uint32_t)e->rows;
+    out->agents_per_thread = (uint32_t)e->apt;
+    out->engine = (uint32_t)e->engine;
+    out->lanes = (uint32_t)e->lanes.size();
+    out->lane_agent_shape = (uint32_t)e->lane_agent_shape;
+    out->lane_trail_tile = (uint32_t)e->lane_trail_tile;
     return SLIME_OK;
 }
 

@@ -13,7 +13,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import (BLUR_GAUSS, BLUR_REF_BOX3, DECAY_MULTIPLY, DECAY_REF_SUBTRACT, DISPATCH_EACH_AGENT,
-                   DISPATCH_REFERENCE, MAX_BLUR_RADIUS, SENSOR_ROTATED, SENSOR_SHADER, SlimeEnsembleInfo,
+                   DISPATCH_REFERENCE, ENSEMBLE_COOPERATIVE, ENSEMBLE_LANES, MAX_BLUR_RADIUS, SENSOR_ROTATED, SENSOR_SHADER, SlimeEnsembleInfo,
                    SlimeGrads, SlimeInfo, SlimeOptions, SlimeParams, SlimeSettings)
 
 __all__ = [
@@ -22,6 +22,7 @@ __all__ = [
     "Simulation", "Ensemble", "SlimeParams", "SlimeOptions", "SlimeGrads", "lib",
     "DECAY_REF_SUBTRACT", "DECAY_MULTIPLY", "BLUR_REF_BOX3", "BLUR_GAUSS", "MAX_BLUR_RADIUS",
     "DISPATCH_EACH_AGENT", "DISPATCH_REFERENCE", "SENSOR_SHADER", "SENSOR_ROTATED",
+    "ENSEMBLE_COOPERATIVE", "ENSEMBLE_LANES",
 ]
 
 Settings = SlimeSettings
@@ -247,6 +248,11 @@ class Simulation:
     def step(self, n_steps=1):
         self._check(self._L.slime_step(self._h, n_steps), "step")
 
+    def prepare_steps(self, n_steps):
+        """Capture the CUDA graphs the next n_steps steps replay, without
+        stepping (slime_prepare_steps)."""
+        self._check(self._L.slime_prepare_steps(self._h, n_steps), "prepare_steps")
+
     def sync(self):
         self._check(self._L.slime_sync(self._h), "sync")
 
@@ -407,6 +413,10 @@ class Ensemble:
     def step(self, n_steps=1):
         self._check(self._L.slime_ensemble_step(self._h, n_steps), "step")
 
+    def prepare_steps(self, n_steps):
+        """Capture the graphs of the next n_steps steps now (slime_ensemble_prepare_steps)."""
+        self._check(self._L.slime_ensemble_prepare_steps(self._h, n_steps), "prepare_steps")
+
     def sync(self):
         self._check(self._L.slime_ensemble_sync(self._h), "sync")
 
@@ -417,6 +427,18 @@ class Ensemble:
 
     def autotune(self, reps=5):
         self._check(self._L.slime_ensemble_autotune(self._h, reps), "autotune")
+
+    def set_engine(self, engine, lane_agent_shape=13, lane_trail_tile=8):
+        """Pick the stepping engine by hand (slime_ensemble_set_engine):
+        ENSEMBLE_COOPERATIVE or ENSEMBLE_LANES with its agent shape and trail
+        tile."""
+        self._check(self._L.slime_ensemble_set_engine(self._h, engine, lane_agent_shape, lane_trail_tile),
+                    "set_engine")
+
+    def set_shape(self, strip_rows=16, blocks_per_sm=0, agents_per_thread=4):
+        """Pick the cooperative step's launch shape by hand (slime_ensemble_set_shape)."""
+        self._check(self._L.slime_ensemble_set_shape(self._h, strip_rows, blocks_per_sm, agents_per_thread),
+                    "set_shape")
 
     def selftest_barrier_timeout(self):
         """Make the grid barrier's bounded wait run out; returns the status

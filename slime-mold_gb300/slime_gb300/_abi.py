@@ -26,6 +26,8 @@ DISPATCH_EACH_AGENT = 0
 DISPATCH_REFERENCE = 1
 SENSOR_SHADER = 0
 SENSOR_ROTATED = 1
+ENSEMBLE_COOPERATIVE = 0
+ENSEMBLE_LANES = 1
 
 
 class SlimeParams(C.Structure):
@@ -127,6 +129,12 @@ class SlimeEnsembleInfo(C.Structure):
         ("total_cells", C.c_uint64),
         ("grid_blocks", C.c_uint32),
         ("strip_rows", C.c_uint32),
+        ("agents_per_thread", C.c_uint32),
+        ("engine", C.c_uint32),
+        ("lanes", C.c_uint32),
+        ("lane_agent_shape", C.c_uint32),
+        ("lane_trail_tile", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -178,6 +186,7 @@ SIGNATURES = {
     "slime_state_load": (C.c_int, [P, C.c_char_p]),
     "slime_set_steps_done": (C.c_int, [P, C.c_uint64]),
     "slime_step": (C.c_int, [P, C.c_uint32]),
+    "slime_prepare_steps": (C.c_int, [P, C.c_uint32]),
     "slime_sync": (C.c_int, [P]),
     "slime_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
     "slime_download_deposit_counts": (C.c_int, [P, U32P, C.c_uint64]),
@@ -202,9 +211,12 @@ SIGNATURES = {
     "slime_ensemble_download_trail": (C.c_int, [P, C.c_uint32, F32P, C.c_uint64]),
     "slime_ensemble_set_reorder": (C.c_int, [P, C.c_uint32, C.c_uint32]),
     "slime_ensemble_step": (C.c_int, [P, C.c_uint32]),
+    "slime_ensemble_prepare_steps": (C.c_int, [P, C.c_uint32]),
     "slime_ensemble_sync": (C.c_int, [P]),
     "slime_ensemble_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
     "slime_ensemble_autotune": (C.c_int, [P, C.c_uint32]),
+    "slime_ensemble_set_shape": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "slime_ensemble_set_engine": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "slime_ensemble_launch_count": (C.c_int, [P, C.POINTER(C.c_uint64)]),
     "slime_ensemble_get_info": (C.c_int, [P, C.POINTER(SlimeEnsembleInfo)]),
     "slime_ensemble_selftest_barrier_timeout": (C.c_int, [P]),

@@ -33,11 +33,13 @@ def colony_setup(seed, blur_mode, radius=1.0):
     return cols
 
 
+@pytest.mark.parametrize("engine", [0, 1])
 @pytest.mark.parametrize("blur_mode,radius,reorder", [(1, 1.0, 0), (0, 1.0, 3), (1, 2.0, 2)])
-def test_ensemble_matches_plain_runs(gpu, blur_mode, radius, reorder):
+def test_ensemble_matches_plain_runs(gpu, blur_mode, radius, reorder, engine):
     import slime_gb300 as sg
     cols = colony_setup(7, blur_mode, radius)
     ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    ens.set_engine(engine)
     ens.set_reorder(reorder, 1)
     for j, (W, H, n, p, agents, trail) in enumerate(cols):
         ens.upload_agents(j, agents)
@@ -47,11 +49,13 @@ def test_ensemble_matches_plain_runs(gpu, blur_mode, radius, reorder):
     ens.sync()
     assert ens.launch_count() >= 7
     info = ens.info()
-    # the cooperative step launches were captured and replayed as graphs
-    assert info.graphs_in_use == 1, "capture of the cooperative launch fell back to direct launches"
+    # the step launches were captured and replayed as graphs
+    assert info.graphs_in_use == 1, "capture of the step launches fell back to direct launches"
+    assert info.engine == engine and info.lanes == (len(cols) if engine == sg.ENSEMBLE_LANES else 0)
     assert (info.n_colonies, info.steps_done) == (len(cols), 7)
     assert info.total_agents == sum(c[2] for c in cols) and info.total_cells == sum(c[0] * c[1] for c in cols)
     assert info.grid_blocks > 0 and info.strip_rows in (8, 16, 32)
+    assert info.agents_per_thread in (2, 4)
     for j, (W, H, n, p, agents, trail) in enumerate(cols):
         with sg.Simulation(W, H, n, p) as sim:
             sim.upload_agents(agents)
@@ -63,6 +67,81 @@ def test_ensemble_matches_plain_runs(gpu, blur_mode, radius, reorder):
             ca, ct = agents.copy(), trail.copy()
             oracle.run(p, W, H, ca, ct, 7)
             assert_bitexact(ens.download_trail(j), ct, f"colony {j} trail vs oracle")
+
+
+@pytest.mark.parametrize("rows,bps,apt", [(8, 0, 2), (32, 2, 2), (16, 1, 2), (8, 4, 4), (32, 0, 4)])
+def test_every_launch_shape_gives_the_same_result(gpu, rows, bps, apt):
+    """Strip height, residency and agents per thread (four alone or two as a
+    pair; colonies with agent counts that leave a ragged last group) change
+    the launch only: every colony matches a plain run bit for bit."""
+    import slime_gb300 as sg
+    cols = colony_setup(17, 1)
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    ens.set_shape(rows, bps, apt)
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        ens.upload_agents(j, agents)
+        ens.upload_trail(j, trail)
+    ens.step(5)
+    ens.sync()
+    info = ens.info()
+    assert (info.strip_rows, info.agents_per_thread) == (rows, apt)
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        with sg.Simulation(W, H, n, p) as sim:
+            sim.upload_agents(agents)
+            sim.upload_trail(trail)
+            sim.step(5)
+            assert_bitexact(ens.download_agents(j), sim.download_agents(), f"colony {j} agents")
+            assert_bitexact(ens.download_trail(j), sim.download_trail(), f"colony {j} trail")
+    with pytest.raises(sg.SlimeError):
+        ens.set_shape(12, 0, 4)
+    with pytest.raises(sg.SlimeError):
+        ens.set_shape(16, 0, 3)
+    ens.close()
+
+
+@pytest.mark.parametrize("shape,tile", [(13, 8), (9, 7), (15, 9), (0, 3), (12, 4)])
+def test_lanes_engine_shapes_and_params_update(gpu, shape, tile):
+    """The lanes engine (each colony a chain of the single-colony kernels on
+    its own capture lane) with persistent and regular agent shapes, streaming
+    and shared-memory trail tiles, and a parameter change between chunks
+    (the captured graphs hold parameters as kernel arguments): bit for bit
+    the plain runs."""
+    import slime_gb300 as sg
+    cols = colony_setup(19, 1)
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    ens.set_engine(sg.ENSEMBLE_LANES, shape, tile)
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        ens.upload_agents(j, agents)
+        ens.upload_trail(j, trail)
+    ens.prepare_steps(3)
+    assert ens.info().steps_done == 0
+    ens.step(3)
+    q = cols[1][3].copy()
+    q.agent_turn_speed = 0.05
+    q.decay_factor = 0.5
+    ens.set_params(1, q)
+    ens.step(4)
+    ens.sync()
+    info = ens.info()
+    assert (info.engine, info.lane_agent_shape, info.lane_trail_tile) == (sg.ENSEMBLE_LANES, shape, tile)
+    assert info.kernel_launches > 0 and info.steps_done == 7
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        with sg.Simulation(W, H, n, p) as sim:
+            sim.upload_agents(agents)
+            sim.upload_trail(trail)
+            sim.step(3)
+            if j == 1:
+                sim.set_params(q)
+            sim.step(4)
+            assert_bitexact(ens.download_agents(j), sim.download_agents(), f"colony {j} agents")
+            assert_bitexact(ens.download_trail(j), sim.download_trail(), f"colony {j} trail")
+    with pytest.raises(sg.SlimeError):
+        ens.set_engine(2)
+    with pytest.raises(sg.SlimeError):
+        ens.set_engine(sg.ENSEMBLE_LANES, 99, 8)
+    with pytest.raises(sg.SlimeError):
+        ens.set_engine(sg.ENSEMBLE_LANES, 13, 10)  # the tensor-copy tile needs per-colony maps
+    ens.close()
 
 
 def test_ensemble_autotune_and_params_update(gpu):

@@ -104,6 +104,31 @@ def test_graph_chunks_match_single_steps(gpu):
     assert a.info().steps_done == 23
 
 
+def test_prepare_steps_captures_without_stepping(gpu):
+    """slime_prepare_steps captures the chunk graphs (graph_chunk 7, a reorder
+    every 10 steps cutting chunks) without stepping; the steps after it replay
+    them with the same result as an unprepared run."""
+    W, H, n = 256, 96, 9000
+    p = config0_params(W, H, agent_speed_min=20.0, agent_speed_max=40.0, agent_jitter=0.2)
+    agents = agents_uniform(n, W, H, 20.0, 40.0, seed=5)
+    a = make_sim(W, H, n, p, agents)
+    b = make_sim(W, H, n, p, agents)
+    for s in (a, b):
+        s.set_options(use_graphs=1, graph_chunk=7, reorder_every=10)
+    a.step(3)
+    b.step(3)
+    t0, g0 = a.download_trail(), a.download_agents()
+    a.prepare_steps(31)
+    assert a.info().steps_done == 3
+    assert_bitexact(a.download_trail(), t0, "trail after prepare")
+    assert_bitexact(a.download_agents(), g0, "agents after prepare")
+    a.step(31)
+    b.step(31)
+    assert_bitexact(a.download_agents(), b.download_agents(), "agents")
+    assert_bitexact(a.download_trail(), b.download_trail(), "trail")
+    assert a.info().steps_done == 34
+
+
 @pytest.mark.parametrize("tile", range(1, 12))
 @pytest.mark.parametrize("W,H", [(333, 77), (336, 77), (256, 40), (8, 9)])
 def test_every_trail_tile_is_bitexact(gpu, tile, W, H):
