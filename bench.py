@@ -267,50 +267,16 @@ def ensemble_colonies(seed=1, k=64):
     return cols
 
 
-def run_ensemble(args):
-    """Batched ensemble: one persistent launch per step over 64 colonies,
-    against the same colonies run one after the other with the plain path,
-    and against the plain 4096^2 per-cell throughput."""
+def ensemble_comparisons(args, cols, cells, agents_total, R):
+    """The ensemble's colonies one plain Simulation after the other, the
+    plain 4096^2 per-cell throughput, and the plain path's per-agent and
+    per-cell costs (for the ensemble at equal work)."""
     import torch
     import slime_gb300 as sg
-    torch.cuda.set_device(0)
-    cols = ensemble_colonies(k=args.colonies)
-    cells = sum(c[0] * c[1] for c in cols)
-    agents_total = sum(c[2] for c in cols)
-    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
-    for j, (W, H, n, p, seed) in enumerate(cols):
-        ens.seed_agents(j, 1000 + seed)
-    ens.set_reorder(args.reorder_every, 2)
-    ens.autotune(2)
-    info = ens.info()
-    if info.engine == sg.ENSEMBLE_LANES:
-        tuned = {"engine": "lanes", "what": "each colony a chain of the single-colony kernels on its own "
-                 "capture lane, one CUDA graph per chunk of steps",
-                 "agent_shape": info.lane_agent_shape, "trail_tile": info.lane_trail_tile}
-    else:
-        tuned = {"engine": "cooperative", "what": "one cooperative persistent launch per step",
-                 "strip_rows": info.strip_rows, "grid_blocks": info.grid_blocks,
-                 "agents_per_thread": info.agents_per_thread}
-    stream = torch.cuda.ExternalStream(ens.stream_ptr())
-    ens.step(args.warmup)
-    ens.prepare_steps(args.steps)
-    ens.sync()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = ens.launch_count()
-    with ClockSampler(0) as clocks:
-        e0.record(stream)
-        ens.step(args.steps)
-        e1.record(stream)
-        ens.sync()
-    ms = e0.elapsed_time(e1)
-    launches = ens.launch_count() - l0
-    tuned["lanes"] = ens.info().lanes
-    ens_cells = cells * args.steps / (ms / 1e3)
-    ens_agents = agents_total * args.steps / (ms / 1e3)
-    del ens
     # the same colonies, one plain Simulation after the other
     seq_steps = max(3, min(args.steps, 50))
     seq_ms = 0.0
+    seq_reorder_ms = 0.0
     for W, H, n, p, seed in cols:
         sim = sg.Simulation(W, H, n, p)
         sim.seed_agents(1000 + seed)
@@ -325,7 +291,12 @@ def run_ensemble(args):
         sim.step(seq_steps)
         b.record(st)
         sim.sync()
-        seq_ms += a.elapsed_time(b)
+        # charged as the ensemble's window: reorders inside it out, each
+        # step's share in
+        r_ms = sim.profile_reorder(1) if R else 0.0
+        r_in = sum(1 for s in range(3, 3 + seq_steps) if R and s % R == 0)
+        seq_reorder_ms += seq_steps * r_ms / R if R else 0.0
+        seq_ms += a.elapsed_time(b) - r_in * r_ms + (seq_steps * r_ms / R if R else 0.0)
         sim.close()
     seq_cells = cells * seq_steps / (seq_ms / 1e3)
     # plain single-colony per-cell throughput at 4096^2 (short run)
@@ -353,6 +324,67 @@ def run_ensemble(args):
     t_cell = pt_ms / 50 / (W * H)
     plain_model_ms = agents_total * t_agent + cells * t_cell
     sim.close()
+    return {"seq_cells": seq_cells, "seq_reorder_ms_per_step": seq_reorder_ms / seq_steps,
+            "plain_cells": plain_cells, "plain_model_ms": plain_model_ms}
+
+
+def run_ensemble(args):
+    """Batched ensemble: one persistent launch per step over 64 colonies,
+    against the same colonies run one after the other with the plain path,
+    and against the plain 4096^2 per-cell throughput."""
+    import torch
+    import slime_gb300 as sg
+    torch.cuda.set_device(0)
+    cols = ensemble_colonies(k=args.colonies)
+    cells = sum(c[0] * c[1] for c in cols)
+    agents_total = sum(c[2] for c in cols)
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    for j, (W, H, n, p, seed) in enumerate(cols):
+        ens.seed_agents(j, 1000 + seed)
+    ens.set_reorder(args.reorder_every, 2)
+    if args.ensemble_engine == "auto":
+        ens.autotune(2)
+    elif args.ensemble_engine == "lanes":  # the autotuner's usual pick, fixed (short profiler runs)
+        ens.set_engine(sg.ENSEMBLE_LANES, 13, 9, 0)
+    else:
+        ens.set_engine(sg.ENSEMBLE_COOPERATIVE)
+        ens.set_shape(16, 4, 4)
+    info = ens.info()
+    if info.engine == sg.ENSEMBLE_LANES:
+        tuned = {"engine": "lanes", "what": "each colony a chain of the single-colony kernels on its own "
+                 "capture lane, one CUDA graph per chunk of steps",
+                 "agent_shape": info.lane_agent_shape, "trail_tile": info.lane_trail_tile}
+    else:
+        tuned = {"engine": "cooperative", "what": "one cooperative persistent launch per step",
+                 "strip_rows": info.strip_rows, "grid_blocks": info.grid_blocks,
+                 "agents_per_thread": info.agents_per_thread}
+    stream = torch.cuda.ExternalStream(ens.stream_ptr())
+    ens.step(args.warmup)
+    ens.prepare_steps(args.steps)
+    ens.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ens.launch_count()
+    s0 = ens.info().steps_done
+    with ClockSampler(0) as clocks:
+        e0.record(stream)
+        ens.step(args.steps)
+        e1.record(stream)
+        ens.sync()
+    window_ms = e0.elapsed_time(e1)
+    launches = ens.launch_count() - l0
+    info = ens.info()
+    tuned["lanes"] = info.lanes
+    tuned["marks_colonies"] = info.marks_colonies
+    # every step pays its share of the Morton reorders (one per reorder_every
+    # steps), whether or not one fell inside the window
+    R = args.reorder_every
+    reorders_in = sum(1 for s in range(s0, s0 + args.steps) if R and s % R == 0)
+    reorder_ms = ens.profile_reorder(3) / 3 if R else 0.0
+    ms = window_ms - reorders_in * reorder_ms + (args.steps * reorder_ms / R if R else 0.0)
+    ens_cells = cells * args.steps / (ms / 1e3)
+    ens_agents = agents_total * args.steps / (ms / 1e3)
+    del ens
+    cmp = {} if args.no_compare else ensemble_comparisons(args, cols, cells, agents_total, R)
     line = {
         "metric": "trail cells/s (batched ensemble, 64 colonies)",
         "value": ens_cells, "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -360,13 +392,21 @@ def run_ensemble(args):
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": f"ensemble-{len(cols)}", "colonies": len(cols), "cells": cells, "agents": agents_total,
                    "sides": sorted(set(c[0] for c in cols)), "reorder_every": args.reorder_every},
-        "agent_steps_per_s": ens_agents,
-        "sequential_plain_cells_per_s": seq_cells, "ensemble_over_sequential": ens_cells / seq_cells,
-        "plain_4096_cells_per_s": plain_cells, "ensemble_over_plain_per_cell": ens_cells / plain_cells,
-        "plain_path_ms_for_this_work": plain_model_ms,
-        "ensemble_over_plain_equal_work": plain_model_ms / (ms / args.steps),
+        "agent_steps_per_s": ens_agents, "window_ms_per_step": window_ms / args.steps,
+        "reorder": {"ms": reorder_ms, "every": R, "ms_per_step": reorder_ms / R if R else 0.0,
+                    "in_timed_window": reorders_in,
+                    "sequential_ms_per_step": cmp.get("seq_reorder_ms_per_step"),
+                    "what": "ms_per_step = timed window - reorders inside it + K x (one reorder's time / "
+                            "reorder_every), the sequential runs charged the same way"},
         "tuned": tuned, "gpu_launches": launches, "clocks": clocks.summary(),
     }
+    if cmp:
+        line.update({
+            "sequential_plain_cells_per_s": cmp["seq_cells"], "ensemble_over_sequential": ens_cells / cmp["seq_cells"],
+            "plain_4096_cells_per_s": cmp["plain_cells"],
+            "ensemble_over_plain_per_cell": ens_cells / cmp["plain_cells"],
+            "plain_path_ms_for_this_work": cmp["plain_model_ms"],
+            "ensemble_over_plain_equal_work": cmp["plain_model_ms"] / (ms / args.steps)})
     print(json.dumps(line), flush=True)
 
 
@@ -587,6 +627,10 @@ def main():
                     help="agents updated per step: every agent once, or the reference's own dispatch")
     ap.add_argument("--colonies", type=int, default=64,
                     help="ensemble-64: the first K of the 64 seeded colonies (smaller captures)")
+    ap.add_argument("--ensemble-engine", default="auto", choices=["auto", "lanes", "cooperative"],
+                    help="ensemble-64: autotuned engine, or one fixed without tuning (profiler runs)")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="ensemble-64: skip the sequential and plain comparison runs (profiler runs)")
     ap.add_argument("--adjoint-steps", type=int, default=2000,
                     help="adjoint-1024: steps recorded and back-propagated (2000 in the configuration)")
     args = ap.parse_args()

@@ -341,6 +341,9 @@ int slime_ensemble_seed_agents(slime_ensemble* ens, uint32_t colony, uint64_t se
                                float heading_max);
 int slime_ensemble_upload_trail(slime_ensemble* ens, uint32_t colony, const float* trail, uint64_t n_cells);
 int slime_ensemble_download_trail(slime_ensemble* ens, uint32_t colony, float* trail, uint64_t n_cells);
+/* Milliseconds that `reps` back-to-back Morton reorders of every colony take
+ * on the device (after one untimed reorder); results do not change. */
+int slime_ensemble_profile_reorder(slime_ensemble* ens, uint32_t reps, double* ms);
 /* Morton-reorder every colony's agents every `every` steps (0 = never);
  * results do not change, only the memory order of the agents. */
 int slime_ensemble_set_reorder(slime_ensemble* ens, uint32_t every, uint32_t cell_log2);
@@ -360,9 +363,11 @@ int slime_ensemble_autotune(slime_ensemble* ens, uint32_t reps);
 #define SLIME_ENSEMBLE_LANES 1u
 /* Choose the engine by hand; for LANES also the agent-kernel shape and trail
  * tile (indices of the single-colony tables; the tensor-copy tile is not
- * available here).  Results do not change. */
+ * available here) and the number of lanes (1..64; 0 = one per colony up to
+ * 64), over which the colonies are spread largest first onto the least
+ * loaded lane.  Results do not change. */
 int slime_ensemble_set_engine(slime_ensemble* ens, uint32_t engine, uint32_t lane_agent_shape,
-                              uint32_t lane_trail_tile);
+                              uint32_t lane_trail_tile, uint32_t lanes);
 /* Choose the cooperative step's launch shape by hand (what slime_ensemble_autotune picks
  * by timing): trail rows per strip item (8, 16 or 32), resident blocks per SM
  * (0 = as many as fit, else 1..4) and agents per thread of the agent phase
@@ -388,7 +393,8 @@ typedef struct SlimeEnsembleInfo {
     uint32_t lanes;             /* capture lanes of the lanes engine (0 until it first steps) */
     uint32_t lane_agent_shape;  /* lanes engine: agent-kernel shape (slime_set_agent_shape's table) */
     uint32_t lane_trail_tile;   /* lanes engine: trail tile (slime_set_trail_tile's table) */
-    uint32_t reserved;
+    uint32_t marks_colonies;    /* colonies whose last steps recorded deposits as byte marks (lanes
+                                   engine, deposition >= 1 on a clean trail) instead of counts */
 } SlimeEnsembleInfo;
 int slime_ensemble_get_info(const slime_ensemble* ens, SlimeEnsembleInfo* out);
 /* Failure-detection self-test: runs one block at the ensemble's grid barrier

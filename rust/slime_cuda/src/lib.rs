@@ -153,7 +153,7 @@ pub mod ffi {
         pub lanes: u32,
         pub lane_agent_shape: u32,
         pub lane_trail_tile: u32,
-        pub reserved: u32,
+        pub marks_colonies: u32,
     }
 
     #[repr(C)]
@@ -231,6 +231,7 @@ pub mod ffi {
         pub fn slime_ensemble_set_reorder(ens: *mut slime_ensemble, every: u32, cell_log2: u32) -> c_int;
         pub fn slime_ensemble_step(ens: *mut slime_ensemble, n_steps: u32) -> c_int;
         pub fn slime_ensemble_prepare_steps(ens: *mut slime_ensemble, n_steps: u32) -> c_int;
+        pub fn slime_ensemble_profile_reorder(ens: *mut slime_ensemble, reps: u32, ms: *mut f64) -> c_int;
         pub fn slime_ensemble_sync(ens: *mut slime_ensemble) -> c_int;
         pub fn slime_ensemble_get_stream(ens: *mut slime_ensemble, stream: *mut *mut c_void) -> c_int;
         pub fn slime_ensemble_autotune(ens: *mut slime_ensemble, reps: u32) -> c_int;
@@ -239,6 +240,7 @@ pub mod ffi {
             engine: u32,
             lane_agent_shape: u32,
             lane_trail_tile: u32,
+            lanes: u32,
         ) -> c_int;
         pub fn slime_ensemble_set_shape(
             ens: *mut slime_ensemble,
@@ -782,6 +784,12 @@ impl Ensemble {
     pub fn prepare_steps(&mut self, n_steps: u32) -> Result<()> {
         self.check(unsafe { ffi::slime_ensemble_prepare_steps(self.ens, n_steps) })
     }
+    /// Milliseconds that `reps` back-to-back reorders of every colony take.
+    pub fn profile_reorder(&mut self, reps: u32) -> Result<f64> {
+        let mut ms = 0.0f64;
+        self.check(unsafe { ffi::slime_ensemble_profile_reorder(self.ens, reps, &mut ms) })?;
+        Ok(ms)
+    }
     pub fn sync(&mut self) -> Result<()> {
         self.check(unsafe { ffi::slime_ensemble_sync(self.ens) })
     }
@@ -794,9 +802,12 @@ impl Ensemble {
         self.check(unsafe { ffi::slime_ensemble_autotune(self.ens, reps) })
     }
     /// Engine by hand (`SLIME_ENSEMBLE_COOPERATIVE` / `SLIME_ENSEMBLE_LANES`),
-    /// with the lanes engine's agent shape and trail tile.
-    pub fn set_engine(&mut self, engine: u32, lane_agent_shape: u32, lane_trail_tile: u32) -> Result<()> {
-        self.check(unsafe { ffi::slime_ensemble_set_engine(self.ens, engine, lane_agent_shape, lane_trail_tile) })
+    /// with the lanes engine's agent shape, trail tile and lane count (0: one
+    /// per colony, at most 64).
+    pub fn set_engine(&mut self, engine: u32, lane_agent_shape: u32, lane_trail_tile: u32, lanes: u32) -> Result<()> {
+        self.check(unsafe {
+            ffi::slime_ensemble_set_engine(self.ens, engine, lane_agent_shape, lane_trail_tile, lanes)
+        })
     }
     /// Cooperative launch shape by hand: strip rows (8, 16, 32), blocks per SM (0 = all
     /// that fit), agents per thread (4 or 2).

@@ -114,6 +114,7 @@ int set_error(std::string& err, int code, const char* fmt, ...);
 int cuda_error(std::string& err, cudaError_t e, const char* what);
 void invalidate_graphs(slime_ctx* ctx);
 bool marks_allowed(const slime_ctx* ctx);
+bool keeps_trail_clean(const DevParams& d);
 bool use_marks(const slime_ctx* ctx);
 int prepare_deposits(slime_ctx* ctx, bool marks);
 cudaError_t enqueue_step(slime_ctx* ctx, bool marks, bool chained);

@@ -65,6 +65,14 @@ struct Colony {
     SlimeParams params;
     DevParams dev;
     cudaTextureObject_t tex[2] = {0, 0};
+    // deposit records (as the single-colony context keeps them): whether the
+    // trail is clean (finite values >= 0, or +inf) so that byte marks can
+    // stand in for counts, which of the colony's two count / mark regions
+    // hold deposits, and the record the captured graphs use
+    bool trail_clean = true;
+    bool counts_dirty[2] = {false, false};
+    bool marks_dirty[2] = {false, false};
+    bool marks = false;
 };
 
 // Bounded grid barrier: every block arrives once; the last one to arrive
@@ -273,6 +281,7 @@ struct slime_ensemble {
     ReorderScratch reorder;
     float* trail[2] = {nullptr, nullptr};
     uint32_t* counts[2] = {nullptr, nullptr};
+    uint8_t* marks[2] = {nullptr, nullptr}; // per-cell deposit marks (lanes engine; allocated on first use)
     int cur = 0;
     DevColony* d_cols = nullptr;
     uint2* d_agent_items = nullptr;
@@ -293,6 +302,7 @@ struct slime_ensemble {
     int engine = SLIME_ENSEMBLE_COOPERATIVE;
     int lane_agent_shape = 13; // agent-kernel shape of the lanes engine (persistent, texture gather)
     int lane_trail_tile = 8;   // trail tile of the lanes engine (streaming, 16-row strips)
+    int max_lanes = 0;         // lanes of the lanes engine (0: one per colony, at most 64)
     std::vector<cudaStream_t> lanes;
     std::vector<cudaEvent_t> lane_ev;
     cudaEvent_t fork_ev = nullptr;
@@ -441,7 +451,8 @@ constexpr size_t kMaxLanes = 64;
 int ensure_lanes(slime_ensemble* e) {
     if (!e->lanes.empty()) return SLIME_OK;
     const size_t k = e->colonies.size();
-    const size_t nl = k < kMaxLanes ? k : kMaxLanes;
+    const size_t cap = e->max_lanes > 0 ? (size_t)e->max_lanes : kMaxLanes;
+    const size_t nl = k < cap ? k : cap;
     ECK(cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming), "creating lane events");
     for (size_t l = 0; l < nl; l++) {
         cudaStream_t s = nullptr;
@@ -502,15 +513,21 @@ cudaError_t enqueue_lane_steps(slime_ensemble* e, uint32_t m) {
             int cur = e->cur;
             for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) {
                 float* tin = e->trail[cur] + c.trail_off;
+                float* tout = e->trail[1 - cur] + c.trail_off;
                 uint32_t* cin = e->counts[cur] + c.trail_off;
+                uint8_t* min = c.marks ? e->marks[cur] + c.trail_off : nullptr;
                 if (c.n) {
                     ce = launch_agents(c.dev, a, tin, cin, s, e->lane_agent_shape, nullptr, tex_shape ? c.tex[cur] : 0,
-                                       nullptr, after_kernel);
+                                       min, after_kernel);
                     after_kernel = true;
                     if (ce != cudaSuccess) break;
                 }
-                ce = launch_trail(c.dev, e->lane_trail_tile, tin, cin, e->trail[1 - cur] + c.trail_off,
-                                  e->counts[1 - cur] + c.trail_off, s, nullptr, after_kernel);
+                if (c.marks)
+                    ce = launch_trail_marks(c.dev, e->lane_trail_tile, tin, min, tout, e->marks[1 - cur] + c.trail_off,
+                                            s, nullptr, after_kernel);
+                else
+                    ce = launch_trail(c.dev, e->lane_trail_tile, tin, cin, tout, e->counts[1 - cur] + c.trail_off, s,
+                                      nullptr, after_kernel);
                 after_kernel = true;
                 cur = 1 - cur;
             }
@@ -546,6 +563,63 @@ int check_barrier(slime_ensemble* e) {
         return ens_fail(e, SLIME_ERR_DEVICE_TIMEOUT, "the ensemble's grid barrier timed out");
     }
     return SLIME_OK;
+}
+
+// Whether colony c records its deposits as byte marks in the next steps:
+// the lanes engine on a streaming trail tile, a deposition of at least 1 on
+// a clean trail that the colony's steps keep clean (every deposit then folds
+// the cell to 1, so whether a cell received any carries the fold).
+bool colony_marks(const slime_ensemble* e, const Colony& c) {
+    return e->engine == SLIME_ENSEMBLE_LANES && c.n > 0 && c.trail_clean && c.dev.dep >= 1.0f &&
+           keeps_trail_clean(c.dev) && trail_tile_streams(c.dev, e->lane_trail_tile);
+}
+
+// Before a chunk: each colony's record kind (a change drops the captured
+// graphs, which hold it), and the record the chunk's first step writes
+// (counts[cur] or marks[cur]) cleared where steps of the other kind or the
+// other engine left deposits in it.
+int prepare_ens_deposits(slime_ensemble* e) {
+    bool changed = false;
+    for (Colony& c : e->colonies) {
+        const bool mk = colony_marks(e, c);
+        changed = changed || mk != c.marks;
+        c.marks = mk;
+    }
+    if (changed) ens_invalidate(e);
+    const int cur = e->cur;
+    for (Colony& c : e->colonies) {
+        const size_t cells = (size_t)c.W * c.H;
+        if (c.marks) {
+            if (!e->marks[0]) {
+                for (int i = 0; i < 2; i++) {
+                    ECK(dev_alloc((void**)&e->marks[i], e->total_cells), "allocating deposit marks");
+                    ECK(cudaMemsetAsync(e->marks[i], 0, e->total_cells, e->stream), "clearing deposit marks");
+                }
+                for (Colony& o : e->colonies) o.marks_dirty[0] = o.marks_dirty[1] = false;
+            }
+            if (c.marks_dirty[cur]) {
+                ECK(cudaMemsetAsync(e->marks[cur] + c.trail_off, 0, cells, e->stream), "clearing deposit marks");
+                c.marks_dirty[cur] = false;
+            }
+        } else if (c.counts_dirty[cur]) {
+            ECK(cudaMemsetAsync(e->counts[cur] + c.trail_off, 0, cells * sizeof(uint32_t), e->stream),
+                "clearing deposit counts");
+            c.counts_dirty[cur] = false;
+        }
+    }
+    return SLIME_OK;
+}
+
+// After m steps (e->cur already advanced): the last step's record holds its
+// deposits, its trail pass cleared the other one.
+void after_ens_steps(slime_ensemble* e, uint32_t m) {
+    if (m == 0) return;
+    for (Colony& c : e->colonies) {
+        bool* dirty = c.marks ? c.marks_dirty : c.counts_dirty;
+        dirty[e->cur] = false;
+        dirty[1 - e->cur] = true;
+        c.trail_clean = c.trail_clean && keeps_trail_clean(c.dev);
+    }
 }
 
 // The graph of m steps of the current engine from the current parity,
@@ -586,6 +660,10 @@ int prepare_ens_steps(slime_ensemble* e, uint32_t n) {
         int rc = ensure_lanes(e);
         if (rc != SLIME_OK) return rc;
     }
+    // the record kinds the graphs hold (clearing a stale record early is
+    // what the next step would do first)
+    int rc = prepare_ens_deposits(e);
+    if (rc != SLIME_OK) return rc;
     const int saved = e->cur;
     uint64_t steps = e->steps_done;
     while (n > 0) {
@@ -619,29 +697,24 @@ int run_ens_steps(slime_ensemble* e, uint32_t n) {
             int rc = ensure_lanes(e);
             if (rc != SLIME_OK) return rc;
         }
+        int rc = prepare_ens_deposits(e);
+        if (rc != SLIME_OK) return rc;
         const uint64_t kernels = lanes ? m * lane_kernels_per_step(e) : m;
-        if (e->use_graphs || lanes) {
-            cudaGraphExec_t exec = chunk_graph(e, m);
-            if (!exec) {
-                if (lanes) { // the lane chains run directly
-                    ECK(enqueue_lane_steps(e, m), "launching ensemble lanes");
-                    e->last_chunk_graph = false;
-                    e->launches += kernels;
-                    e->steps_done += m;
-                    n -= m;
-                    continue;
-                }
-                // cooperative launches that cannot be captured run directly
-                e->use_graphs = false;
-                continue;
-            }
+        cudaGraphExec_t exec = (e->use_graphs || lanes) ? chunk_graph(e, m) : nullptr;
+        if (exec) {
             ECK(cudaGraphLaunch(exec, e->stream), "launching ensemble graph");
             if (m & 1) e->cur = 1 - e->cur;
             e->last_chunk_graph = true;
+        } else if (lanes) { // the lane chains run directly when they cannot be captured
+            ECK(enqueue_lane_steps(e, m), "launching ensemble lanes");
+            e->last_chunk_graph = false;
         } else {
+            // cooperative launches that cannot be captured run directly from now on
+            e->use_graphs = false;
             for (uint32_t i = 0; i < m; i++) ECK(enqueue_ens_step(e), "launching ensemble step");
             e->last_chunk_graph = false;
         }
+        after_ens_steps(e, m);
         e->launches += kernels;
         e->steps_done += m;
         n -= m;
@@ -781,8 +854,9 @@ void slime_ensemble_destroy(slime_ensemble* e) {
     for (Colony& c : e->colonies)
         for (int i = 0; i < 2; i++)
             if (c.tex[i]) cudaDestroyTextureObject(c.tex[i]);
-    void* ptrs[] = {e->agent_block, e->ids, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->d_cols,
-                    e->d_agent_items, e->d_strip_items, e->d_bar, e->staging, e->reorder.buf};
+    void* ptrs[] = {e->agent_block, e->ids, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->marks[0],
+                    e->marks[1], e->d_cols, e->d_agent_items, e->d_strip_items, e->d_bar, e->staging,
+                    e->reorder.buf};
     for (void* p : ptrs)
         if (p) dev_free(p);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -886,7 +960,12 @@ int slime_ensemble_upload_trail(slime_ensemble* e, uint32_t j, const float* trai
     if (!trail || n_cells != (uint64_t)c.W * c.H) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "trail size mismatch");
     ECK(cudaMemcpyAsync(e->trail[e->cur] + c.trail_off, trail, n_cells * sizeof(float), cudaMemcpyHostToDevice,
                         e->stream), "uploading trail");
+    // deposit marks need every value finite and >= 0 (or +inf): checked
+    // while the copy runs
+    bool clean = true;
+    for (uint64_t i = 0; i < n_cells; i++) clean = clean && (trail[i] >= 0.0f);
     ECK(cudaStreamSynchronize(e->stream), "uploading trail");
+    c.trail_clean = clean;
     return SLIME_OK;
 }
 
@@ -926,8 +1005,35 @@ int slime_ensemble_get_stream(slime_ensemble* e, void** stream) {
     return SLIME_OK;
 }
 
-int slime_ensemble_set_engine(slime_ensemble* e, uint32_t engine, uint32_t agent_shape, uint32_t trail_tile) {
+int slime_ensemble_profile_reorder(slime_ensemble* e, uint32_t reps, double* ms) {
+    if (!e || !ms) return SLIME_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(e->device);
+    *ms = 0.0;
+    if (reps == 0) return SLIME_OK;
+    // the first reorder sizes the sort scratch: untimed
+    int rc = reorder_all(e);
+    if (rc != SLIME_OK) return rc;
+    cudaEvent_t e0, e1;
+    ECK(cudaEventCreate(&e0), "creating events");
+    ECK(cudaEventCreate(&e1), "creating events");
+    cudaError_t ce = cudaEventRecord(e0, e->stream);
+    for (uint32_t r = 0; r < reps && rc == SLIME_OK && ce == cudaSuccess; r++) rc = reorder_all(e);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e1, e->stream);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != SLIME_OK) return rc;
+    ECK(ce, "timing reorders");
+    *ms = t;
+    return SLIME_OK;
+}
+
+int slime_ensemble_set_engine(slime_ensemble* e, uint32_t engine, uint32_t agent_shape, uint32_t trail_tile,
+                              uint32_t lanes) {
     if (!e) return SLIME_ERR_INVALID_ARGUMENT;
+    if (lanes > kMaxLanes) return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "at most 64 lanes");
     if (engine != SLIME_ENSEMBLE_COOPERATIVE && engine != SLIME_ENSEMBLE_LANES)
         return ens_fail(e, SLIME_ERR_INVALID_ARGUMENT, "unknown ensemble engine");
     if (agent_shape >= (uint32_t)agent_shape_count() || trail_tile >= (uint32_t)kTrailTileTma)
@@ -941,6 +1047,10 @@ int slime_ensemble_set_engine(slime_ensemble* e, uint32_t engine, uint32_t agent
     e->lane_agent_shape = (int)agent_shape;
     e->lane_trail_tile = (int)trail_tile;
     ens_invalidate(e);
+    if (lanes != (uint32_t)e->max_lanes) {
+        destroy_lanes(e);
+        e->max_lanes = (int)lanes;
+    }
     return SLIME_OK;
 }
 
@@ -995,6 +1105,7 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
     const int saved_cur = e->cur;
     const bool saved_graphs = e->use_graphs;
     e->use_graphs = false;
+    const std::vector<Colony> saved_cols = e->colonies; // deposit-record flags
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1075,8 +1186,19 @@ int slime_ensemble_autotune(slime_ensemble* e, uint32_t reps) {
         cudaMemcpyAsync(e->counts[i], s + abytes + 2 * tbytes + i * tbytes, tbytes, cudaMemcpyDeviceToDevice,
                         e->stream);
     }
+    // the trials' deposit marks are stale: every mark region starts clear
+    for (int i = 0; i < 2; i++)
+        if (e->marks[i]) cudaMemsetAsync(e->marks[i], 0, e->total_cells, e->stream);
     cudaStreamSynchronize(e->stream);
     dev_free(snap);
+    for (size_t j = 0; j < e->colonies.size(); j++) {
+        Colony& c = e->colonies[j];
+        const Colony& o = saved_cols[j];
+        c.trail_clean = o.trail_clean;
+        c.counts_dirty[0] = o.counts_dirty[0];
+        c.counts_dirty[1] = o.counts_dirty[1];
+        c.marks_dirty[0] = c.marks_dirty[1] = false;
+    }
     e->cur = saved_cur;
     e->use_graphs = saved_graphs;
     e->steps_done = saved_steps;
@@ -1139,6 +1261,7 @@ int slime_ensemble_get_info(const slime_ensemble* e, SlimeEnsembleInfo* out) {
     out->lanes = (uint32_t)e->lanes.size();
     out->lane_agent_shape = (uint32_t)e->lane_agent_shape;
     out->lane_trail_tile = (uint32_t)e->lane_trail_tile;
+    for (const Colony& c : e->colonies) out->marks_colonies += c.marks ? 1u : 0u;
     return SLIME_OK;
 }
 

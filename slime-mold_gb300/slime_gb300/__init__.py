@@ -417,6 +417,12 @@ class Ensemble:
         """Capture the graphs of the next n_steps steps now (slime_ensemble_prepare_steps)."""
         self._check(self._L.slime_ensemble_prepare_steps(self._h, n_steps), "prepare_steps")
 
+    def profile_reorder(self, reps=3):
+        """Milliseconds that `reps` back-to-back reorders of every colony take."""
+        ms = C.c_double()
+        self._check(self._L.slime_ensemble_profile_reorder(self._h, reps, C.byref(ms)), "profile_reorder")
+        return ms.value
+
     def sync(self):
         self._check(self._L.slime_ensemble_sync(self._h), "sync")
 
@@ -428,11 +434,11 @@ class Ensemble:
     def autotune(self, reps=5):
         self._check(self._L.slime_ensemble_autotune(self._h, reps), "autotune")
 
-    def set_engine(self, engine, lane_agent_shape=13, lane_trail_tile=8):
+    def set_engine(self, engine, lane_agent_shape=13, lane_trail_tile=8, lanes=0):
         """Pick the stepping engine by hand (slime_ensemble_set_engine):
-        ENSEMBLE_COOPERATIVE or ENSEMBLE_LANES with its agent shape and trail
-        tile."""
-        self._check(self._L.slime_ensemble_set_engine(self._h, engine, lane_agent_shape, lane_trail_tile),
+        ENSEMBLE_COOPERATIVE or ENSEMBLE_LANES with its agent shape, trail
+        tile and number of lanes (0: one per colony, at most 64)."""
+        self._check(self._L.slime_ensemble_set_engine(self._h, engine, lane_agent_shape, lane_trail_tile, lanes),
                     "set_engine")
 
     def set_shape(self, strip_rows=16, blocks_per_sm=0, agents_per_thread=4):

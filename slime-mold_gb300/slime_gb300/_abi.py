@@ -134,7 +134,7 @@ class SlimeEnsembleInfo(C.Structure):
         ("lanes", C.c_uint32),
         ("lane_agent_shape", C.c_uint32),
         ("lane_trail_tile", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("marks_colonies", C.c_uint32),
     ]
 
 
@@ -212,11 +212,12 @@ SIGNATURES = {
     "slime_ensemble_set_reorder": (C.c_int, [P, C.c_uint32, C.c_uint32]),
     "slime_ensemble_step": (C.c_int, [P, C.c_uint32]),
     "slime_ensemble_prepare_steps": (C.c_int, [P, C.c_uint32]),
+    "slime_ensemble_profile_reorder": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_double)]),
     "slime_ensemble_sync": (C.c_int, [P]),
     "slime_ensemble_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
     "slime_ensemble_autotune": (C.c_int, [P, C.c_uint32]),
     "slime_ensemble_set_shape": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
-    "slime_ensemble_set_engine": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "slime_ensemble_set_engine": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
     "slime_ensemble_launch_count": (C.c_int, [P, C.POINTER(C.c_uint64)]),
     "slime_ensemble_get_info": (C.c_int, [P, C.POINTER(SlimeEnsembleInfo)]),
     "slime_ensemble_selftest_barrier_timeout": (C.c_int, [P]),

@@ -52,6 +52,8 @@ def test_ensemble_matches_plain_runs(gpu, blur_mode, radius, reorder, engine):
     # the step launches were captured and replayed as graphs
     assert info.graphs_in_use == 1, "capture of the step launches fell back to direct launches"
     assert info.engine == engine and info.lanes == (len(cols) if engine == sg.ENSEMBLE_LANES else 0)
+    if engine == sg.ENSEMBLE_COOPERATIVE:
+        assert info.marks_colonies == 0
     assert (info.n_colonies, info.steps_done) == (len(cols), 7)
     assert info.total_agents == sum(c[2] for c in cols) and info.total_cells == sum(c[0] * c[1] for c in cols)
     assert info.grid_blocks > 0 and info.strip_rows in (8, 16, 32)
@@ -113,13 +115,25 @@ def test_lanes_engine_shapes_and_params_update(gpu, shape, tile):
     for j, (W, H, n, p, agents, trail) in enumerate(cols):
         ens.upload_agents(j, agents)
         ens.upload_trail(j, trail)
+    assert ens.profile_reorder(2) > 0  # reorders change only the slot order: results below still match
     ens.prepare_steps(3)
     assert ens.info().steps_done == 0
     ens.step(3)
-    q = cols[1][3].copy()
-    q.agent_turn_speed = 0.05
-    q.decay_factor = 0.5
-    ens.set_params(1, q)
+    marks_before = ens.info().marks_colonies
+    streams = tile in (7, 8, 9)
+    assert (marks_before > 0) == streams  # deposition >= 1 on a streaming tile: byte marks
+    # colony 1: new decay and turn; colonies 2 and 4: deposition moved across 1,
+    # so that their deposit records switch between counts and marks mid-run
+    changed = {}
+    for j in (1, 2, 4):
+        q = cols[j][3].copy()
+        if j == 1:
+            q.agent_turn_speed = 0.05
+            q.decay_factor = 0.5
+        else:
+            q.pheromone_deposition_amount = 0.6 if q.pheromone_deposition_amount >= 1.0 else 1.5
+        ens.set_params(j, q)
+        changed[j] = q
     ens.step(4)
     ens.sync()
     info = ens.info()
@@ -130,8 +144,8 @@ def test_lanes_engine_shapes_and_params_update(gpu, shape, tile):
             sim.upload_agents(agents)
             sim.upload_trail(trail)
             sim.step(3)
-            if j == 1:
-                sim.set_params(q)
+            if j in changed:
+                sim.set_params(changed[j])
             sim.step(4)
             assert_bitexact(ens.download_agents(j), sim.download_agents(), f"colony {j} agents")
             assert_bitexact(ens.download_trail(j), sim.download_trail(), f"colony {j} trail")
