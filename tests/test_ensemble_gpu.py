@@ -158,6 +158,45 @@ def test_lanes_engine_shapes_and_params_update(gpu, shape, tile):
     ens.close()
 
 
+@pytest.mark.parametrize("lanes", [0, 3])
+def test_lanes_engine_many_small_colonies(gpu, lanes):
+    """70 small colonies (some without agents): more colonies than lanes, so
+    a lane chains several colonies' kernels one after another (programmatic
+    dependent launches across colonies); every colony matches its plain run."""
+    import slime_gb300 as sg
+    rng = np.random.default_rng(23)
+    cols = []
+    for j in range(70):
+        W, H = 4 * int(rng.integers(2, 17)), int(rng.integers(4, 41))
+        n = 0 if j % 11 == 5 else int(rng.integers(1, 2000))
+        p = config0_params(W, H, blur_mode=1, agent_speed_min=20.0, agent_speed_max=60.0,
+                           agent_jitter=float(rng.uniform(0, 0.2)),
+                           pheromone_deposition_amount=float(rng.uniform(0.5, 2.0)))
+        agents = agents_uniform(n, W, H, 20.0, 60.0, seed=500 + j) if n else np.zeros((0, 4), np.float32)
+        cols.append((W, H, n, p, agents, rng.random((H, W), dtype=np.float32)))
+    ens = sg.Ensemble([c[0] for c in cols], [c[1] for c in cols], [c[2] for c in cols], [c[3] for c in cols])
+    ens.set_engine(sg.ENSEMBLE_LANES, 13, 8, lanes)
+    ens.set_reorder(2, 1)
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        if n:
+            ens.upload_agents(j, agents)
+        ens.upload_trail(j, trail)
+    ens.step(5)
+    ens.sync()
+    info = ens.info()
+    assert info.lanes == (lanes if lanes else 64) and info.graphs_in_use == 1
+    for j, (W, H, n, p, agents, trail) in enumerate(cols):
+        with sg.Simulation(W, H, n, p) as sim:
+            if n:
+                sim.upload_agents(agents)
+            sim.upload_trail(trail)
+            sim.step(5)
+            if n:
+                assert_bitexact(ens.download_agents(j), sim.download_agents(), f"colony {j} agents")
+            assert_bitexact(ens.download_trail(j), sim.download_trail(), f"colony {j} trail")
+    ens.close()
+
+
 def test_ensemble_autotune_and_params_update(gpu):
     import slime_gb300 as sg
     cols = colony_setup(11, 1)
