@@ -446,6 +446,16 @@ AgentsSoA colony_soa(slime_ensemble* e, const Colony& c) {
 
 constexpr size_t kMaxLanes = 64;
 
+void destroy_lanes(slime_ensemble* e) {
+    for (cudaStream_t s : e->lanes) cudaStreamDestroy(s);
+    for (cudaEvent_t ev : e->lane_ev) cudaEventDestroy(ev);
+    if (e->fork_ev) cudaEventDestroy(e->fork_ev);
+    e->lanes.clear();
+    e->lane_ev.clear();
+    e->fork_ev = nullptr;
+    e->lane_cols.clear();
+}
+
 // Lanes and their colonies: the colonies by descending work (agents plus a
 // quarter of the cells), each onto the lane with the least work so far.
 int ensure_lanes(slime_ensemble* e) {
@@ -453,14 +463,18 @@ int ensure_lanes(slime_ensemble* e) {
     const size_t k = e->colonies.size();
     const size_t cap = e->max_lanes > 0 ? (size_t)e->max_lanes : kMaxLanes;
     const size_t nl = k < cap ? k : cap;
-    ECK(cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming), "creating lane events");
-    for (size_t l = 0; l < nl; l++) {
+    cudaError_t ce = cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming);
+    for (size_t l = 0; l < nl && ce == cudaSuccess; l++) {
         cudaStream_t s = nullptr;
         cudaEvent_t ev = nullptr;
-        ECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "creating lanes");
+        if ((ce = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) break;
         e->lanes.push_back(s);
-        ECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "creating lane events");
+        if ((ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) break;
         e->lane_ev.push_back(ev);
+    }
+    if (ce != cudaSuccess) { // no half-built lanes: the next step tries again
+        destroy_lanes(e);
+        return cuda_error(e->err, ce, "creating lanes");
     }
     std::vector<uint32_t> order(k);
     for (size_t j = 0; j < k; j++) order[j] = (uint32_t)j;
@@ -481,15 +495,6 @@ int ensure_lanes(slime_ensemble* e) {
     return SLIME_OK;
 }
 
-void destroy_lanes(slime_ensemble* e) {
-    for (cudaStream_t s : e->lanes) cudaStreamDestroy(s);
-    for (cudaEvent_t ev : e->lane_ev) cudaEventDestroy(ev);
-    if (e->fork_ev) cudaEventDestroy(e->fork_ev);
-    e->lanes.clear();
-    e->lane_ev.clear();
-    e->fork_ev = nullptr;
-    e->lane_cols.clear();
-}
 
 // Kernels one lanes-engine step enqueues.
 uint64_t lane_kernels_per_step(const slime_ensemble* e) {
