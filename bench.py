@@ -502,6 +502,9 @@ def measure_plain(sim, stream, params, agents, args, barrier, local, torch):
     sim.upload_agents(agents)
     sim.clear_trail()
     sim.set_params(params)
+    # step 0 of the seeded run for every mode: the Morton reorder falls due
+    # at once (the upload left the agents unsorted), with or without tuning
+    sim.set_steps_done(0)
     if not (args.trail_tile and args.agent_shape):
         sim.autotune(5)
     tuned = sim.info()
