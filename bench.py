@@ -329,9 +329,10 @@ def ensemble_comparisons(args, cols, cells, agents_total, R):
 
 
 def run_ensemble(args):
-    """Batched ensemble: one persistent launch per step over 64 colonies,
-    against the same colonies run one after the other with the plain path,
-    and against the plain 4096^2 per-cell throughput."""
+    """Batched ensemble over 64 colonies (the autotuned engine: lanes of
+    single-colony kernel chains in one CUDA graph, or one cooperative launch
+    per step), against the same colonies run one after the other with the
+    plain path, and against the plain 4096^2 per-cell throughput."""
     import torch
     import slime_gb300 as sg
     torch.cuda.set_device(0)

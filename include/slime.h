@@ -325,8 +325,9 @@ int slime_forward_record(slime_ctx* ctx, uint32_t n_steps, uint32_t ckpt_every);
 int slime_backward(slime_ctx* ctx, const float* dl_dtrail_final, SlimeGrads* grads, float* d_trail0);
 
 /* ------------------------------------------------ batched ensemble */
-/* Independent colonies of uneven sizes advanced together: one launch per
- * step covers every colony. */
+/* Independent colonies of uneven sizes advanced together by one of two
+ * engines (SLIME_ENSEMBLE_LANES / SLIME_ENSEMBLE_COOPERATIVE below): every
+ * colony's result is the one a single context would produce for it. */
 typedef struct slime_ensemble slime_ensemble;
 
 slime_ensemble* slime_ensemble_create(uint32_t n_colonies, const uint32_t* widths,

@@ -1,4 +1,5 @@
-"""The batched ensemble (one persistent launch per step over colonies of
+"""The batched ensemble (both engines: per-colony kernel chains on capture
+lanes, and one cooperative persistent launch per step, over colonies of
 uneven sizes and parameters) against one plain Simulation per colony and the
 CPU oracle, bit for bit."""
 import numpy as np
