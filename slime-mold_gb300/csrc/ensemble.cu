@@ -206,7 +206,9 @@ __device__ __forceinline__ void agent_item(const DevParams& sp, const DevColony&
 
 // Four agents per thread at four blocks per SM (a 64-register cap; a few
 // bytes spilled), or two per thread stepped as one pair at three blocks per
-// SM (80 registers): the autotuner times both.
+// SM (80 registers): the autotuner times both (on 64 colonies of 256^2 to
+// 2048^2, 3.54 against 3.70 ms per step; the pair loses the prefetch of the
+// next group that the plain persistent kernel has).
 template <int R, bool kGauss, int ROWS, int APT>
 __global__ void __launch_bounds__(kEnsThreads, APT == 4 ? 4 : 3) ensemble_step_kernel(
     const DevColony* __restrict__ cols, const uint2* __restrict__ agent_items, uint32_t n_agent_items,
