@@ -89,6 +89,24 @@ __device__ __forceinline__ void step_group(const DevParams& p, float* x, float* 
     }
 }
 
+// The last group of a pass when fewer than APT of its agents are live, out
+// of line: it runs for one thread of a launch at most, and inlined it would
+// add a second copy of the agent code to the loop (instruction-cache space).
+template <int APT>
+struct GroupState {
+    float x[APT], y[APT], th[APT], v[APT];
+    uint32_t id[APT];
+    int cell[APT];
+};
+template <int APT, class Trail>
+__device__ __noinline__ GroupState<APT> step_partial_group(const DevParams& p, GroupState<APT> s, uint32_t live,
+                                                           const Trail trail) {
+#pragma unroll
+    for (int j = 0; j < APT; j++)
+        s.cell[j] = (uint32_t)j < live ? agent_step(p, s.x[j], s.y[j], s.th[j], s.v[j], (int32_t)s.id[j], trail) : -1;
+    return s;
+}
+
 // A thread moves APT consecutive slots with one vector load/store per field.
 // MINB > 0 asks the compiler to fit MINB blocks per SM (caps registers).
 // Trail is the reader of the sensed trail (TrailPtr or TrailTex).
@@ -235,9 +253,24 @@ __global__ void __launch_bounds__(BS, MINB) agents_persistent_kernel(
         if (base + APT <= n) {
             step_group<APT>(p, x, y, th, v, id, trail, cell);
         } else {
+            GroupState<APT> s;
 #pragma unroll
-            for (int j = 0; j < APT; j++)
-                cell[j] = (base + j < n) ? agent_step(p, x[j], y[j], th[j], v[j], (int32_t)id[j], trail) : -1;
+            for (int j = 0; j < APT; j++) {
+                s.x[j] = x[j];
+                s.y[j] = y[j];
+                s.th[j] = th[j];
+                s.v[j] = v[j];
+                s.id[j] = id[j];
+            }
+            s = step_partial_group<APT>(p, s, (uint32_t)(n - base), trail);
+#pragma unroll
+            for (int j = 0; j < APT; j++) {
+                x[j] = s.x[j];
+                y[j] = s.y[j];
+                th[j] = s.th[j];
+                v[j] = s.v[j];
+                cell[j] = s.cell[j];
+            }
         }
 #pragma unroll
         for (int j = 0; j < APT; j++)
