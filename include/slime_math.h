@@ -178,6 +178,14 @@ SLM_FN float slm_fmod(float x, float y) {
     return in0 ? x : (in1 ? r1 : r2);
 }
 
+/* The general case of slm_wrap, out of line (values more than a period
+ * outside [0, n), -n, -0, NaN, infinities, n <= 0). */
+SLM_COLD_FN float slm_wrap_general(float v, float n) {
+    float r = slm_fmod(v, n);
+    if (r < 0.0f) r = slm_add(r, n);
+    return r;
+}
+
 /* The shader's toroidal wrap, `v = v % n; if (v < 0.0) { v = v + n; }`
  * (compute.wgsl:121-122, :130-133), for n > 0.  Values within one period of
  * [0, n) take the exact short paths; -n and -0 give -0 as the remainder does. */
@@ -185,9 +193,7 @@ SLM_FN float slm_wrap(float v, float n) {
     if (v >= 0.0f && v < n) return v;
     if (v >= n && v < slm_add(n, n)) return slm_sub(v, n);
     if (v < 0.0f && v > -n) return slm_add(v, n);
-    float r = slm_fmod(v, n);
-    if (r < 0.0f) r = slm_add(r, n);
-    return r;
+    return slm_wrap_general(v, n);
 }
 
 /* WGSL i32(f32): truncate toward zero, saturate to the i32 range, NaN -> 0.
@@ -474,10 +480,12 @@ SLM_FN void slm_reduce_pio2_hash(float x, float* r_out, int* q_out) {
 /* The quadrant step of slm_sincos: (sin, cos) from the polynomials s, c and
  * the quadrant q. */
 SLM_FN void slm_sincos_quadrant(float s, float c, int q, float* s_out, float* c_out) {
-    float a = (q & 1) ? c : s;
-    float bb = (q & 1) ? s : c;
-    *s_out = (q & 2) ? -a : a;
-    *c_out = ((q + 1) & 2) ? -bb : bb;
+    const float a = (q & 1) ? c : s;
+    const float bb = (q & 1) ? s : c;
+    /* negation as a flip of the sign bit: bit 1 of q for the sine, of q + 1
+     * for the cosine, shifted to bit 31 */
+    *s_out = slm_u2f_bits(slm_f2u_bits(a) ^ (((uint32_t)q << 30) & 0x80000000u));
+    *c_out = slm_u2f_bits(slm_f2u_bits(bb) ^ (((uint32_t)q + 1u) << 30 & 0x80000000u));
 }
 
 /* sin and cos from the reduced argument r and the quadrant q. */
