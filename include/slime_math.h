@@ -149,7 +149,17 @@ SLM_FN float slm_max(float a, float b) {
 SLM_FN float slm_clamp(float e, float lo, float hi) { return slm_min(slm_max(e, lo), hi); }
 /* WGSL sign: 1, -1 or 0 (NaN maps to 0). */
 SLM_FN float slm_sign(float x) { return (x > 0.0f) ? 1.0f : ((x < 0.0f) ? -1.0f : 0.0f); }
-SLM_FN float slm_abs(float x) { return slm_u2f_bits(slm_f2u_bits(x) & 0x7fffffffu); }
+/* |x|: the sign bit cleared.  On the device abs.f32, which folds into the
+ * instruction that uses it as an operand modifier; its result for a NaN is
+ * some NaN, and every use here (compares, minimumNumber) treats all NaNs
+ * alike. */
+SLM_FN float slm_abs(float x) {
+#if defined(__CUDA_ARCH__)
+    return fabsf(x);
+#else
+    return slm_u2f_bits(slm_f2u_bits(x) & 0x7fffffffu);
+#endif
+}
 SLM_FN float slm_floor(float x) { return floorf(x); }
 /* WGSL fract(e) = e - floor(e). */
 SLM_FN float slm_fract(float x) { return slm_sub(x, slm_floor(x)); }

@@ -22,8 +22,9 @@ namespace slime {
 // point filtering, clamped, unnormalised coordinates); gathering at
 // (x0 + 1, y0 + 1) selects texels x0..x0+1, y0..y0+1, returned as
 // w = (x0, y0), z = (x0+1, y0), x = (x0, y0+1), y = (x0+1, y0+1).  An
-// out-of-grid sample gathers at (1, 1) (always inside a trail of at least
-// 2x2) and is discarded.  The in-grid test needs no integer x0: with
+// out-of-grid sample gathers wherever its coordinates point (the clamped
+// addressing keeps every coordinate, infinite or NaN included, on the
+// texture) and is discarded.  The in-grid test needs no integer x0: with
 // fx = floor(px), 0 <= i32(fx) < W - 1 holds exactly when
 // !(fx < 0) && !(fx >= W - 1) for every fx, NaN included (i32(NaN) = 0 is
 // in the grid, and NaN fails both compares), on trails at least 2 wide and
@@ -76,7 +77,7 @@ struct TrailTex {
         // in range, f32(x0 + 1) == floor(px) + 1 exactly (|x0| < 2^24); a NaN
         // position passes the test (i32(NaN) = 0) and gathers at a NaN
         // coordinate, whose texels do not matter: its weights are NaN
-        k.g = tex2Dgather<float4>(t, k.ok ? fx + 1.0f : 1.0f, k.ok ? fy + 1.0f : 1.0f, 0);
+        k.g = tex2Dgather<float4>(t, fx + 1.0f, fy + 1.0f, 0);
         return k;
     }
     __device__ __forceinline__ static float value(const Tap& k) {
@@ -128,7 +129,10 @@ __device__ __forceinline__ void agent_turn(const DevParams& p, float& angle, flo
     float turned = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
     angle = (turn_left || turn_right) ? turned : angle;
 
-    angle = slm_add(angle, slm_mul(slm_sub(slm_mul(rv, 2.0f), 1.0f), p.jitter));
+    // (rv * 2.0 - 1.0) as one fused multiply-add: the product is exact (a
+    // power-of-two scaling), so rounding once after the sum gives the bits of
+    // the shader's product-then-difference
+    angle = slm_add(angle, slm_mul(slm_fma(rv, 2.0f, -1.0f), p.jitter));
     angle = slm_wrap(angle, SLM_WGSL_TWO_PI);
 }
 
