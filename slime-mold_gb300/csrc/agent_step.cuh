@@ -181,19 +181,50 @@ __device__ __forceinline__ int agent_step(const DevParams& p, float& x, float& y
 // sin/cos polynomials that the two evaluate on different arguments (centre
 // directions, jitter hashes, moves) paired into packed fused multiply-adds,
 // as are each agent's two side directions.  Bit for bit agent_step twice.
+// The two agents' sensor directions (centre, left, right), (cos, sin) each.
+struct SensorDirs2 {
+    float cca, sca, ccb, scb, cla, sla, cra, sra, clb, slb, crb, srb;
+};
+
+// The sensor directions of two agents in either sensor mode, with every
+// sin/cos taking its own range test: the general case, out of line.
+static __device__ __noinline__ SensorDirs2 sensor_dirs2_general(const DevParams& p, float tha, float thb) {
+    SensorDirs2 o;
+    slm_sincos2(tha, thb, &o.sca, &o.cca, &o.scb, &o.ccb);
+    if (p.sensor_mode == SLIME_SENSOR_ROTATED) {
+        slm_rotate_dirs(o.cca, o.sca, p.sensor_sin, p.sensor_cos, &o.cla, &o.sla, &o.cra, &o.sra);
+        slm_rotate_dirs(o.ccb, o.scb, p.sensor_sin, p.sensor_cos, &o.clb, &o.slb, &o.crb, &o.srb);
+    } else {
+        slm_side_dirs_shader(tha, p.sensor_angle, &o.cla, &o.sla, &o.cra, &o.sra);
+        slm_side_dirs_shader(thb, p.sensor_angle, &o.clb, &o.slb, &o.crb, &o.srb);
+    }
+    return o;
+}
+
 template <class Trail>
 __device__ __forceinline__ void agent_step2(const DevParams& p, float& xa, float& ya, float& tha, float& va,
                                             int32_t ia, float& xb, float& yb, float& thb, float& vb, int32_t ib,
                                             const Trail& trail, int& cell_a, int& cell_b) {
     float sca, cca, scb, ccb;
-    slm_sincos2(tha, thb, &sca, &cca, &scb, &ccb);
     float cla, sla, cra, sra, clb, slb, crb, srb;
-    if (p.sensor_mode == SLIME_SENSOR_ROTATED) {
-        slm_rotate_dirs(cca, sca, p.sensor_sin, p.sensor_cos, &cla, &sla, &cra, &sra);
-        slm_rotate_dirs(ccb, scb, p.sensor_sin, p.sensor_cos, &clb, &slb, &crb, &srb);
+    if (slm_abs(tha) < 4000.0f && slm_abs(thb) < 4000.0f && slm_abs(p.sensor_angle) < 64.0f) {
+        // every sensor angle, angle -/+ a included, is below 4096 in magnitude
+        // (all the shader produces after its first step): the packed
+        // Cody-Waite forms the range tests would pick, without the tests
+        slm_sincos2_cw(tha, thb, &sca, &cca, &scb, &ccb);
+        if (p.sensor_mode == SLIME_SENSOR_ROTATED) {
+            slm_rotate_dirs(cca, sca, p.sensor_sin, p.sensor_cos, &cla, &sla, &cra, &sra);
+            slm_rotate_dirs(ccb, scb, p.sensor_sin, p.sensor_cos, &clb, &slb, &crb, &srb);
+        } else {
+            const float a = p.sensor_angle;
+            slm_sincos2_cw(slm_sub(tha, a), slm_add(tha, a), &sla, &cla, &sra, &cra);
+            slm_sincos2_cw(slm_sub(thb, a), slm_add(thb, a), &slb, &clb, &srb, &crb);
+        }
     } else {
-        slm_side_dirs_shader(tha, p.sensor_angle, &cla, &sla, &cra, &sra);
-        slm_side_dirs_shader(thb, p.sensor_angle, &clb, &slb, &crb, &srb);
+        const SensorDirs2 o = sensor_dirs2_general(p, tha, thb);
+        cca = o.cca, sca = o.sca, ccb = o.ccb, scb = o.scb;
+        cla = o.cla, sla = o.sla, cra = o.cra, sra = o.sra;
+        clb = o.clb, slb = o.slb, crb = o.crb, srb = o.srb;
     }
     const float d = p.sensor_dist;
     const typename Trail::Tap la = trail.fetch(p, slm_add(xa, slm_mul(d, cla)), slm_add(ya, slm_mul(d, sla)));
@@ -207,8 +238,10 @@ __device__ __forceinline__ void agent_step2(const DevParams& p, float& xa, float
     slm_jitter_hash2(ia, xa, ya, ib, xb, yb, &rva, &rvb);
     agent_turn(p, tha, va, rva, Trail::value(la), Trail::value(ra), Trail::value(ca));
     agent_turn(p, thb, vb, rvb, Trail::value(lb), Trail::value(rb), Trail::value(cb));
+    // the new headings are wrapped into [0, 2pi] (or NaN, whose sin and cos
+    // are NaN on every path), so the packed Cody-Waite form needs no range test
     float sma, cma, smb, cmb;
-    slm_sincos2(tha, thb, &sma, &cma, &smb, &cmb);
+    slm_sincos2_cw(tha, thb, &sma, &cma, &smb, &cmb);
     cell_a = agent_move(p, xa, ya, va, sma, cma);
     cell_b = agent_move(p, xb, yb, vb, smb, cmb);
 }
