@@ -564,8 +564,9 @@ static __device__ __forceinline__ void slm_sincos2_cw(float x0, float x1, float*
                                                       float* c1) {
     const float b0 = slm_add(slm_mul(x0, SLM_TWO_OVER_PI_F), 12582912.0f);
     const float b1 = slm_add(slm_mul(x1, SLM_TWO_OVER_PI_F), 12582912.0f);
-    /* -j, exactly: 1.5 * 2^23 - biased */
-    const float2 nj = make_float2(slm_sub(12582912.0f, b0), slm_sub(12582912.0f, b1));
+    /* -j, exactly: 1.5 * 2^23 - biased, as one packed sum (a packed sum of
+     * operands that no packed product produced rounds per lane) */
+    const float2 nj = __fadd2_rn(make_float2(12582912.0f, 12582912.0f), make_float2(-b0, -b1));
     float2 r = __ffma2_rn(nj, make_float2(SLM_PIO2_1, SLM_PIO2_1), make_float2(x0, x1));
     r = __ffma2_rn(nj, make_float2(SLM_PIO2_2, SLM_PIO2_2), r);
     r = __ffma2_rn(nj, make_float2(SLM_PIO2_3, SLM_PIO2_3), r);

@@ -124,7 +124,8 @@ __device__ __forceinline__ void agent_turn(const DevParams& p, float& angle, flo
     // compute.wgsl:98-112: keep straight, or turn toward target = angle -/+ TAU
     bool turn_left = !(center > left && center > right) && (left > right);
     bool turn_right = !(center > left && center > right) && !(left > right) && (right > left);
-    float target = turn_left ? slm_sub(angle, SLM_WGSL_TAU) : slm_add(angle, SLM_WGSL_TAU);
+    // angle - TAU or angle + TAU: the same sum with the signed constant chosen
+    float target = slm_add(angle, turn_left ? -SLM_WGSL_TAU : SLM_WGSL_TAU);
     float diff = slm_sub(target, angle);
     float turned = slm_add(angle, slm_mul(slm_min(p.turn, slm_abs(diff)), slm_sign(diff)));
     angle = (turn_left || turn_right) ? turned : angle;
