@@ -78,6 +78,7 @@ TRAFFIC_PROFILES = {
     ("plain-4096", "trail_stream_kernel"): "trail_stream_kernel_plain-4096.md",
     ("plain-8192", "agents_persistent_kernel"): "agents_kernel_plain-8192.md",
     ("plain-8192", "trail_stream_kernel"): "trail_stream_kernel_plain-8192.md",
+    ("plain-8192", "trail_tma_kernel"): "trail_tma_kernel_plain-8192.md",
 }
 
 
