@@ -98,7 +98,9 @@ __device__ __forceinline__ void fetch_row(const DevParams& p, const float* __res
         f.ht[j] = 0.0f;
         f.hk[j] = 0u;
         if (has_halo) {
-            int col = wrap_coord(hcol0 + j, p.W);
+            // hcol0 + j lies in [-R, W + R) and W >= 8 > R: one wrap, as selects
+            const int g = hcol0 + j;
+            const int col = g < 0 ? g + p.W : (g >= p.W ? g - p.W : g);
             f.ht[j] = __ldg(in + base + col);
             f.hk[j] = load_dep<kCoherent>(cin + base + col);
         }
