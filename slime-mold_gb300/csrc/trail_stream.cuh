@@ -171,14 +171,24 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     const bool has_halo = active && (left_edge || right_edge);
     const int hcol0 = left_edge ? c0 - R : c0 + 4;
     RowFetch<R, D> fa, fb;
+    // the input rows y0 - R .. y0 + ROWS + R - 1, wrapped: the first one
+    // wrapped once, each next one by a step back to 0 after H - 1
+    const auto next_row = [H](int v) { return v + 1 == H ? 0 : v + 1; };
+    int fr = wrap_coord(y0 - R, H); // the next row to fetch into registers
+    fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fa);
+    fr = next_row(fr);
+    fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fb);
+    fr = next_row(fr);
     // rows further ahead are prefetched into L2 (kPrefetchL2 rows beyond the
     // two held in registers) by the streaming kernel
     constexpr int kPrefetchL2 = kUnrolled ? 2 : 0;
+    int pr = fr; // the next row to prefetch
 #pragma unroll
     for (int q = 0; q < kPrefetchL2; q++)
-        if (2 + q < NR) prefetch_row<D>(p, in, cin, wrap_coord(y0 - R + 2 + q, H), cl);
-    fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R, H), cl, has_halo, hcol0, fa);
-    fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + 1, H), cl, has_halo, hcol0, fb);
+        if (2 + q < NR) {
+            prefetch_row<D>(p, in, cin, pr, cl);
+            pr = next_row(pr);
+        }
     // short strips unroll completely when asked to; long ones stay rolled
     // (unrolled, their live ranges exceed the register budget and spill)
     constexpr int kUnroll = (kUnrolled && NR <= 12) ? NR : 1;
@@ -186,10 +196,14 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     for (int r = 0; r < NR; r++) {
         RowFetch<R, D> cur = fa;
         fa = fb;
-        if (r + 2 < NR)
-            fetch_row<R, kCoherent, D>(p, in, cin, wrap_coord(y0 - R + r + 2, H), cl, has_halo, hcol0, fb);
-        if (kPrefetchL2 && r + 2 + kPrefetchL2 < NR)
-            prefetch_row<D>(p, in, cin, wrap_coord(y0 - R + r + 2 + kPrefetchL2, H), cl);
+        if (r + 2 < NR) { // row y0 - R + r + 2
+            fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fb);
+            fr = next_row(fr);
+        }
+        if (kPrefetchL2 && r + 2 + kPrefetchL2 < NR) { // row y0 - R + r + 2 + kPrefetchL2
+            prefetch_row<D>(p, in, cin, pr, cl);
+            pr = next_row(pr);
+        }
         // shift the window and add the new row
 #pragma unroll
         for (int q = 0; q < NWIN - 1; q++) {
