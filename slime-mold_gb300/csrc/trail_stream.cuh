@@ -164,28 +164,31 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     ExtRow<R> win[NWIN];
     float hwin[NWIN][4];
 
-    // rows are fetched two ahead of their use, halo cells with them (three or
-    // four ahead measured slower: the registers cost more warps than the
-    // deeper prefetch hides)
+    // rows are fetched kRegRows ahead of their use, halo cells with them
+    // (three: since the rows are wrapped incrementally the kernel issues
+    // fewer instructions, and the third row in flight now measures 1-2 %
+    // faster than two; before, with more instructions per row, it was slower)
     constexpr int NR = ROWS + 2 * R;
     const bool has_halo = active && (left_edge || right_edge);
     const int hcol0 = left_edge ? c0 - R : c0 + 4;
-    RowFetch<R, D> fa, fb;
+    constexpr int kRegRows = 3;
+    RowFetch<R, D> fq[kRegRows];
     // the input rows y0 - R .. y0 + ROWS + R - 1, wrapped: the first one
     // wrapped once, each next one by a step back to 0 after H - 1
     const auto next_row = [H](int v) { return v + 1 == H ? 0 : v + 1; };
     int fr = wrap_coord(y0 - R, H); // the next row to fetch into registers
-    fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fa);
-    fr = next_row(fr);
-    fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fb);
-    fr = next_row(fr);
+#pragma unroll
+    for (int q = 0; q < kRegRows; q++) {
+        if (q < NR) fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fq[q]);
+        fr = next_row(fr);
+    }
     // rows further ahead are prefetched into L2 (kPrefetchL2 rows beyond the
-    // two held in registers) by the streaming kernel
+    // ones held in registers) by the streaming kernel
     constexpr int kPrefetchL2 = kUnrolled ? 2 : 0;
     int pr = fr; // the next row to prefetch
 #pragma unroll
     for (int q = 0; q < kPrefetchL2; q++)
-        if (2 + q < NR) {
+        if (kRegRows + q < NR) {
             prefetch_row<D>(p, in, cin, pr, cl);
             pr = next_row(pr);
         }
@@ -194,13 +197,14 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     constexpr int kUnroll = (kUnrolled && NR <= 12) ? NR : 1;
 #pragma unroll kUnroll
     for (int r = 0; r < NR; r++) {
-        RowFetch<R, D> cur = fa;
-        fa = fb;
-        if (r + 2 < NR) { // row y0 - R + r + 2
-            fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fb);
+        RowFetch<R, D> cur = fq[0];
+#pragma unroll
+        for (int q = 0; q + 1 < kRegRows; q++) fq[q] = fq[q + 1];
+        if (r + kRegRows < NR) { // row y0 - R + r + kRegRows
+            fetch_row<R, kCoherent, D>(p, in, cin, fr, cl, has_halo, hcol0, fq[kRegRows - 1]);
             fr = next_row(fr);
         }
-        if (kPrefetchL2 && r + 2 + kPrefetchL2 < NR) { // row y0 - R + r + 2 + kPrefetchL2
+        if (kPrefetchL2 && r + kRegRows + kPrefetchL2 < NR) { // row y0 - R + r + kRegRows + kPrefetchL2
             prefetch_row<D>(p, in, cin, pr, cl);
             pr = next_row(pr);
         }
