@@ -165,13 +165,14 @@ __device__ __forceinline__ void process_strip_m(const DevParams& p, const float*
     float hwin[NWIN][4];
 
     // rows are fetched kRegRows ahead of their use, halo cells with them
-    // (three: since the rows are wrapped incrementally the kernel issues
-    // fewer instructions, and the third row in flight now measures 1-2 %
-    // faster than two; before, with more instructions per row, it was slower)
+    // (with byte marks three: since the rows are wrapped incrementally the
+    // kernel issues fewer instructions, and the third row in flight measures
+    // 1-2 % faster than two; with 32-bit counts, whose rows take four times
+    // the registers, two)
     constexpr int NR = ROWS + 2 * R;
     const bool has_halo = active && (left_edge || right_edge);
     const int hcol0 = left_edge ? c0 - R : c0 + 4;
-    constexpr int kRegRows = 3;
+    constexpr int kRegRows = sizeof(D) == 1 ? 3 : 2;
     RowFetch<R, D> fq[kRegRows];
     // the input rows y0 - R .. y0 + ROWS + R - 1, wrapped: the first one
     // wrapped once, each next one by a step back to 0 after H - 1
