@@ -281,6 +281,7 @@ struct slime_ensemble {
     uint64_t steps_done = 0;
     uint64_t last_reorder_step = ~0ull;
     ReorderScratch reorder;
+    ReorderScratch lane_reorder[3]; // sort scratch of the lanes engine's concurrent reorders (with `reorder`)
     float* trail[2] = {nullptr, nullptr};
     uint32_t* counts[2] = {nullptr, nullptr};
     uint8_t* marks[2] = {nullptr, nullptr}; // per-cell deposit marks (lanes engine; allocated on first use)
@@ -548,13 +549,43 @@ cudaError_t enqueue_lane_steps(slime_ensemble* e, uint32_t m) {
 }
 
 // Morton-reorder every colony's slots (results are unchanged: each slot keeps
-// its colony-local id).
+// its colony-local id).  With the lanes engine's lanes in place the colonies'
+// sorts run on four of them at once (largest first, each onto the lane with
+// the fewest agents so far), each of those lanes with its own sort scratch;
+// otherwise one after another on the ensemble's stream.
 int reorder_all(slime_ensemble* e) {
-    for (const Colony& c : e->colonies) {
-        if (c.n == 0) continue;
-        AgentsSoA a = colony_soa(e, c);
-        ECK(launch_reorder(a, c.W, c.H, e->reorder_cell_log2, e->reorder, e->stream), "reordering agents");
-        e->launches += 5;
+    const size_t nr = e->lanes.size() < 4 ? e->lanes.size() : 4;
+    if (e->engine == SLIME_ENSEMBLE_LANES && nr > 1) {
+        ECK(cudaEventRecord(e->fork_ev, e->stream), "forking reorders");
+        for (size_t l = 0; l < nr; l++) ECK(cudaStreamWaitEvent(e->lanes[l], e->fork_ev, 0), "forking reorders");
+        std::vector<uint32_t> order;
+        for (uint32_t j = 0; j < (uint32_t)e->colonies.size(); j++)
+            if (e->colonies[j].n) order.push_back(j);
+        std::stable_sort(order.begin(), order.end(),
+                         [&](uint32_t a, uint32_t b) { return e->colonies[a].n > e->colonies[b].n; });
+        std::vector<uint64_t> load(nr, 0);
+        for (uint32_t j : order) {
+            size_t l = 0;
+            for (size_t k = 1; k < nr; k++)
+                if (load[k] < load[l]) l = k;
+            load[l] += e->colonies[j].n;
+            const Colony& c = e->colonies[j];
+            AgentsSoA a = colony_soa(e, c);
+            ReorderScratch& scratch = l == 0 ? e->reorder : e->lane_reorder[l - 1];
+            ECK(launch_reorder(a, c.W, c.H, e->reorder_cell_log2, scratch, e->lanes[l]), "reordering agents");
+            e->launches += 5;
+        }
+        for (size_t l = 0; l < nr; l++) {
+            ECK(cudaEventRecord(e->lane_ev[l], e->lanes[l]), "joining reorders");
+            ECK(cudaStreamWaitEvent(e->stream, e->lane_ev[l], 0), "joining reorders");
+        }
+    } else {
+        for (const Colony& c : e->colonies) {
+            if (c.n == 0) continue;
+            AgentsSoA a = colony_soa(e, c);
+            ECK(launch_reorder(a, c.W, c.H, e->reorder_cell_log2, e->reorder, e->stream), "reordering agents");
+            e->launches += 5;
+        }
     }
     e->last_reorder_step = e->steps_done;
     return SLIME_OK;
@@ -863,7 +894,7 @@ void slime_ensemble_destroy(slime_ensemble* e) {
             if (c.tex[i]) cudaDestroyTextureObject(c.tex[i]);
     void* ptrs[] = {e->agent_block, e->ids, e->trail[0], e->trail[1], e->counts[0], e->counts[1], e->marks[0],
                     e->marks[1], e->d_cols, e->d_agent_items, e->d_strip_items, e->d_bar, e->staging,
-                    e->reorder.buf};
+                    e->reorder.buf, e->lane_reorder[0].buf, e->lane_reorder[1].buf, e->lane_reorder[2].buf};
     for (void* p : ptrs)
         if (p) dev_free(p);
     if (e->stream) cudaStreamDestroy(e->stream);
