@@ -692,14 +692,34 @@ SLM_FN float slm_jitter_hash(int32_t agent_index, float x, float y) {
     return slm_fract(slm_mul(s, 43758.5453f));
 }
 #if defined(__CUDACC__)
-/* Two jitter hashes, their sin polynomials as one packed pair; the same
- * bits as slm_jitter_hash for each. */
+/* The reductions of two hash arguments that are not both in the fixed
+ * window, each with its own range test, out of line. */
+typedef struct SlmRQ2 {
+    SlmRQ a, b;
+} SlmRQ2;
+static __device__ __noinline__ SlmRQ2 slm_reduce_pio2_hash2_cold(float x0, float x1) {
+    SlmRQ2 o;
+    slm_reduce_pio2_hash(x0, &o.a.r, &o.a.q);
+    slm_reduce_pio2_hash(x1, &o.b.r, &o.b.q);
+    return o;
+}
+
+/* Two jitter hashes, the same bits as slm_jitter_hash for each: one range
+ * test for both arguments (the fixed-window reduction inline when both are
+ * in it, the rest out of line), their sin polynomials as one packed pair. */
 static __device__ __forceinline__ void slm_jitter_hash2(int32_t i0, float x0, float y0, int32_t i1, float x1,
                                                         float y1, float* h0, float* h1) {
     float r0, r1, s0, c0, s1, c1;
     int q0, q1;
-    slm_reduce_pio2_hash(slm_jitter_arg(i0, x0, y0), &r0, &q0);
-    slm_reduce_pio2_hash(slm_jitter_arg(i1, x1, y1), &r1, &q1);
+    const float a0 = slm_jitter_arg(i0, x0, y0), a1 = slm_jitter_arg(i1, x1, y1);
+    const uint32_t e0 = ((slm_f2u_bits(a0) >> 23) & 0xffu) - 139u, e1 = ((slm_f2u_bits(a1) >> 23) & 0xffu) - 139u;
+    if (e0 <= 31u && e1 <= 31u) {
+        slm_reduce_pio2_win(a0, &r0, &q0);
+        slm_reduce_pio2_win(a1, &r1, &q1);
+    } else {
+        const SlmRQ2 o = slm_reduce_pio2_hash2_cold(a0, a1);
+        r0 = o.a.r, q0 = o.a.q, r1 = o.b.r, q1 = o.b.q;
+    }
     slm_sincos_rq2(r0, q0, r1, q1, &s0, &c0, &s1, &c1);
     *h0 = slm_fract(slm_mul(s0, 43758.5453f));
     *h1 = slm_fract(slm_mul(s1, 43758.5453f));
