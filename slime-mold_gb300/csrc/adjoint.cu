@@ -172,6 +172,8 @@ cudaError_t launch_adjoint_step(const DevParams& p, const float* T, const uint32
 
 void free_adjoint(slime_ctx* ctx) {
     auto& a = ctx->adj;
+    for (auto& kv : a.seg_graphs) cudaGraphExecDestroy(kv.second);
+    a.seg_graphs.clear();
     void* ptrs[] = {a.ckpt_agents, a.ckpt_ids, a.ckpt_trail, a.seg_trail, a.seg_counts, a.g[0], a.g[1],
                     a.acc, a.agents_tmp, a.ids_tmp};
     for (void* q : ptrs)
@@ -278,6 +280,44 @@ int slime_backward(slime_ctx* ctx, const float* dl_dtrail_final, SlimeGrads* gra
     tmp.ids = a.with_ids ? a.ids_tmp : nullptr;
     tmp.n = a.n;
     tmp.n_pad = a.n_pad;
+    // One segment after its restore: the replay of its m steps from the
+    // checkpoint (keeping T_s and k_s), then its m backward steps, starting
+    // from g[g0].  The same launches for every segment of m steps: captured
+    // once per (m, g0) as a CUDA graph and replayed.
+    auto enqueue_segment = [&](uint32_t m, int g0) -> cudaError_t {
+        cudaError_t ce = cudaSuccess;
+        for (uint32_t i = 0; i < m && ce == cudaSuccess; i++) {
+            float* Ti = a.seg_trail + (size_t)i * cells;
+            uint32_t* Ki = a.seg_counts + (size_t)i * cells;
+            ce = launch_agents(a.dev, tmp, Ti, Ki, ctx->stream, a.agent_shape);
+            if (ce == cudaSuccess && i + 1 < m) ce = launch_trail(a.dev, a.tile, Ti, Ki, Ti + cells, nullptr, ctx->stream);
+        }
+        int gi = g0;
+        for (int64_t i = (int64_t)m - 1; i >= 0 && ce == cudaSuccess; i--) {
+            ce = launch_adjoint_step(a.dev, a.seg_trail + (size_t)i * cells, a.seg_counts + (size_t)i * cells, a.g[gi],
+                                     a.g[1 - gi], a.acc, a.rate_active, ctx->stream);
+            gi = 1 - gi;
+        }
+        return ce;
+    };
+    auto segment_graph = [&](uint32_t m, int g0) -> cudaGraphExec_t {
+        auto key = std::make_pair(m, g0);
+        auto it = a.seg_graphs.find(key);
+        if (it != a.seg_graphs.end()) return it->second;
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) ce = enqueue_segment(m, g0);
+        cudaGraph_t graph = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(ctx->stream, &graph);
+        if (ce == cudaSuccess && ee == cudaSuccess) ee = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess || ee != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr; // the segment runs as direct launches
+        }
+        a.seg_graphs[key] = exec;
+        return exec;
+    };
     for (int64_t j = (int64_t)a.n_ckpt - 1; j >= 0; j--) {
         const uint32_t s0 = (uint32_t)j * K;
         const uint32_t m = (a.n_steps - s0) < K ? (a.n_steps - s0) : K;
@@ -290,23 +330,13 @@ int slime_backward(slime_ctx* ctx, const float* dl_dtrail_final, SlimeGrads* gra
         CK(cudaMemcpyAsync(a.seg_trail, a.ckpt_trail + (size_t)j * cells, cells * sizeof(float),
                            cudaMemcpyDeviceToDevice, ctx->stream), "restoring trail");
         CK(cudaMemsetAsync(a.seg_counts, 0, (size_t)m * cells * sizeof(uint32_t), ctx->stream), "clearing counts");
-        for (uint32_t i = 0; i < m; i++) {
-            float* Ti = a.seg_trail + (size_t)i * cells;
-            uint32_t* Ki = a.seg_counts + (size_t)i * cells;
-            CK(launch_agents(a.dev, tmp, Ti, Ki, ctx->stream, a.agent_shape), "replaying agents");
-            ctx->launches++;
-            if (i + 1 < m) {
-                CK(launch_trail(a.dev, a.tile, Ti, Ki, Ti + cells, nullptr, ctx->stream), "replaying trail");
-                ctx->launches++;
-            }
-        }
-        for (int64_t i = (int64_t)m - 1; i >= 0; i--) {
-            CK(launch_adjoint_step(a.dev, a.seg_trail + (size_t)i * cells, a.seg_counts + (size_t)i * cells,
-                                   a.g[cg], a.g[1 - cg], a.acc, a.rate_active, ctx->stream),
-               "adjoint step");
-            ctx->launches++;
-            cg = 1 - cg;
-        }
+        cudaGraphExec_t exec = segment_graph(m, cg);
+        if (exec)
+            CK(cudaGraphLaunch(exec, ctx->stream), "launching a backward segment");
+        else
+            CK(enqueue_segment(m, cg), "replaying a segment and its backward steps");
+        ctx->launches += (uint64_t)m * agent_pass_kernels(a.dev, a.n, false) + (m - 1) + m;
+        if (m & 1) cg = 1 - cg;
     }
     double acc[4];
     CK(cudaMemcpyAsync(acc, a.acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "reading gradients");

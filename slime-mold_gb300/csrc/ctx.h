@@ -103,6 +103,8 @@ struct slime_ctx {
         double* acc = nullptr;            // d_decay, d_rate, d_dep
         float* agents_tmp = nullptr;      // replay copy of the agents (4 * n_pad)
         uint32_t* ids_tmp = nullptr;
+        // captured segments (replay and backward steps) by (steps, g buffer)
+        std::map<std::pair<uint32_t, int>, cudaGraphExec_t> seg_graphs;
     } adj;
 
     std::string err;
